@@ -1,0 +1,210 @@
+/*
+ * ipic3d_gpu.h -- C ABI of the GB300 (sm_103a) particle hot path.
+ *
+ * Replaces the per-timestep loop of the AllScale iPIC3D reference,
+ *   template<P,F,M> simulateSteps(numSteps, Universe&)
+ *     code/app/include/ipic3d/app/simulator.h:42-47,127-242
+ * with its policy functors (simulator.h:244-276):
+ *   default_particle_mover      -> mover IPIC3D_MOVER_DIPOLE   (cell.h:896-964 + 975-1159)
+ *   default_field_solver        -> solver IPIC3D_SOLVER_STATIC (field.h:272-289)
+ *   leapfrog_field_solver       -> solver IPIC3D_SOLVER_LEAPFROG (field.h:342-402)
+ *   forward_field_solver        -> solver IPIC3D_SOLVER_FORWARD (field.h:294-337)
+ *   default_particle_to_field_projector -> projector IPIC3D_PROJECT_CIC (cell.h:787-824)
+ * and the migration mailboxes TransferBuffers (transfer_buffer.h:48-95) with
+ * importParticles (cell.h:1195-1310).
+ *
+ * One context = one Universe (universe.h:12-51) resident on one GPU:
+ * particles structure-of-arrays, grouped by cell, FP64 absolute or FP32
+ * cell-relative positions; fields FP64. All entry points are
+ * single-host-thread and ordered on the context's CUDA stream. Every call
+ * returns IPIC3D_OK (0) or a negative IPIC3D_E* status;
+ * ipic3d_gpu_last_error() describes the last failure. (The reference aborts
+ * through assert_* instead, e.g. cell.h:1309.)
+ */
+#ifndef IPIC3D_GPU_H
+#define IPIC3D_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "ipic3d_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IPIC3D_GPU_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------- */
+#define IPIC3D_OK 0
+#define IPIC3D_E_INVALID -1     /* bad argument / configuration            */
+#define IPIC3D_E_NOMEM -2       /* device or host allocation failed        */
+#define IPIC3D_E_CUDA -3        /* a CUDA runtime call failed              */
+#define IPIC3D_E_CAPACITY -4    /* particle storage full (grow and retry)  */
+#define IPIC3D_E_NODEVICE -5    /* no usable sm_103 device                 */
+#define IPIC3D_E_STATE -6       /* call out of order (e.g. no particles)   */
+
+/* ---- step configuration (the simulateSteps template arguments) ---------- */
+enum ipic3d_precision {
+    IPIC3D_FP64 = 0, /* absolute FP64 positions, reference arithmetic order   */
+    IPIC3D_FP32 = 1  /* FP32 cell-relative positions and velocities; FP64
+                        node accumulation, field update and reductions        */
+};
+
+enum ipic3d_mover {
+    /* moveParticles (cell.h:896-964): analytic Earth dipole at the origin,
+       E = 0, adaptive sub-cycling (<= 100). The field grid is not read.      */
+    IPIC3D_MOVER_DIPOLE = 0,
+    /* field-gather mover of the commented code at cell.h:905-937: trilinear
+       interpolation of node E and B (trilinearInterpolationF2P, cell.h:867),
+       same sub-cycling rule; IPIC3D_F_DIPOLE_IN_GATHER adds the analytic
+       dipole B.                                                              */
+    IPIC3D_MOVER_FIELD = 1
+};
+
+enum ipic3d_solver {
+    IPIC3D_SOLVER_STATIC = 0,   /* solveFieldStatically: no-op (field.h:272)  */
+    IPIC3D_SOLVER_LEAPFROG = 1, /* solveFieldLeapfrog, E then Bc (field.h:342) */
+    IPIC3D_SOLVER_FORWARD = 2   /* solveFieldForward, E, Bc, node B (field.h:294) */
+};
+
+enum ipic3d_projector {
+    IPIC3D_PROJECT_NONE = 0, /* the reference's active loop (simulator.h:189) */
+    IPIC3D_PROJECT_CIC = 1   /* cloud-in-cell J (cell.h:787-824) and rho     */
+};
+
+/* particle boundary of one domain face */
+enum ipic3d_boundary {
+    IPIC3D_BC_REFLECT = 0,  /* exportParticles' wall rule (cell.h:1102-1121):
+                               shift by half a cell width, negate velocity   */
+    IPIC3D_BC_PERIODIC = 1, /* wrap around (both faces of the axis)          */
+    IPIC3D_BC_OPEN = 2      /* outflow: the particle is removed             */
+};
+
+/* flags */
+#define IPIC3D_F_J_DIV8 (1u << 0)          /* J = Js/vol/8 as cell.h:823 (else Js/vol) */
+#define IPIC3D_F_GATHER_DIV_VOL (1u << 1)  /* trilinear result / vol as cell.h:884     */
+#define IPIC3D_F_DIPOLE_IN_GATHER (1u << 2)/* FIELD mover adds the analytic dipole B   */
+#define IPIC3D_F_REFRESH_NODE_B (1u << 3)  /* after LEAPFROG, node B = interpC2N(Bc)   */
+#define IPIC3D_F_TRACK_IDS (1u << 4)       /* keep a 32-bit id per particle            */
+#define IPIC3D_F_INJECT_LOW_X (1u << 5)    /* inject a drifting Maxwellian at -x face  */
+#define IPIC3D_F_USE_GRAPH (1u << 6)       /* run multi-step calls as a CUDA graph     */
+
+typedef struct ipic3d_config {
+    int32_t precision;      /* enum ipic3d_precision */
+    int32_t mover;          /* enum ipic3d_mover     */
+    int32_t solver;         /* enum ipic3d_solver    */
+    int32_t projector;      /* enum ipic3d_projector */
+    int32_t bc_low[3];      /* enum ipic3d_boundary, faces x=0, y=0, z=0   */
+    int32_t bc_high[3];     /* enum ipic3d_boundary, faces x=L, y=L, z=L   */
+    uint32_t flags;         /* IPIC3D_F_*                                  */
+    /* storage: per-cell slack (fraction of the particles uploaded into the
+       cell, plus `slack_min` slots) reserved for arrivals; 0 = defaults.     */
+    double slack;
+    int32_t slack_min;
+    int32_t block_size;     /* 0 = autotuned launch shape                  */
+    /* injection at the x=0 face (IPIC3D_F_INJECT_LOW_X, bc_low[0] OPEN):
+       expected particles per face cell per step, their q, qom, drift and
+       thermal velocities, and the seed of the counter-based generator.      */
+    double inject_per_cell;
+    double inject_q, inject_qom;
+    double inject_drift[3];
+    double inject_vth[3];
+    uint64_t seed;
+    uint64_t reserved[8];
+} ipic3d_config;
+
+/* Fills a config with the reference's defaults: FP64, dipole mover, static
+ * solver, no projection, reflecting walls, no flags (simulator.h:42-47). */
+void ipic3d_gpu_config_default(ipic3d_config* cfg);
+
+typedef struct ipic3d_ctx ipic3d_ctx;
+
+/* ---- lifetime ------------------------------------------------------------ */
+/* Creates a context on the current CUDA device with the Universe's properties
+ * (Universe(properties), universe.h:36). Fields start at zero. */
+int ipic3d_gpu_create(const ipic3d_props* props, const ipic3d_config* cfg, ipic3d_ctx** out);
+int ipic3d_gpu_destroy(ipic3d_ctx* ctx);
+
+/* ---- state transfer (host memory) --------------------------------------- */
+/* Uploads the particles of Universe::cells (cell.h:31-38): n particles
+ * grouped by cell in row-major cell order, cell_counts[ncells] of them per
+ * cell. ids may be NULL (then ids are the input indices when tracking).
+ * Replaces all particles. Capacity = n plus the configured slack. */
+int ipic3d_gpu_upload_particles(ipic3d_ctx* ctx, const ipic3d_particle* particles, const uint64_t* cell_counts,
+                                const uint32_t* ids);
+/* Reserves room for at least `n` particles (allocation happens here, not in
+ * ipic3d_gpu_step). */
+int ipic3d_gpu_reserve(ipic3d_ctx* ctx, uint64_t n);
+/* Number of particles currently stored. */
+int ipic3d_gpu_particle_count(ipic3d_ctx* ctx, uint64_t* n);
+/* Downloads particles grouped by cell (row-major) with per-cell counts; the
+ * order inside a cell is unspecified. `capacity` = entries in particles/ids;
+ * cell_counts and ids may be NULL. */
+int ipic3d_gpu_download_particles(ipic3d_ctx* ctx, ipic3d_particle* particles, uint64_t capacity,
+                                  uint64_t* cell_counts, uint32_t* ids);
+/* Per-cell particle counts (outputNumberOfParticlesPerCell, cell.h:1360). */
+int ipic3d_gpu_cell_counts(ipic3d_ctx* ctx, uint64_t* cell_counts);
+
+/* Field grids in the reference layout (ipic3d_types.h); any pointer may be
+ * NULL to skip that grid. rho is (size+1)^3 doubles (download only). */
+int ipic3d_gpu_upload_fields(ipic3d_ctx* ctx, const double* field, const double* bcfield, const double* density);
+int ipic3d_gpu_download_fields(ipic3d_ctx* ctx, double* field, double* bcfield, double* density, double* rho);
+
+/* ---- the timestep ------------------------------------------------------- */
+/* simulateSteps(numSteps, universe) (simulator.h:127-242) with the policies
+ * of the context's config: per step
+ *   projector (J, rho) -> updateFieldsOnBoundaries -> field solver
+ *   -> mover + export -> import (-> injection)
+ * Asynchronous: returns once the work is enqueued. */
+int ipic3d_gpu_step(ipic3d_ctx* ctx, uint64_t num_steps);
+/* Single phases, for the reference's per-function tests:
+ * projectToDensityField over all nodes (cell.h:787-824) into J (and rho). */
+int ipic3d_gpu_project(ipic3d_ctx* ctx);
+/* updateFieldsOnBoundaries (field.h:407-440). */
+int ipic3d_gpu_update_boundaries(ipic3d_ctx* ctx);
+/* the configured field solver over [1, size+2)^3 (simulator.h:207-209). */
+int ipic3d_gpu_solve_fields(ipic3d_ctx* ctx);
+/* mover + export + import for every cell (simulator.h:214-223). */
+int ipic3d_gpu_move(ipic3d_ctx* ctx);
+
+/* Conserved quantities (simulator.h:76-83) computed on the device with
+ * compensated FP64 sums. Synchronous. */
+int ipic3d_gpu_conserved(ipic3d_ctx* ctx, ipic3d_conserved* out);
+/* Waits for all work on the context's stream. */
+int ipic3d_gpu_synchronize(ipic3d_ctx* ctx);
+/* The context's CUDA stream (a cudaStream_t) for callers that order their
+ * own work after the step. */
+void* ipic3d_gpu_stream(ipic3d_ctx* ctx);
+
+/* ---- counters ------------------------------------------------------------ */
+typedef struct ipic3d_stats {
+    uint64_t steps;             /* steps executed                          */
+    uint64_t particles;         /* particles stored                        */
+    uint64_t capacity;          /* particle slots allocated                */
+    uint64_t migrated_last;     /* particles that changed cell, last step  */
+    uint64_t removed_last;      /* particles removed (planet/outflow)      */
+    uint64_t injected_last;     /* particles injected, last step           */
+    uint64_t rebuilds;          /* storage re-layouts (overflow of a cell) */
+    uint64_t kernel_launches;   /* kernels launched by this context        */
+} ipic3d_stats;
+int ipic3d_gpu_stats(ipic3d_ctx* ctx, ipic3d_stats* out);
+
+/* ---- element kernels (the reference's unit-level functions) ------------- */
+/* Particle::updateVelocity + updatePosition (particle.h:24-49) applied
+ * nsteps times to n host particles with uniform E, B: the Boris KATs
+ * (particle_test.cc:45-81, simulation_test.cc:237-246). push_position = 0
+ * applies only updateVelocity. */
+int ipic3d_gpu_boris(ipic3d_particle* particles, uint64_t n, const double E[3], const double B[3], double dt,
+                     uint64_t nsteps, int push_position);
+
+/* ---- errors -------------------------------------------------------------- */
+/* Copies the message of the last failure on this thread into buf. Returns
+ * the last status. */
+int ipic3d_gpu_last_error(char* buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* IPIC3D_GPU_H */
