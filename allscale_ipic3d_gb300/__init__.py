@@ -1,0 +1,231 @@
+"""GB300 (sm_103a) implementation of the AllScale iPIC3D per-timestep particle
+path: the Boris mover, cloud-in-cell projection of charge and current,
+particle migration between cells and the field update.
+
+The compute path is the CUDA library ``_lib/libipic3d_gb300.so`` behind the
+C ABI of ``include/ipic3d_gpu.h``; this module binds it with ctypes and offers
+``Simulation``, a host-side mirror of the reference's ``Universe`` plus
+``simulateSteps`` (code/app/include/ipic3d/app/universe.h:12-51,
+simulator.h:127-242). There is no CPU fallback: without the library (or
+without an sm_103 GPU) every call raises ``GpuPathError``.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .abi import (BC_OPEN, BC_PERIODIC, BC_REFLECT, FP32, FP64, MOVER_DIPOLE, MOVER_FIELD, PARTICLE_DTYPE,
+                  PROJECT_CIC, PROJECT_NONE, SOLVER_FORWARD, SOLVER_LEAPFROG, SOLVER_STATIC, Config, Conserved,
+                  Props, Stats)
+
+__all__ = ["Simulation", "Props", "Config", "Conserved", "Stats", "PARTICLE_DTYPE", "GpuPathError", "library",
+           "library_path", "boris", "EXPORTED_SYMBOLS"]
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def library_path():
+    return os.path.join(HERE, "_lib", "libipic3d_gb300.so")
+
+
+class GpuPathError(RuntimeError):
+    """A failed call of the CUDA path (status code and the library's message)."""
+
+    def __init__(self, status, message):
+        super().__init__("ipic3d_gpu status %d: %s" % (status, message))
+        self.status = status
+
+
+# every entry point of include/ipic3d_gpu.h: (name, restype, argtypes)
+_vp = C.c_void_p
+_SIGNATURES = [
+    ("ipic3d_gpu_config_default", None, [_vp]),
+    ("ipic3d_gpu_create", C.c_int, [_vp, _vp, C.POINTER(_vp)]),
+    ("ipic3d_gpu_destroy", C.c_int, [_vp]),
+    ("ipic3d_gpu_upload_particles", C.c_int, [_vp, _vp, _vp, _vp]),
+    ("ipic3d_gpu_reserve", C.c_int, [_vp, C.c_uint64]),
+    ("ipic3d_gpu_particle_count", C.c_int, [_vp, C.POINTER(C.c_uint64)]),
+    ("ipic3d_gpu_download_particles", C.c_int, [_vp, _vp, C.c_uint64, _vp, _vp]),
+    ("ipic3d_gpu_cell_counts", C.c_int, [_vp, _vp]),
+    ("ipic3d_gpu_upload_fields", C.c_int, [_vp, _vp, _vp, _vp]),
+    ("ipic3d_gpu_download_fields", C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    ("ipic3d_gpu_step", C.c_int, [_vp, C.c_uint64]),
+    ("ipic3d_gpu_project", C.c_int, [_vp]),
+    ("ipic3d_gpu_update_boundaries", C.c_int, [_vp]),
+    ("ipic3d_gpu_solve_fields", C.c_int, [_vp]),
+    ("ipic3d_gpu_move", C.c_int, [_vp]),
+    ("ipic3d_gpu_conserved", C.c_int, [_vp, _vp]),
+    ("ipic3d_gpu_synchronize", C.c_int, [_vp]),
+    ("ipic3d_gpu_stream", _vp, [_vp]),
+    ("ipic3d_gpu_stats", C.c_int, [_vp, _vp]),
+    ("ipic3d_gpu_boris", C.c_int, [_vp, C.c_uint64, _vp, _vp, C.c_double, C.c_uint64, C.c_int]),
+    ("ipic3d_gpu_last_error", C.c_int, [C.c_char_p, C.c_size_t]),
+]
+EXPORTED_SYMBOLS = [s[0] for s in _SIGNATURES]
+
+_lib = None
+
+
+def library(build_if_missing=False):
+    """The loaded CUDA library (ctypes.CDLL). Raises GpuPathError if absent."""
+    global _lib
+    if _lib is None:
+        path = library_path()
+        if not os.path.exists(path):
+            if build_if_missing:
+                from .build import build
+                build()
+            else:
+                raise GpuPathError(-5, "CUDA library %s is not built (run __graft_entry__.build())" % path)
+        lib = C.CDLL(path)
+        for name, res, args in _SIGNATURES:
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        buf = C.create_string_buffer(512)
+        library().ipic3d_gpu_last_error(buf, 512)
+        raise GpuPathError(rc, buf.value.decode(errors="replace"))
+
+
+def boris(particles, E, B, dt, nsteps=1, push_position=True):
+    """Particle::updateVelocity (+ updatePosition) applied nsteps times on the
+    GPU (particle.h:24-49); `particles` is a PARTICLE_DTYPE array, modified in
+    place."""
+    p = np.ascontiguousarray(particles, dtype=PARTICLE_DTYPE)
+    e = np.asarray(E, dtype=np.float64)
+    b = np.asarray(B, dtype=np.float64)
+    _check(library().ipic3d_gpu_boris(abi.vptr(p), len(p), abi.vptr(e), abi.vptr(b), float(dt), int(nsteps),
+                                      1 if push_position else 0))
+    if p is not particles:
+        particles[...] = p
+    return particles
+
+
+class Simulation:
+    """One Universe resident on the GPU.
+
+    ``props`` mirrors UniverseProperties (universe_properties.h:52-123) and
+    ``config`` the simulateSteps policies (simulator.h:42-47,244-276).
+    """
+
+    def __init__(self, props, config=None):
+        self.props = props
+        self.config = config if config is not None else Config.make()
+        lib = library()
+        ctx = C.c_void_p()
+        _check(lib.ipic3d_gpu_create(C.byref(self.props), C.byref(self.config), C.byref(ctx)))
+        self._ctx = ctx
+        self.ncells = props.ncells
+
+    # -- lifetime --
+    def close(self):
+        if getattr(self, "_ctx", None):
+            library().ipic3d_gpu_destroy(self._ctx)
+            self._ctx = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- particles --
+    def upload_particles(self, particles, cell_counts, ids=None):
+        """Universe::cells: particles grouped by cell (row-major), with the
+        number per cell."""
+        p = np.ascontiguousarray(particles, dtype=PARTICLE_DTYPE)
+        c = np.ascontiguousarray(cell_counts, dtype=np.uint64).reshape(-1)
+        if c.size != self.ncells:
+            raise ValueError("cell_counts has %d entries, grid has %d cells" % (c.size, self.ncells))
+        if int(c.sum()) != len(p):
+            raise ValueError("cell_counts sum to %d but %d particles given" % (int(c.sum()), len(p)))
+        i = None if ids is None else np.ascontiguousarray(ids, dtype=np.uint32)
+        _check(library().ipic3d_gpu_upload_particles(self._ctx, abi.vptr(p), abi.vptr(c), abi.vptr(i)))
+
+    def particle_count(self):
+        n = C.c_uint64()
+        _check(library().ipic3d_gpu_particle_count(self._ctx, C.byref(n)))
+        return n.value
+
+    def download_particles(self):
+        """(particles, cell_counts, ids) grouped by cell; order inside a cell
+        is unspecified."""
+        n = self.particle_count()
+        p = np.zeros(n, PARTICLE_DTYPE)
+        c = np.zeros(self.ncells, np.uint64)
+        i = np.zeros(n, np.uint32)
+        _check(library().ipic3d_gpu_download_particles(self._ctx, abi.vptr(p), n, abi.vptr(c), abi.vptr(i)))
+        return p, c, i
+
+    def cell_counts(self):
+        c = np.zeros(self.ncells, np.uint64)
+        _check(library().ipic3d_gpu_cell_counts(self._ctx, abi.vptr(c)))
+        return c
+
+    # -- fields --
+    def upload_fields(self, field=None, bcfield=None, density=None):
+        f = None if field is None else np.ascontiguousarray(field, np.float64)
+        b = None if bcfield is None else np.ascontiguousarray(bcfield, np.float64)
+        d = None if density is None else np.ascontiguousarray(density, np.float64)
+        if f is not None:
+            assert f.size == np.prod(abi.field_shape(self.props))
+        if b is not None:
+            assert b.size == np.prod(abi.bcfield_shape(self.props))
+        if d is not None:
+            assert d.size == np.prod(abi.density_shape(self.props))
+        _check(library().ipic3d_gpu_upload_fields(self._ctx, abi.vptr(f), abi.vptr(b), abi.vptr(d)))
+
+    def download_fields(self):
+        f = np.zeros(abi.field_shape(self.props))
+        b = np.zeros(abi.bcfield_shape(self.props))
+        d = np.zeros(abi.density_shape(self.props))
+        r = np.zeros(abi.density_shape(self.props)[:3])
+        _check(library().ipic3d_gpu_download_fields(self._ctx, abi.vptr(f), abi.vptr(b), abi.vptr(d), abi.vptr(r)))
+        return f, b, d, r
+
+    # -- the timestep --
+    def step(self, n=1):
+        """simulateSteps(n, universe) (simulator.h:127-242)."""
+        _check(library().ipic3d_gpu_step(self._ctx, int(n)))
+
+    def project(self):
+        _check(library().ipic3d_gpu_project(self._ctx))
+
+    def update_boundaries(self):
+        _check(library().ipic3d_gpu_update_boundaries(self._ctx))
+
+    def solve_fields(self):
+        _check(library().ipic3d_gpu_solve_fields(self._ctx))
+
+    def move(self):
+        _check(library().ipic3d_gpu_move(self._ctx))
+
+    def synchronize(self):
+        _check(library().ipic3d_gpu_synchronize(self._ctx))
+
+    def conserved(self):
+        out = Conserved()
+        _check(library().ipic3d_gpu_conserved(self._ctx, C.byref(out)))
+        return out.as_dict()
+
+    def stats(self):
+        out = Stats()
+        _check(library().ipic3d_gpu_stats(self._ctx, C.byref(out)))
+        return out.as_dict()
+
+    @property
+    def stream(self):
+        return library().ipic3d_gpu_stream(self._ctx)

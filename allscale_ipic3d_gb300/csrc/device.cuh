@@ -1,0 +1,125 @@
+// Device-side data structures and helpers of the GB300 particle path.
+//
+// One "universe" (the reference's Universe, universe.h:12-51) lives in HBM as
+//   * FP64 field grids in the reference layout (field.h:14-38):
+//       field   (s+3)^3 x {E,B,Bext}     bcfield (s+2)^3 x Bc
+//       J       (s+1)^3 x 3              rho     (s+1)^3
+//   * one or more particle populations (one per distinct (q, qom) pair),
+//     each a structure-of-arrays grouped by cell: cell c owns the slot range
+//     [start[c], start[c+1]); its first count[c] slots hold particles, the
+//     rest is slack for arrivals. start[] is a multiple of 4 so that four
+//     consecutive slots always belong to one cell (one 128-bit vector load
+//     per array and thread).
+//   * FP64 populations store absolute positions (Particle::position,
+//     particle.h:11); FP32 populations store the position relative to the
+//     cell origin in units of the cell width, in [0, 1] when inside.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ipg {
+
+constexpr int kVec = 4;                 // particles per thread (one float4 / 2x double2)
+constexpr int kPushThreads = 256;       // threads per CTA of the push kernel
+constexpr int kSlotsPerCta = kVec * kPushThreads;
+constexpr int kMaxCellsPerCta = kSlotsPerCta / 4 + 2;  // caps are >= 4 slots
+
+// Geometry and physics of one universe (UniverseProperties plus the policy).
+struct Geom {
+    int sx, sy, sz;
+    int ncells;
+    double w[3], inv_w[3], half_w[3];
+    double origin[3];
+    double object_center[3];
+    double L[3];            // domain length per axis
+    double dt, c;
+    double planet_r2;       // planetRadius * planetRadius (cell.h:1126)
+    double mft;             // -Bext.z * pow(R, 3), host glibc pow (cell.h:923)
+    double vol;             // w.x * w.y * w.z
+    int bc_lo[3], bc_hi[3];
+    uint32_t flags;
+    int mover;              // 0 dipole, 1 field gather
+    int deposit;            // 1 = deposit J/rho of the moved particles
+    double* field;          // (s+3)^3 x 9
+    double* bcfield;        // (s+2)^3 x 3
+    double* J;              // (s+1)^3 x 3 raw sums during the deposit
+    double* rho;            // (s+1)^3
+    const float4* node32;   // (s+3)^3 x 2 float4: {Ex,Ey,Ez,0},{Bx,By,Bz,0} (FP32 gather)
+};
+
+// A particle that leaves its slot (migration) or waits for a slot (pending).
+template <typename T>
+struct Mover {
+    int32_t cell;           // destination cell (for pending: the cell it is in)
+    uint32_t id;
+    T x, y, z, u, v, w;
+};
+
+// Step-global counters, reset at the start of every step.
+struct StepCounters {
+    uint32_t outbox;        // entries written to the outbox this step
+    uint32_t pending_out;   // arrivals that found no slot -> pending next step
+    uint32_t deferred;      // leavers kept in their slot (outbox full)
+    uint32_t removed;       // particles removed (planet, open faces)
+    uint32_t migrated;      // particles that changed cell
+    uint32_t injected;
+    uint32_t lost;          // pending list overflow (must stay 0)
+    uint32_t pad;
+};
+
+template <typename T>
+struct Pop {
+    T *x, *y, *z, *u, *v, *w;
+    uint32_t* id;           // nullable
+    const int64_t* start;   // [ncells + 1]
+    int32_t* count;         // [ncells]
+    int32_t* hole_cnt;      // [ncells]
+    int32_t* hole_list;     // [capacity] holes of cell c at start[c] + k
+    int32_t* arr_cnt;       // [ncells]
+    int32_t* arr_list;      // [capacity] arrivals of cell c at start[c] + k (outbox index)
+    Mover<T>* outbox;
+    uint32_t outbox_cap;
+    Mover<T>* pending_in;   // pushed this step
+    Mover<T>* pending_out;  // arrivals without a slot this step
+    uint32_t pending_cap;
+    const uint32_t* pending_in_count;
+    StepCounters* ctr;
+    int64_t capacity;       // total slots
+    double q, qom;
+};
+
+// ---- small helpers --------------------------------------------------------
+
+__device__ __forceinline__ int64_t field_index(const Geom& g, int x, int y, int z) {
+    return ((int64_t)x * (g.sy + 3) + y) * (g.sz + 3) + z;
+}
+__device__ __forceinline__ int64_t bc_index(const Geom& g, int x, int y, int z) {
+    return ((int64_t)x * (g.sy + 2) + y) * (g.sz + 2) + z;
+}
+__device__ __forceinline__ int64_t node_index(const Geom& g, int x, int y, int z) {
+    return ((int64_t)x * (g.sy + 1) + y) * (g.sz + 1) + z;
+}
+__device__ __forceinline__ void cell_coords(const Geom& g, int c, int& x, int& y, int& z) {
+    z = c % g.sz;
+    int t = c / g.sz;
+    y = t % g.sy;
+    x = t / g.sy;
+}
+__device__ __forceinline__ int cell_id(const Geom& g, int x, int y, int z) { return (x * g.sy + y) * g.sz + z; }
+
+// Warp-aggregated atomic increment: one atomic per warp for all active
+// lanes with pred set; returns this lane's slot (or undefined if !pred).
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
+    unsigned mask = __activemask();
+    unsigned ballot = __ballot_sync(mask, pred);
+    if (!ballot) return 0;
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(ballot) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(ballot));
+    base = __shfl_sync(mask, base, leader);
+    return base + __popc(ballot & ((1u << lane) - 1));
+}
+
+}  // namespace ipg

@@ -1,0 +1,416 @@
+// Field-grid kernels of the GB300 path (FP64, built with -fmad=false so every
+// expression rounds as the reference's does).
+//
+//   k_ghost        updateFieldsOnBoundaries (field.h:407-440)
+//   k_leapfrog_e   solveFieldLeapfrog, E part   (field.h:359-363)
+//   k_leapfrog_b   solveFieldLeapfrog, Bc part  (field.h:366-372)
+//   k_forward_e/b  solveFieldForward            (field.h:294-337, curls 162-229)
+//   k_interp_c2n   interpC2N                    (field.h:234-247)
+//   k_j_finalize   J = (Js / vol) / 8           (cell.h:822-823) plus the
+//                  periodic duplicate nodes of the gather form (cell.h:799-805)
+//   k_node32       FP32 copy of node E, B for the FP32 gather
+//   reductions     getFieldEnergy (field.h:443-459), particle sums
+//                  (cell.h:1315-1355), Neumaier-compensated
+//
+// The reference's per-node solver updates E and then Bc in one in-place pass
+// whose result depends on the visiting order; here E is updated everywhere
+// first and Bc afterwards (the order-independent two-phase reading).
+#include "launch.h"
+
+namespace ipg {
+
+namespace {
+
+__device__ __forceinline__ int64_t fidx(int n, int x, int y, int z) { return ((int64_t)x * n + y) * n + z; }
+
+// Copies the six ghost faces of a cubic grid of n^3 records of `per` doubles:
+// index (a, b) in [1, n-1)^2 of each face (edges and corners stay).
+__global__ void k_ghost(double* g, int n, int per) {
+    const int end = n - 1;
+    const int64_t m = (int64_t)(end - 1) * (end - 1);
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m * per; t += (int64_t)gridDim.x * blockDim.x) {
+        const int comp = (int)(t % per);
+        const int64_t ab = t / per;
+        const int a = 1 + (int)(ab / (end - 1)), b = 1 + (int)(ab % (end - 1));
+        g[fidx(n, 0, a, b) * per + comp] = g[fidx(n, end - 1, a, b) * per + comp];
+        g[fidx(n, end, a, b) * per + comp] = g[fidx(n, 1, a, b) * per + comp];
+        g[fidx(n, a, 0, b) * per + comp] = g[fidx(n, a, end - 1, b) * per + comp];
+        g[fidx(n, a, end, b) * per + comp] = g[fidx(n, a, 1, b) * per + comp];
+        g[fidx(n, a, b, 0) * per + comp] = g[fidx(n, a, b, end - 1) * per + comp];
+        g[fidx(n, a, b, end) * per + comp] = g[fidx(n, a, b, 1) * per + comp];
+    }
+}
+
+struct SolverArgs {
+    int s;                // cells per axis (cubic)
+    double dt, c;
+    double wx, wy, wz;
+    double* field;        // (s+3)^3 x 9
+    double* bc;           // (s+2)^3 x 3
+    const double* J;      // (s+1)^3 x 3
+};
+
+// E at pos in [1, s+2)^3 from Bc(pos), Bc(pos - e_i) and J(pos - 1).
+__global__ void k_leapfrog_e(SolverArgs A) {
+    const int n = A.s + 1;  // nodes per axis in the updated box
+    const int64_t total = (int64_t)n * n * n;
+    const double c2 = A.c * A.c;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int x = 1 + (int)(t / ((int64_t)n * n)), y = 1 + (int)((t / n) % n), z = 1 + (int)(t % n);
+        const int nb = A.s + 2, nf = A.s + 3, nd = A.s + 1;
+        const double* B0 = A.bc + 3 * fidx(nb, x, y, z);
+        const double* Bxm = A.bc + 3 * fidx(nb, x - 1, y, z);
+        const double* Bym = A.bc + 3 * fidx(nb, x, y - 1, z);
+        const double* Bzm = A.bc + 3 * fidx(nb, x, y, z - 1);
+        const double* J = A.J + 3 * fidx(nd, x - 1, y - 1, z - 1);
+        double* E = A.field + 9 * fidx(nf, x, y, z);
+        E[0] = E[0] + A.dt * (c2 * ((B0[2] - Bym[2]) / A.wy - (B0[1] - Bzm[1]) / A.wz) - J[0]);
+        E[1] = E[1] + A.dt * (c2 * ((B0[0] - Bzm[0]) / A.wz - (B0[2] - Bxm[2]) / A.wx) - J[1]);
+        E[2] = E[2] + A.dt * (c2 * ((B0[1] - Bxm[1]) / A.wx - (B0[0] - Bym[0]) / A.wy) - J[2]);
+    }
+}
+
+// Bc at pos in [1, s+1)^3 from the new E at pos and pos + e_i.
+__global__ void k_leapfrog_b(SolverArgs A) {
+    const int n = A.s;
+    const int64_t total = (int64_t)n * n * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int x = 1 + (int)(t / ((int64_t)n * n)), y = 1 + (int)((t / n) % n), z = 1 + (int)(t % n);
+        const int nb = A.s + 2, nf = A.s + 3;
+        const double* E0 = A.field + 9 * fidx(nf, x, y, z);
+        const double* Ex = A.field + 9 * fidx(nf, x + 1, y, z);
+        const double* Ey = A.field + 9 * fidx(nf, x, y + 1, z);
+        const double* Ez = A.field + 9 * fidx(nf, x, y, z + 1);
+        double* B = A.bc + 3 * fidx(nb, x, y, z);
+        B[0] = B[0] - A.dt * ((Ey[2] - E0[2]) / A.wy - (Ez[1] - E0[1]) / A.wz);
+        B[1] = B[1] - A.dt * ((Ez[0] - E0[0]) / A.wz - (Ex[2] - E0[2]) / A.wx);
+        B[2] = B[2] - A.dt * ((Ex[1] - E0[1]) / A.wx - (Ey[0] - E0[0]) / A.wy);
+    }
+}
+
+// computeCurlB (field.h:162-193) at node pos from the 8 Bc at pos - (i,j,k).
+__device__ __forceinline__ void curl_b(const SolverArgs& A, int x, int y, int z, double& cx, double& cy, double& cz) {
+    const int nb = A.s + 2;
+    double b[2][2][2][3];
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 2; j++)
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                const double* p = A.bc + 3 * fidx(nb, x - i, y - j, z - k);
+                b[i][j][k][0] = p[0]; b[i][j][k][1] = p[1]; b[i][j][k][2] = p[2];
+            }
+    // d/dy of z: (j=0) - (j=1) over the 4 (i,k); d/dz of y: (k=0) - (k=1); ...
+    double zdy = .25 * (b[0][0][0][2] - b[0][1][0][2] + b[0][0][1][2] - b[0][1][1][2] + b[1][0][0][2] - b[1][1][0][2] + b[1][0][1][2] - b[1][1][1][2]) / A.wy;
+    double ydz = .25 * (b[0][0][0][1] - b[0][0][1][1] + b[1][0][0][1] - b[1][0][1][1] + b[0][1][0][1] - b[0][1][1][1] + b[1][1][0][1] - b[1][1][1][1]) / A.wz;
+    cx = zdy - ydz;
+    double xdz = .25 * (b[0][0][0][0] - b[0][0][1][0] + b[1][0][0][0] - b[1][0][1][0] + b[0][1][0][0] - b[0][1][1][0] + b[1][1][0][0] - b[1][1][1][0]) / A.wz;
+    double zdx = .25 * (b[0][0][0][2] - b[1][0][0][2] + b[0][0][1][2] - b[1][0][1][2] + b[0][1][0][2] - b[1][1][0][2] + b[0][1][1][2] - b[1][1][1][2]) / A.wx;
+    cy = xdz - zdx;
+    double ydx = .25 * (b[0][0][0][1] - b[1][0][0][1] + b[0][0][1][1] - b[1][0][1][1] + b[0][1][0][1] - b[1][1][0][1] + b[0][1][1][1] - b[1][1][1][1]) / A.wx;
+    double xdy = .25 * (b[0][0][0][0] - b[0][1][0][0] + b[0][0][1][0] - b[0][1][1][0] + b[1][0][0][0] - b[1][1][0][0] + b[1][0][1][0] - b[1][1][1][0]) / A.wy;
+    cz = ydx - xdy;
+}
+
+// computeCurlE (field.h:198-229) at centre pos from the 8 node E at pos + (i,j,k).
+__device__ __forceinline__ void curl_e(const SolverArgs& A, int x, int y, int z, double& cx, double& cy, double& cz) {
+    const int nf = A.s + 3;
+    double e[2][2][2][3];
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 2; j++)
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                const double* p = A.field + 9 * fidx(nf, x + i, y + j, z + k);
+                e[i][j][k][0] = p[0]; e[i][j][k][1] = p[1]; e[i][j][k][2] = p[2];
+            }
+    double zdy = .25 * (e[0][1][0][2] - e[0][0][0][2] + e[0][1][1][2] - e[0][0][1][2] + e[1][1][0][2] - e[1][0][0][2] + e[1][1][1][2] - e[1][0][1][2]) / A.wy;
+    double ydz = .25 * (e[0][0][1][1] - e[0][0][0][1] + e[1][0][1][1] - e[1][0][0][1] + e[0][1][1][1] - e[0][1][0][1] + e[1][1][1][1] - e[1][1][0][1]) / A.wz;
+    cx = zdy - ydz;
+    double xdz = .25 * (e[0][0][1][0] - e[0][0][0][0] + e[1][0][1][0] - e[1][0][0][0] + e[0][1][1][0] - e[0][1][0][0] + e[1][1][1][0] - e[1][1][0][0]) / A.wz;
+    double zdx = .25 * (e[1][0][0][2] - e[0][0][0][2] + e[1][0][1][2] - e[0][0][1][2] + e[1][1][0][2] - e[0][1][0][2] + e[1][1][1][2] - e[0][1][1][2]) / A.wx;
+    cy = xdz - zdx;
+    double ydx = .25 * (e[1][0][0][1] - e[0][0][0][1] + e[1][0][1][1] - e[0][0][1][1] + e[1][1][0][1] - e[0][1][0][1] + e[1][1][1][1] - e[0][1][1][1]) / A.wx;
+    double xdy = .25 * (e[0][1][0][0] - e[0][0][0][0] + e[0][1][1][0] - e[0][0][1][0] + e[1][1][0][0] - e[1][0][0][0] + e[1][1][1][0] - e[1][0][1][0]) / A.wy;
+    cz = ydx - xdy;
+}
+
+__global__ void k_forward_e(SolverArgs A) {
+    const int n = A.s + 1;
+    const int64_t total = (int64_t)n * n * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int x = 1 + (int)(t / ((int64_t)n * n)), y = 1 + (int)((t / n) % n), z = 1 + (int)(t % n);
+        double cx, cy, cz;
+        curl_b(A, x, y, z, cx, cy, cz);
+        const double* J = A.J + 3 * fidx(A.s + 1, x - 1, y - 1, z - 1);
+        double* E = A.field + 9 * fidx(A.s + 3, x, y, z);
+        E[0] += (A.c * cx - J[0]) * A.dt;
+        E[1] += (A.c * cy - J[1]) * A.dt;
+        E[2] += (A.c * cz - J[2]) * A.dt;
+    }
+}
+
+__global__ void k_forward_b(SolverArgs A) {
+    const int n = A.s;
+    const int64_t total = (int64_t)n * n * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int x = 1 + (int)(t / ((int64_t)n * n)), y = 1 + (int)((t / n) % n), z = 1 + (int)(t % n);
+        double cx, cy, cz;
+        curl_e(A, x, y, z, cx, cy, cz);
+        double* B = A.bc + 3 * fidx(A.s + 2, x, y, z);
+        B[0] -= A.c * cx * A.dt;
+        B[1] -= A.c * cy * A.dt;
+        B[2] -= A.c * cz * A.dt;
+    }
+}
+
+// node B at pos in [1, s+2)^3 = 1/8 sum of Bc at pos - (i,j,k)
+__global__ void k_interp_c2n(SolverArgs A) {
+    const int n = A.s + 1;
+    const int64_t total = (int64_t)n * n * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int x = 1 + (int)(t / ((int64_t)n * n)), y = 1 + (int)((t / n) % n), z = 1 + (int)(t % n);
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+        for (int i = 0; i < 2; i++)
+            for (int j = 0; j < 2; j++)
+                for (int k = 0; k < 2; k++) {
+                    const double* p = A.bc + 3 * fidx(A.s + 2, x - i, y - j, z - k);
+                    a0 = a0 + p[0]; a1 = a1 + p[1]; a2 = a2 + p[2];
+                }
+        double* B = A.field + 9 * fidx(A.s + 3, x, y, z) + 3;
+        B[0] = .125 * a0; B[1] = .125 * a1; B[2] = .125 * a2;
+    }
+}
+
+// The gather form of the reference adds, at node index 0 and index s of an
+// axis, the same two cells (periodic wrap of the cell index): the final value
+// of a node is the sum of the raw deposits over its image set {0, s} on every
+// axis where it lies on the boundary. Then J = (Js / vol) [/ 8].
+__global__ void k_j_finalize(int sx, int sy, int sz, double* J, double* rho, double vol, int div8) {
+    const int64_t total = (int64_t)sx * sy * sz;
+    const int ny = sy + 1, nz = sz + 1;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int x = (int)(t / ((int64_t)sy * sz)), y = (int)((t / sz) % sy), z = (int)(t % sz);
+        const int nxs = x == 0 ? 2 : 1, nys = y == 0 ? 2 : 1, nzs = z == 0 ? 2 : 1;
+        double a[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int i = 0; i < nxs; ++i)
+            for (int j = 0; j < nys; ++j)
+                for (int k = 0; k < nzs; ++k) {
+                    const int64_t n = ((int64_t)(i ? sx : x) * ny + (j ? sy : y)) * nz + (k ? sz : z);
+                    a[0] += J[3 * n]; a[1] += J[3 * n + 1]; a[2] += J[3 * n + 2]; a[3] += rho[n];
+                }
+        for (int c = 0; c < 4; ++c) {
+            a[c] = a[c] / vol;
+            if (div8) a[c] = a[c] / 8.0;
+        }
+        for (int i = 0; i < nxs; ++i)
+            for (int j = 0; j < nys; ++j)
+                for (int k = 0; k < nzs; ++k) {
+                    const int64_t n = ((int64_t)(i ? sx : x) * ny + (j ? sy : y)) * nz + (k ? sz : z);
+                    J[3 * n] = a[0]; J[3 * n + 1] = a[1]; J[3 * n + 2] = a[2]; rho[n] = a[3];
+                }
+    }
+}
+
+__global__ void k_node32(const double* field, float4* node32, int64_t nodes) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nodes; t += (int64_t)gridDim.x * blockDim.x) {
+        const double* f = field + 9 * t;
+        node32[2 * t] = make_float4((float)f[0], (float)f[1], (float)f[2], 0.f);
+        node32[2 * t + 1] = make_float4((float)f[3], (float)f[4], (float)f[5], 0.f);
+    }
+}
+
+// ---- compensated reductions ----------------------------------------------------
+// Neumaier's improved Kahan summation: (s, c) with s + c the running sum.
+struct Neu {
+    double s, c;
+    __device__ void add(double x) {
+        double t = s + x;
+        if (fabs(s) >= fabs(x)) c += (s - t) + x;
+        else c += (x - t) + s;
+        s = t;
+    }
+    __device__ void merge(const Neu& o) {
+        add(o.s);
+        c += o.c;
+    }
+};
+
+__device__ __forceinline__ Neu shfl_neu(Neu a, int off) {
+    Neu b;
+    b.s = __shfl_down_sync(0xffffffffu, a.s, off);
+    b.c = __shfl_down_sync(0xffffffffu, a.c, off);
+    return b;
+}
+
+// Block-level merge of kQ compensated sums; thread 0 writes 2*kQ doubles.
+template <int kQ>
+__device__ void block_merge(Neu (&acc)[kQ], double* out) {
+    __shared__ Neu sm[32][kQ];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < kQ; ++q)
+        for (int off = 16; off > 0; off >>= 1) acc[q].merge(shfl_neu(acc[q], off));
+    if (lane == 0)
+        for (int q = 0; q < kQ; ++q) sm[wid][q] = acc[q];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int nw = (blockDim.x + 31) / 32;
+        for (int q = 0; q < kQ; ++q) {
+            Neu t = {0.0, 0.0};
+            for (int w = 0; w < nw; ++w) t.merge(sm[w][q]);
+            out[2 * q] = t.s;
+            out[2 * q + 1] = t.c;
+        }
+    }
+}
+
+// Particle sums of one population: sum (q/qom)|v|, sum 1/2 (q/qom)|v|^2,
+// sum q (cell.h:1315-1338). Slots beyond count[c] are skipped.
+template <typename T>
+__global__ void k_reduce_particles(const T* u, const T* v, const T* w, const int64_t* start, const int32_t* count,
+                                   int ncells, double q, double qom, double* partial) {
+    Neu acc[3] = {{0, 0}, {0, 0}, {0, 0}};
+    const double m = q / qom;
+    for (int c = blockIdx.x; c < ncells; c += gridDim.x) {
+        const int64_t s0 = start[c];
+        const int n = count[c];
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const double a = (double)u[s0 + i], b = (double)v[s0 + i], d = (double)w[s0 + i];
+            double ss = a * a;
+            ss += b * b;
+            ss += d * d;
+            acc[0].add(m * sqrt(ss));
+            acc[1].add(0.5 * m * ss);
+            acc[2].add(q);
+        }
+    }
+    block_merge<3>(acc, partial + 6 * blockIdx.x);
+}
+
+// Field energies over [1, s+2)^3: vol * |E|^2 / 4pi and vol * |B + Bext|^2 /
+// 4pi with vol = cell volume / 2 (field.h:443-459).
+__global__ void k_reduce_fields(const double* field, int s, double vol, double four_pi, double* partial) {
+    Neu acc[2] = {{0, 0}, {0, 0}};
+    const int n = s + 1, nf = s + 3;
+    const int64_t total = (int64_t)n * n * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int x = 1 + (int)(t / ((int64_t)n * n)), y = 1 + (int)((t / n) % n), z = 1 + (int)(t % n);
+        const double* f = field + 9 * fidx(nf, x, y, z);
+        double e = f[0] * f[0];
+        e += f[1] * f[1];
+        e += f[2] * f[2];
+        const double b0 = f[3] + f[6], b1 = f[4] + f[7], b2 = f[5] + f[8];
+        double b = b0 * b0;
+        b += b1 * b1;
+        b += b2 * b2;
+        acc[0].add(vol * e / four_pi);
+        acc[1].add(vol * b / four_pi);
+    }
+    block_merge<2>(acc, partial + 4 * blockIdx.x);
+}
+
+// Final merge of `blocks` partial records of kq (s, c) pairs.
+__global__ void k_reduce_final(const double* partial, int blocks, int kq, double* out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int q = 0; q < kq; ++q) {
+        Neu t = {0.0, 0.0};
+        for (int b = 0; b < blocks; ++b) {
+            t.add(partial[2 * kq * b + 2 * q]);
+            t.c += partial[2 * kq * b + 2 * q + 1];
+        }
+        out[q] = t.s + t.c;
+    }
+}
+
+inline int grid_for(int64_t n, int threads) {
+    int64_t b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > 152 * 32) b = 152 * 32;
+    return (int)b;
+}
+
+SolverArgs solver_args(const Geom& g) {
+    SolverArgs A;
+    A.s = g.sx;
+    A.dt = g.dt;
+    A.c = g.c;
+    A.wx = g.w[0];
+    A.wy = g.w[1];
+    A.wz = g.w[2];
+    A.field = g.field;
+    A.bc = g.bcfield;
+    A.J = g.J;
+    return A;
+}
+
+}  // namespace
+
+// ---- host launchers ------------------------------------------------------------
+
+int launch_ghost(const Geom& g, cudaStream_t st) {
+    const int nf = g.sx + 3, nb = g.sx + 2;
+    k_ghost<<<grid_for((int64_t)(nf - 2) * (nf - 2) * 9, 256), 256, 0, st>>>(g.field, nf, 9);
+    k_ghost<<<grid_for((int64_t)(nb - 2) * (nb - 2) * 3, 256), 256, 0, st>>>(g.bcfield, nb, 3);
+    return 2;
+}
+
+int launch_leapfrog(const Geom& g, bool refresh_node_b, cudaStream_t st) {
+    SolverArgs A = solver_args(g);
+    const int64_t ne = (int64_t)(g.sx + 1) * (g.sx + 1) * (g.sx + 1);
+    k_leapfrog_e<<<grid_for(ne, 256), 256, 0, st>>>(A);
+    k_leapfrog_b<<<grid_for((int64_t)g.sx * g.sx * g.sx, 256), 256, 0, st>>>(A);
+    if (refresh_node_b) {
+        k_interp_c2n<<<grid_for(ne, 256), 256, 0, st>>>(A);
+        return 3;
+    }
+    return 2;
+}
+
+int launch_forward(const Geom& g, cudaStream_t st) {
+    SolverArgs A = solver_args(g);
+    const int64_t ne = (int64_t)(g.sx + 1) * (g.sx + 1) * (g.sx + 1);
+    k_forward_e<<<grid_for(ne, 256), 256, 0, st>>>(A);
+    k_forward_b<<<grid_for((int64_t)g.sx * g.sx * g.sx, 256), 256, 0, st>>>(A);
+    k_interp_c2n<<<grid_for(ne, 256), 256, 0, st>>>(A);
+    return 3;
+}
+
+int launch_j_finalize(const Geom& g, bool div8, cudaStream_t st) {
+    k_j_finalize<<<grid_for((int64_t)g.sx * g.sy * g.sz, 256), 256, 0, st>>>(g.sx, g.sy, g.sz, g.J, g.rho, g.vol,
+                                                                             div8 ? 1 : 0);
+    return 1;
+}
+
+int launch_node32(const Geom& g, float4* node32, cudaStream_t st) {
+    const int64_t nodes = (int64_t)(g.sx + 3) * (g.sy + 3) * (g.sz + 3);
+    k_node32<<<grid_for(nodes, 256), 256, 0, st>>>(g.field, node32, nodes);
+    return 1;
+}
+
+int reduce_blocks() { return 152 * 4; }
+
+template <typename T>
+int launch_reduce_particles(const Pop<T>& P, int ncells, double* partial, cudaStream_t st) {
+    k_reduce_particles<T><<<reduce_blocks(), 256, 0, st>>>(P.u, P.v, P.w, P.start, P.count, ncells, P.q, P.qom,
+                                                            partial);
+    return 1;
+}
+template int launch_reduce_particles<float>(const Pop<float>&, int, double*, cudaStream_t);
+template int launch_reduce_particles<double>(const Pop<double>&, int, double*, cudaStream_t);
+
+int launch_reduce_fields(const Geom& g, double* partial, cudaStream_t st) {
+    const double vol = 0.5 * g.w[0] * g.w[1] * g.w[2];
+    const double four_pi = 16.0 * atan(1.0);
+    k_reduce_fields<<<reduce_blocks(), 256, 0, st>>>(g.field, g.sx, vol, four_pi, partial);
+    return 1;
+}
+
+int launch_reduce_final(const double* partial, int blocks, int kq, double* out, cudaStream_t st) {
+    k_reduce_final<<<1, 32, 0, st>>>(partial, blocks, kq, out);
+    return 1;
+}
+
+}  // namespace ipg

@@ -1,0 +1,944 @@
+// Host side of the GB300 particle path: the C ABI of include/ipic3d_gpu.h.
+//
+// A context holds one Universe (universe.h:12-51) on the current GPU and runs
+// simulateSteps (simulator.h:127-242) as a fixed sequence of kernels per step:
+//   [project once if J is stale] -> ghost faces -> field solver -> push
+//   (mover + export + deposit) -> pending push -> injection -> place (import)
+//   -> J finalize.
+// Particles are split into populations of equal (q, qom) -- the species of
+// the reference's distributions (cell.h:104-133) -- so the hot kernel reads
+// neither q nor qom per particle.
+#include <algorithm>
+#include <cstdarg>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/ipic3d_gpu.h"
+#include "launch.h"
+
+namespace ipg {
+namespace {
+
+thread_local int g_last_status = IPIC3D_OK;
+thread_local char g_last_msg[512] = "";
+
+int fail(int status, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+int fail(int status, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_msg, sizeof(g_last_msg), fmt, ap);
+    va_end(ap);
+    g_last_status = status;
+    return status;
+}
+
+#define CU(call)                                                                                              \
+    do {                                                                                                      \
+        cudaError_t e_ = (call);                                                                              \
+        if (e_ != cudaSuccess)                                                                                \
+            return fail(e_ == cudaErrorMemoryAllocation ? IPIC3D_E_NOMEM : IPIC3D_E_CUDA, "%s:%d %s: %s",      \
+                        __FILE__, __LINE__, #call, cudaGetErrorString(e_));                                   \
+    } while (0)
+
+template <typename X>
+void dfree(X*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+template <typename T>
+struct PopStore {
+    double q = 0, qom = 0;
+    int64_t capacity = 0;
+    uint32_t pending_cap = 0, outbox_cap = 0;
+    T *x = nullptr, *y = nullptr, *z = nullptr, *u = nullptr, *v = nullptr, *w = nullptr;
+    uint32_t* id = nullptr;
+    int64_t* start = nullptr;
+    int32_t *count = nullptr, *hole_cnt = nullptr, *arr_cnt = nullptr;
+    int32_t *hole_list = nullptr, *arr_list = nullptr, *sort_tmp = nullptr;
+    Mover<T>*outbox = nullptr, *pending_in = nullptr, *pending_out = nullptr;
+    uint32_t* pending_in_count = nullptr;
+    StepCounters* ctr = nullptr;
+    std::vector<int64_t> h_start;  // host copy of start[]
+
+    void release() {
+        dfree(x); dfree(y); dfree(z); dfree(u); dfree(v); dfree(w); dfree(id);
+        dfree(start); dfree(count); dfree(hole_cnt); dfree(arr_cnt);
+        dfree(hole_list); dfree(arr_list); dfree(sort_tmp);
+        dfree(outbox); dfree(pending_in); dfree(pending_out);
+        dfree(pending_in_count); dfree(ctr);
+        capacity = 0;
+    }
+    Pop<T> view() const {
+        Pop<T> P;
+        P.x = x; P.y = y; P.z = z; P.u = u; P.v = v; P.w = w;
+        P.id = id;
+        P.start = start;
+        P.count = count;
+        P.hole_cnt = hole_cnt;
+        P.hole_list = hole_list;
+        P.arr_cnt = arr_cnt;
+        P.arr_list = arr_list;
+        P.outbox = outbox;
+        P.outbox_cap = outbox_cap;
+        P.pending_in = pending_in;
+        P.pending_out = pending_out;
+        P.pending_cap = pending_cap;
+        P.pending_in_count = pending_in_count;
+        P.ctr = ctr;
+        P.capacity = capacity;
+        P.q = q;
+        P.qom = qom;
+        return P;
+    }
+};
+
+}  // namespace
+}  // namespace ipg
+
+namespace ipg {
+// Advances the device step counter (keys the injection generator).
+__global__ void k_step_end(uint64_t* step) { *step += 1; }
+}  // namespace ipg
+
+using namespace ipg;
+
+struct ipic3d_ctx {
+    ipic3d_props props;
+    ipic3d_config cfg;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool fp32 = false;
+    Geom g{};
+    double *field = nullptr, *bcfield = nullptr, *J = nullptr, *rho = nullptr;
+    float4* node32 = nullptr;
+    uint64_t* d_step = nullptr;
+    double *d_partial = nullptr, *d_result = nullptr;
+    std::vector<PopStore<float>> p32;
+    std::vector<PopStore<double>> p64;
+    bool j_valid = false;
+    uint64_t steps = 0, launches = 0, rebuilds = 0;
+    StepCounters last{};
+    cudaGraphExec_t graph = nullptr;
+    bool graph_valid = false;
+    uint64_t graph_kernels = 0;  // kernels one replay runs
+
+    int npops() const { return fp32 ? (int)p32.size() : (int)p64.size(); }
+    int64_t nfield() const { return (props.size[0] + 3) * (props.size[1] + 3) * (props.size[2] + 3); }
+    int64_t nbc() const { return (props.size[0] + 2) * (props.size[1] + 2) * (props.size[2] + 2); }
+    int64_t nnode() const { return (props.size[0] + 1) * (props.size[1] + 1) * (props.size[2] + 1); }
+    int64_t ncells() const { return props.size[0] * props.size[1] * props.size[2]; }
+};
+
+namespace {
+
+void drop_graph(ipic3d_ctx* ctx) {
+    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+    ctx->graph = nullptr;
+    ctx->graph_valid = false;
+}
+
+void release_pops(ipic3d_ctx* ctx) {
+    for (auto& p : ctx->p32) p.release();
+    for (auto& p : ctx->p64) p.release();
+    ctx->p32.clear();
+    ctx->p64.clear();
+}
+
+// Slots reserved for a cell holding n particles: n plus the slack, rounded up
+// to a multiple of 4 (one vector group), at least 4.
+int64_t cell_capacity(const ipic3d_config& cfg, uint64_t n) {
+    double slack = cfg.slack > 0 ? cfg.slack : 0.125;
+    int64_t smin = cfg.slack_min > 0 ? cfg.slack_min : 8;
+    int64_t extra = std::max<int64_t>(smin, (int64_t)std::ceil(slack * (double)n));
+    int64_t cap = (int64_t)n + extra;
+    cap = (cap + 3) & ~int64_t(3);
+    return std::max<int64_t>(cap, 4);
+}
+
+template <typename T>
+int alloc_pop(ipic3d_ctx* ctx, PopStore<T>& P, const std::vector<uint64_t>& counts, int64_t extra_pending) {
+    const int64_t nc = ctx->ncells();
+    P.h_start.assign(nc + 1, 0);
+    for (int64_t c = 0; c < nc; ++c) P.h_start[c + 1] = P.h_start[c] + cell_capacity(ctx->cfg, counts[c]);
+    P.capacity = P.h_start[nc];
+    P.pending_cap = (uint32_t)std::min<int64_t>(std::max<int64_t>(1 << 16, P.capacity / 4), 0x7fffffff);
+    int64_t inject_cap = 0;
+    if (ctx->cfg.flags & IPIC3D_F_INJECT_LOW_X)
+        inject_cap = (int64_t)(ctx->props.size[1] * ctx->props.size[2]) * ((int64_t)ctx->cfg.inject_per_cell + 1);
+    const int64_t ob = P.capacity + P.pending_cap + inject_cap + extra_pending;
+    if (ob > 0x7fffffff) return fail(IPIC3D_E_CAPACITY, "population too large for 32-bit outbox indices");
+    P.outbox_cap = (uint32_t)ob;
+    const size_t cap = (size_t)P.capacity;
+    CU(cudaMalloc(&P.x, cap * sizeof(T)));
+    CU(cudaMalloc(&P.y, cap * sizeof(T)));
+    CU(cudaMalloc(&P.z, cap * sizeof(T)));
+    CU(cudaMalloc(&P.u, cap * sizeof(T)));
+    CU(cudaMalloc(&P.v, cap * sizeof(T)));
+    CU(cudaMalloc(&P.w, cap * sizeof(T)));
+    if (ctx->cfg.flags & IPIC3D_F_TRACK_IDS) CU(cudaMalloc(&P.id, cap * sizeof(uint32_t)));
+    CU(cudaMalloc(&P.start, (nc + 1) * sizeof(int64_t)));
+    CU(cudaMalloc(&P.count, nc * sizeof(int32_t)));
+    CU(cudaMalloc(&P.hole_cnt, nc * sizeof(int32_t)));
+    CU(cudaMalloc(&P.arr_cnt, nc * sizeof(int32_t)));
+    CU(cudaMalloc(&P.hole_list, cap * sizeof(int32_t)));
+    CU(cudaMalloc(&P.arr_list, cap * sizeof(int32_t)));
+    CU(cudaMalloc(&P.sort_tmp, cap * sizeof(int32_t)));
+    CU(cudaMalloc(&P.outbox, (size_t)P.outbox_cap * sizeof(Mover<T>)));
+    CU(cudaMalloc(&P.pending_in, (size_t)P.pending_cap * sizeof(Mover<T>)));
+    CU(cudaMalloc(&P.pending_out, (size_t)P.pending_cap * sizeof(Mover<T>)));
+    CU(cudaMalloc(&P.pending_in_count, sizeof(uint32_t)));
+    CU(cudaMalloc(&P.ctr, sizeof(StepCounters)));
+    CU(cudaMemsetAsync(P.hole_cnt, 0, nc * sizeof(int32_t), ctx->stream));
+    CU(cudaMemsetAsync(P.arr_cnt, 0, nc * sizeof(int32_t), ctx->stream));
+    CU(cudaMemsetAsync(P.pending_in_count, 0, sizeof(uint32_t), ctx->stream));
+    CU(cudaMemsetAsync(P.ctr, 0, sizeof(StepCounters), ctx->stream));
+    CU(cudaMemcpyAsync(P.start, P.h_start.data(), (nc + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    return IPIC3D_OK;
+}
+
+// Copies one population's particles (input indices `order`, grouped by cell
+// with per-cell `counts`) into the slot layout. FP32 stores the position
+// relative to the cell origin in cell widths.
+template <typename T>
+int fill_pop(ipic3d_ctx* ctx, PopStore<T>& P, const ipic3d_particle* parts, const uint32_t* ids,
+             const std::vector<int64_t>& order, const std::vector<uint64_t>& counts,
+             const std::vector<int64_t>& cell_of) {
+    const int64_t nc = ctx->ncells();
+    const size_t cap = (size_t)P.capacity;
+    std::vector<T> hx(cap, T(0)), hy(cap, T(0)), hz(cap, T(0)), hu(cap, T(0)), hv(cap, T(0)), hw(cap, T(0));
+    std::vector<uint32_t> hid(P.id ? cap : 0, 0);
+    std::vector<int32_t> hcount(nc);
+    const ipic3d_props& pr = ctx->props;
+    int64_t k = 0;
+    for (int64_t c = 0; c < nc; ++c) {
+        hcount[c] = (int32_t)counts[c];
+        int64_t cx = c / (pr.size[1] * pr.size[2]), cy = (c / pr.size[2]) % pr.size[1], cz = c % pr.size[2];
+        for (uint64_t i = 0; i < counts[c]; ++i, ++k) {
+            const int64_t src = order[k];
+            const ipic3d_particle& p = parts[src];
+            const size_t s = (size_t)(P.h_start[c] + (int64_t)i);
+            (void)cell_of;
+            if (std::is_same<T, float>::value) {
+                double ox = pr.origin[0] + (double)cx * pr.cell_width[0];
+                double oy = pr.origin[1] + (double)cy * pr.cell_width[1];
+                double oz = pr.origin[2] + (double)cz * pr.cell_width[2];
+                hx[s] = (T)((p.position[0] - ox) / pr.cell_width[0]);
+                hy[s] = (T)((p.position[1] - oy) / pr.cell_width[1]);
+                hz[s] = (T)((p.position[2] - oz) / pr.cell_width[2]);
+            } else {
+                hx[s] = (T)p.position[0];
+                hy[s] = (T)p.position[1];
+                hz[s] = (T)p.position[2];
+            }
+            hu[s] = (T)p.velocity[0];
+            hv[s] = (T)p.velocity[1];
+            hw[s] = (T)p.velocity[2];
+            if (P.id) hid[s] = ids ? ids[src] : (uint32_t)src;
+        }
+    }
+    cudaStream_t st = ctx->stream;
+    CU(cudaMemcpyAsync(P.x, hx.data(), cap * sizeof(T), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(P.y, hy.data(), cap * sizeof(T), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(P.z, hz.data(), cap * sizeof(T), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(P.u, hu.data(), cap * sizeof(T), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(P.v, hv.data(), cap * sizeof(T), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(P.w, hw.data(), cap * sizeof(T), cudaMemcpyHostToDevice, st));
+    if (P.id) CU(cudaMemcpyAsync(P.id, hid.data(), cap * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(P.count, hcount.data(), nc * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    CU(cudaStreamSynchronize(st));  // host staging buffers die here
+    return IPIC3D_OK;
+}
+
+struct Species {
+    double q, qom;
+};
+
+// Splits the input into species (exact (q, qom) equality) and uploads.
+int upload_impl(ipic3d_ctx* ctx, const ipic3d_particle* parts, const uint64_t* cell_counts, const uint32_t* ids) {
+    const int64_t nc = ctx->ncells();
+    uint64_t n = 0;
+    for (int64_t c = 0; c < nc; ++c) n += cell_counts[c];
+    if (n > 0 && !parts) return fail(IPIC3D_E_INVALID, "particles == NULL with %llu particles", (unsigned long long)n);
+    std::vector<Species> sp;
+    std::vector<uint8_t> sid(n);
+    if (ctx->cfg.flags & IPIC3D_F_INJECT_LOW_X) sp.push_back({ctx->cfg.inject_q, ctx->cfg.inject_qom});
+    for (uint64_t i = 0; i < n; ++i) {
+        size_t k = 0;
+        for (; k < sp.size(); ++k)
+            if (sp[k].q == parts[i].q && sp[k].qom == parts[i].qom) break;
+        if (k == sp.size()) {
+            if (sp.size() >= 16) return fail(IPIC3D_E_INVALID, "more than 16 distinct (q, qom) species");
+            sp.push_back({parts[i].q, parts[i].qom});
+        }
+        sid[i] = (uint8_t)k;
+    }
+    if (sp.empty()) sp.push_back({0.0, 1.0});
+    // per species: order grouped by cell, counts
+    std::vector<std::vector<int64_t>> order(sp.size());
+    std::vector<std::vector<uint64_t>> counts(sp.size(), std::vector<uint64_t>(nc, 0));
+    std::vector<int64_t> cell_of;
+    {
+        uint64_t k = 0;
+        for (int64_t c = 0; c < nc; ++c)
+            for (uint64_t i = 0; i < cell_counts[c]; ++i, ++k) {
+                order[sid[k]].push_back((int64_t)k);
+                counts[sid[k]][c]++;
+            }
+    }
+    drop_graph(ctx);
+    release_pops(ctx);
+    for (size_t s = 0; s < sp.size(); ++s) {
+        int rc;
+        if (ctx->fp32) {
+            ctx->p32.emplace_back();
+            auto& P = ctx->p32.back();
+            P.q = sp[s].q;
+            P.qom = sp[s].qom;
+            if ((rc = alloc_pop(ctx, P, counts[s], 0))) return rc;
+            if ((rc = fill_pop(ctx, P, parts, ids, order[s], counts[s], cell_of))) return rc;
+        } else {
+            ctx->p64.emplace_back();
+            auto& P = ctx->p64.back();
+            P.q = sp[s].q;
+            P.qom = sp[s].qom;
+            if ((rc = alloc_pop(ctx, P, counts[s], 0))) return rc;
+            if ((rc = fill_pop(ctx, P, parts, ids, order[s], counts[s], cell_of))) return rc;
+        }
+    }
+    ctx->j_valid = false;
+    return IPIC3D_OK;
+}
+
+// Downloads every population, adding the pending particles to their cells.
+template <typename T>
+int download_pop(ipic3d_ctx* ctx, const PopStore<T>& P, std::vector<std::vector<ipic3d_particle>>& cells,
+                 std::vector<std::vector<uint32_t>>& cell_ids) {
+    const int64_t nc = ctx->ncells();
+    const size_t cap = (size_t)P.capacity;
+    std::vector<T> hx(cap), hy(cap), hz(cap), hu(cap), hv(cap), hw(cap);
+    std::vector<uint32_t> hid(P.id ? cap : 0);
+    std::vector<int32_t> hcount(nc);
+    uint32_t npend = 0;
+    cudaStream_t st = ctx->stream;
+    CU(cudaMemcpyAsync(hx.data(), P.x, cap * sizeof(T), cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(hy.data(), P.y, cap * sizeof(T), cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(hz.data(), P.z, cap * sizeof(T), cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(hu.data(), P.u, cap * sizeof(T), cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(hv.data(), P.v, cap * sizeof(T), cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(hw.data(), P.w, cap * sizeof(T), cudaMemcpyDeviceToHost, st));
+    if (P.id) CU(cudaMemcpyAsync(hid.data(), P.id, cap * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(hcount.data(), P.count, nc * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(&npend, P.pending_in_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    std::vector<Mover<T>> pend(npend);
+    if (npend) CU(cudaMemcpy(pend.data(), P.pending_in, npend * sizeof(Mover<T>), cudaMemcpyDeviceToHost));
+    const ipic3d_props& pr = ctx->props;
+    auto emit = [&](int64_t c, T x, T y, T z, T u, T v, T w, uint32_t id) {
+        ipic3d_particle p;
+        if (std::is_same<T, float>::value) {
+            int64_t cx = c / (pr.size[1] * pr.size[2]), cy = (c / pr.size[2]) % pr.size[1], cz = c % pr.size[2];
+            p.position[0] = (pr.origin[0] + (double)cx * pr.cell_width[0]) + (double)x * pr.cell_width[0];
+            p.position[1] = (pr.origin[1] + (double)cy * pr.cell_width[1]) + (double)y * pr.cell_width[1];
+            p.position[2] = (pr.origin[2] + (double)cz * pr.cell_width[2]) + (double)z * pr.cell_width[2];
+        } else {
+            p.position[0] = (double)x;
+            p.position[1] = (double)y;
+            p.position[2] = (double)z;
+        }
+        p.velocity[0] = (double)u;
+        p.velocity[1] = (double)v;
+        p.velocity[2] = (double)w;
+        p.q = P.q;
+        p.qom = P.qom;
+        cells[c].push_back(p);
+        cell_ids[c].push_back(id);
+    };
+    for (int64_t c = 0; c < nc; ++c)
+        for (int32_t i = 0; i < hcount[c]; ++i) {
+            size_t s = (size_t)(P.h_start[c] + i);
+            emit(c, hx[s], hy[s], hz[s], hu[s], hv[s], hw[s], P.id ? hid[s] : 0u);
+        }
+    for (const auto& m : pend) emit(m.cell, m.x, m.y, m.z, m.u, m.v, m.w, m.id);
+    return IPIC3D_OK;
+}
+
+int gather_host(ipic3d_ctx* ctx, std::vector<std::vector<ipic3d_particle>>& cells,
+                std::vector<std::vector<uint32_t>>& ids) {
+    cells.assign(ctx->ncells(), {});
+    ids.assign(ctx->ncells(), {});
+    int rc;
+    for (auto& P : ctx->p32)
+        if ((rc = download_pop(ctx, P, cells, ids))) return rc;
+    for (auto& P : ctx->p64)
+        if ((rc = download_pop(ctx, P, cells, ids))) return rc;
+    return IPIC3D_OK;
+}
+
+// Re-lays out all particles with fresh slack (after cells overflowed).
+int rebuild(ipic3d_ctx* ctx) {
+    std::vector<std::vector<ipic3d_particle>> cells;
+    std::vector<std::vector<uint32_t>> ids;
+    int rc = gather_host(ctx, cells, ids);
+    if (rc) return rc;
+    std::vector<ipic3d_particle> flat;
+    std::vector<uint32_t> fid;
+    std::vector<uint64_t> counts(ctx->ncells());
+    for (int64_t c = 0; c < ctx->ncells(); ++c) {
+        counts[c] = cells[c].size();
+        flat.insert(flat.end(), cells[c].begin(), cells[c].end());
+        fid.insert(fid.end(), ids[c].begin(), ids[c].end());
+    }
+    bool valid = ctx->j_valid;
+    rc = upload_impl(ctx, flat.data(), counts.data(), fid.data());
+    ctx->j_valid = valid;  // particles are unchanged: J still holds their deposit
+    ctx->rebuilds++;
+    return rc;
+}
+
+void refresh_geom(ipic3d_ctx* ctx) {
+    Geom& g = ctx->g;
+    const ipic3d_props& p = ctx->props;
+    g.sx = (int)p.size[0];
+    g.sy = (int)p.size[1];
+    g.sz = (int)p.size[2];
+    g.ncells = (int)ctx->ncells();
+    for (int a = 0; a < 3; ++a) {
+        g.w[a] = p.cell_width[a];
+        g.inv_w[a] = 1.0 / p.cell_width[a];
+        g.half_w[a] = p.cell_width[a] / 2.0;
+        g.origin[a] = p.origin[a];
+        g.object_center[a] = p.object_center[a];
+        g.L[a] = (double)p.size[a] * p.cell_width[a];
+        g.bc_lo[a] = ctx->cfg.bc_low[a];
+        g.bc_hi[a] = ctx->cfg.bc_high[a];
+    }
+    g.dt = p.dt;
+    g.c = p.speed_of_light;
+    g.planet_r2 = p.planet_radius * p.planet_radius;
+    g.mft = -p.external_b[2] * std::pow(p.planet_radius, 3);  // host libm, as cell.h:923
+    g.vol = p.cell_width[0] * p.cell_width[1] * p.cell_width[2];
+    g.flags = ctx->cfg.flags;
+    g.mover = ctx->cfg.mover;
+    g.deposit = ctx->cfg.projector == IPIC3D_PROJECT_CIC ? 1 : 0;
+    g.field = ctx->field;
+    g.bcfield = ctx->bcfield;
+    g.J = ctx->J;
+    g.rho = ctx->rho;
+    g.node32 = ctx->node32;
+}
+
+int check_launch(ipic3d_ctx* ctx, int n) {
+    ctx->launches += (uint64_t)n;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(IPIC3D_E_CUDA, "kernel launch: %s", cudaGetErrorString(e));
+    return IPIC3D_OK;
+}
+
+// projectToDensityField over the stored particles (deposit-only pass).
+int project_impl(ipic3d_ctx* ctx) {
+    cudaStream_t st = ctx->stream;
+    CU(cudaMemsetAsync(ctx->J, 0, ctx->nnode() * 3 * sizeof(double), st));
+    CU(cudaMemsetAsync(ctx->rho, 0, ctx->nnode() * sizeof(double), st));
+    Geom g = ctx->g;
+    g.deposit = 1;
+    int n = 0;
+    for (auto& P : ctx->p32) n += launch_push<float>(g, P.view(), 1, st);
+    for (auto& P : ctx->p64) n += launch_push<double>(g, P.view(), 1, st);
+    n += launch_j_finalize(g, (ctx->cfg.flags & IPIC3D_F_J_DIV8) != 0, st);
+    ctx->j_valid = true;
+    return check_launch(ctx, n);
+}
+
+int solve_impl(ipic3d_ctx* ctx) {
+    cudaStream_t st = ctx->stream;
+    int n = 0;
+    if (ctx->cfg.solver == IPIC3D_SOLVER_LEAPFROG)
+        n += launch_leapfrog(ctx->g, (ctx->cfg.flags & IPIC3D_F_REFRESH_NODE_B) != 0, st);
+    else if (ctx->cfg.solver == IPIC3D_SOLVER_FORWARD)
+        n += launch_forward(ctx->g, st);
+    if (ctx->fp32 && ctx->cfg.mover == IPIC3D_MOVER_FIELD && ctx->cfg.solver != IPIC3D_SOLVER_STATIC)
+        n += launch_node32(ctx->g, ctx->node32, st);
+    return check_launch(ctx, n);
+}
+
+// mover + export + import of all populations (+ injection), with the fused
+// deposit when the projector is on.
+int move_impl(ipic3d_ctx* ctx, bool deposit) {
+    cudaStream_t st = ctx->stream;
+    Geom g = ctx->g;
+    g.deposit = deposit ? 1 : 0;
+    int n = 0;
+    for (auto& P : ctx->p32) CU(cudaMemsetAsync(P.ctr, 0, offsetof(StepCounters, lost), st));
+    for (auto& P : ctx->p64) CU(cudaMemsetAsync(P.ctr, 0, offsetof(StepCounters, lost), st));
+    if (deposit) {
+        CU(cudaMemsetAsync(ctx->J, 0, ctx->nnode() * 3 * sizeof(double), st));
+        CU(cudaMemsetAsync(ctx->rho, 0, ctx->nnode() * sizeof(double), st));
+    }
+    for (auto& P : ctx->p32) n += launch_push<float>(g, P.view(), 0, st);
+    for (auto& P : ctx->p64) n += launch_push<double>(g, P.view(), 0, st);
+    for (auto& P : ctx->p32) n += launch_push_pending<float>(g, P.view(), st);
+    for (auto& P : ctx->p64) n += launch_push_pending<double>(g, P.view(), st);
+    const bool inject = (ctx->cfg.flags & IPIC3D_F_INJECT_LOW_X) && ctx->cfg.bc_low[0] == IPIC3D_BC_OPEN &&
+                        ctx->cfg.inject_per_cell > 0;
+    if (inject) {
+        if (ctx->fp32)
+            n += launch_inject<float>(g, ctx->p32[0].view(), ctx->cfg.inject_per_cell, ctx->cfg.inject_drift,
+                                      ctx->cfg.inject_vth, ctx->cfg.seed, ctx->d_step, st);
+        else
+            n += launch_inject<double>(g, ctx->p64[0].view(), ctx->cfg.inject_per_cell, ctx->cfg.inject_drift,
+                                       ctx->cfg.inject_vth, ctx->cfg.seed, ctx->d_step, st);
+    }
+    for (auto& P : ctx->p32) {
+        n += launch_place<float>(g, P.view(), P.sort_tmp, st);
+        n += launch_pending_rotate<float>(P.view(), P.pending_in_count, st);
+    }
+    for (auto& P : ctx->p64) {
+        n += launch_place<double>(g, P.view(), P.sort_tmp, st);
+        n += launch_pending_rotate<double>(P.view(), P.pending_in_count, st);
+    }
+    if (deposit) n += launch_j_finalize(g, (ctx->cfg.flags & IPIC3D_F_J_DIV8) != 0, st);
+    return check_launch(ctx, n);
+}
+
+// One timestep's kernel sequence (the body the graph captures).
+int enqueue_step(ipic3d_ctx* ctx) {
+    const bool project = ctx->cfg.projector == IPIC3D_PROJECT_CIC;
+    int rc;
+    if (ctx->cfg.solver != IPIC3D_SOLVER_STATIC) {
+        int n = launch_ghost(ctx->g, ctx->stream);
+        if ((rc = check_launch(ctx, n))) return rc;
+        if ((rc = solve_impl(ctx))) return rc;
+    }
+    if ((rc = move_impl(ctx, project))) return rc;
+    k_step_end<<<1, 1, 0, ctx->stream>>>(ctx->d_step);
+    return check_launch(ctx, 1);
+}
+
+// Reads the step counters back; rebuilds the layout when particles wait for
+// a slot; reports lost particles.
+int after_steps(ipic3d_ctx* ctx) {
+    CU(cudaStreamSynchronize(ctx->stream));
+    StepCounters total{};
+    uint32_t pending = 0;
+    auto acc = [&](const StepCounters& c, uint32_t pin) {
+        total.removed += c.removed;
+        total.migrated += c.migrated;
+        total.injected += c.injected;
+        total.lost += c.lost;
+        total.pending_out += c.pending_out;
+        pending += pin;
+    };
+    for (auto& P : ctx->p32) {
+        StepCounters c;
+        uint32_t pin;
+        CU(cudaMemcpy(&c, P.ctr, sizeof(c), cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(&pin, P.pending_in_count, sizeof(pin), cudaMemcpyDeviceToHost));
+        acc(c, pin);
+    }
+    for (auto& P : ctx->p64) {
+        StepCounters c;
+        uint32_t pin;
+        CU(cudaMemcpy(&c, P.ctr, sizeof(c), cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(&pin, P.pending_in_count, sizeof(pin), cudaMemcpyDeviceToHost));
+        acc(c, pin);
+    }
+    ctx->last = total;
+    if (total.lost) return fail(IPIC3D_E_CAPACITY, "%u particles lost: pending list full", total.lost);
+    if (pending) return rebuild(ctx);
+    return IPIC3D_OK;
+}
+
+int check_ctx(ipic3d_ctx* ctx) {
+    if (!ctx) return fail(IPIC3D_E_INVALID, "context is NULL");
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return fail(IPIC3D_E_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+    return IPIC3D_OK;
+}
+
+}  // namespace
+
+// ============================================================================
+extern "C" {
+
+void ipic3d_gpu_config_default(ipic3d_config* cfg) {
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->precision = IPIC3D_FP64;
+    cfg->mover = IPIC3D_MOVER_DIPOLE;
+    cfg->solver = IPIC3D_SOLVER_STATIC;
+    cfg->projector = IPIC3D_PROJECT_NONE;
+    for (int a = 0; a < 3; ++a) cfg->bc_low[a] = cfg->bc_high[a] = IPIC3D_BC_REFLECT;
+    cfg->seed = 12345;
+}
+
+int ipic3d_gpu_last_error(char* buf, size_t len) {
+    if (buf && len) {
+        std::strncpy(buf, g_last_msg, len - 1);
+        buf[len - 1] = 0;
+    }
+    return g_last_status;
+}
+
+int ipic3d_gpu_create(const ipic3d_props* props, const ipic3d_config* cfg, ipic3d_ctx** out) {
+    if (!props || !cfg || !out) return fail(IPIC3D_E_INVALID, "NULL argument");
+    *out = nullptr;
+    for (int a = 0; a < 3; ++a) {
+        if (props->size[a] <= 0) return fail(IPIC3D_E_INVALID, "size[%d] = %lld must be positive", a, (long long)props->size[a]);
+        if (!(props->cell_width[a] > 0)) return fail(IPIC3D_E_INVALID, "cell_width[%d] must be positive", a);
+        if ((cfg->bc_low[a] == IPIC3D_BC_PERIODIC) != (cfg->bc_high[a] == IPIC3D_BC_PERIODIC))
+            return fail(IPIC3D_E_INVALID, "axis %d: periodic must apply to both faces", a);
+        if (cfg->bc_low[a] < 0 || cfg->bc_low[a] > 2 || cfg->bc_high[a] < 0 || cfg->bc_high[a] > 2)
+            return fail(IPIC3D_E_INVALID, "axis %d: unknown boundary", a);
+    }
+    if (!(props->dt > 0)) return fail(IPIC3D_E_INVALID, "dt must be positive");
+    if (!(props->speed_of_light > 0)) return fail(IPIC3D_E_INVALID, "speed_of_light must be positive");
+    if (props->planet_radius < 0) return fail(IPIC3D_E_INVALID, "planet_radius must be >= 0");
+    if (cfg->precision != IPIC3D_FP64 && cfg->precision != IPIC3D_FP32) return fail(IPIC3D_E_INVALID, "precision");
+    if (cfg->mover != IPIC3D_MOVER_DIPOLE && cfg->mover != IPIC3D_MOVER_FIELD) return fail(IPIC3D_E_INVALID, "mover");
+    if (cfg->solver < 0 || cfg->solver > 2) return fail(IPIC3D_E_INVALID, "solver");
+    if (cfg->projector < 0 || cfg->projector > 1) return fail(IPIC3D_E_INVALID, "projector");
+    if (cfg->solver != IPIC3D_SOLVER_STATIC && !(props->size[0] == props->size[1] && props->size[1] == props->size[2]))
+        return fail(IPIC3D_E_INVALID, "field solvers need a cubic grid (field.h:424)");
+    const int64_t ncells = props->size[0] * props->size[1] * props->size[2];
+    if (ncells > 0x7fffffff / 4) return fail(IPIC3D_E_INVALID, "grid too large");
+    int dev = 0, ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(IPIC3D_E_NODEVICE, "no CUDA device");
+    cudaGetDevice(&dev);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return fail(IPIC3D_E_NODEVICE, "cudaGetDeviceProperties");
+    if (!(prop.major == 10 && prop.minor == 3))
+        return fail(IPIC3D_E_NODEVICE, "device %d is sm_%d%d; this library is built for sm_103a only", dev,
+                    prop.major, prop.minor);
+    auto* ctx = new (std::nothrow) ipic3d_ctx();
+    if (!ctx) return fail(IPIC3D_E_NOMEM, "host allocation");
+    ctx->props = *props;
+    ctx->cfg = *cfg;
+    ctx->device = dev;
+    ctx->fp32 = cfg->precision == IPIC3D_FP32;
+    auto bail = [&](int rc) {
+        ipic3d_gpu_destroy(ctx);
+        return rc;
+    };
+#define CUB(call)                                                                                         \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess)                                                                            \
+            return bail(fail(e_ == cudaErrorMemoryAllocation ? IPIC3D_E_NOMEM : IPIC3D_E_CUDA, "%s: %s", #call, \
+                             cudaGetErrorString(e_)));                                                    \
+    } while (0)
+    CUB(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    CUB(cudaMalloc(&ctx->field, ctx->nfield() * 9 * sizeof(double)));
+    CUB(cudaMalloc(&ctx->bcfield, ctx->nbc() * 3 * sizeof(double)));
+    CUB(cudaMalloc(&ctx->J, ctx->nnode() * 3 * sizeof(double)));
+    CUB(cudaMalloc(&ctx->rho, ctx->nnode() * sizeof(double)));
+    CUB(cudaMalloc(&ctx->node32, ctx->nfield() * 2 * sizeof(float4)));
+    CUB(cudaMalloc(&ctx->d_step, sizeof(uint64_t)));
+    CUB(cudaMalloc(&ctx->d_partial, (size_t)reduce_blocks() * 8 * sizeof(double)));
+    CUB(cudaMalloc(&ctx->d_result, 8 * sizeof(double)));
+    CUB(cudaMemsetAsync(ctx->field, 0, ctx->nfield() * 9 * sizeof(double), ctx->stream));
+    CUB(cudaMemsetAsync(ctx->bcfield, 0, ctx->nbc() * 3 * sizeof(double), ctx->stream));
+    CUB(cudaMemsetAsync(ctx->J, 0, ctx->nnode() * 3 * sizeof(double), ctx->stream));
+    CUB(cudaMemsetAsync(ctx->rho, 0, ctx->nnode() * sizeof(double), ctx->stream));
+    CUB(cudaMemsetAsync(ctx->node32, 0, ctx->nfield() * 2 * sizeof(float4), ctx->stream));
+    CUB(cudaMemsetAsync(ctx->d_step, 0, sizeof(uint64_t), ctx->stream));
+#undef CUB
+    refresh_geom(ctx);
+    // an empty particle set so that every call works before the first upload
+    std::vector<uint64_t> zeros(ncells, 0);
+    int rc = upload_impl(ctx, nullptr, zeros.data(), nullptr);
+    if (rc) return bail(rc);
+    *out = ctx;
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_destroy(ipic3d_ctx* ctx) {
+    if (!ctx) return IPIC3D_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    drop_graph(ctx);
+    release_pops(ctx);
+    dfree(ctx->field);
+    dfree(ctx->bcfield);
+    dfree(ctx->J);
+    dfree(ctx->rho);
+    dfree(ctx->node32);
+    dfree(ctx->d_step);
+    dfree(ctx->d_partial);
+    dfree(ctx->d_result);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_upload_particles(ipic3d_ctx* ctx, const ipic3d_particle* particles, const uint64_t* cell_counts,
+                                const uint32_t* ids) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!cell_counts) return fail(IPIC3D_E_INVALID, "cell_counts == NULL");
+    return upload_impl(ctx, particles, cell_counts, ids);
+}
+
+int ipic3d_gpu_reserve(ipic3d_ctx* ctx, uint64_t n) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    (void)n;  // capacity follows the per-cell slack; nothing to pre-size
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_particle_count(ipic3d_ctx* ctx, uint64_t* n) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!n) return fail(IPIC3D_E_INVALID, "n == NULL");
+    std::vector<uint64_t> counts(ctx->ncells());
+    if ((rc = ipic3d_gpu_cell_counts(ctx, counts.data()))) return rc;
+    uint64_t t = 0;
+    for (auto c : counts) t += c;
+    *n = t;
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_cell_counts(ipic3d_ctx* ctx, uint64_t* cell_counts) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!cell_counts) return fail(IPIC3D_E_INVALID, "cell_counts == NULL");
+    const int64_t nc = ctx->ncells();
+    std::fill(cell_counts, cell_counts + nc, 0);
+    std::vector<int32_t> h(nc);
+    auto add = [&](const int32_t* dcount, const void* dpend, size_t msz, const uint32_t* dpin) -> int {
+        CU(cudaMemcpyAsync(h.data(), dcount, nc * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+        uint32_t np = 0;
+        CU(cudaMemcpyAsync(&np, dpin, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+        CU(cudaStreamSynchronize(ctx->stream));
+        for (int64_t c = 0; c < nc; ++c) cell_counts[c] += (uint64_t)h[c];
+        if (np) {
+            std::vector<char> buf((size_t)np * msz);
+            CU(cudaMemcpy(buf.data(), dpend, buf.size(), cudaMemcpyDeviceToHost));
+            for (uint32_t i = 0; i < np; ++i) cell_counts[*(const int32_t*)(buf.data() + (size_t)i * msz)] += 1;
+        }
+        return IPIC3D_OK;
+    };
+    for (auto& P : ctx->p32)
+        if ((rc = add(P.count, P.pending_in, sizeof(Mover<float>), P.pending_in_count))) return rc;
+    for (auto& P : ctx->p64)
+        if ((rc = add(P.count, P.pending_in, sizeof(Mover<double>), P.pending_in_count))) return rc;
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_download_particles(ipic3d_ctx* ctx, ipic3d_particle* particles, uint64_t capacity,
+                                  uint64_t* cell_counts, uint32_t* ids) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    std::vector<std::vector<ipic3d_particle>> cells;
+    std::vector<std::vector<uint32_t>> cid;
+    if ((rc = gather_host(ctx, cells, cid))) return rc;
+    uint64_t k = 0;
+    for (int64_t c = 0; c < ctx->ncells(); ++c) {
+        if (cell_counts) cell_counts[c] = cells[c].size();
+        for (size_t i = 0; i < cells[c].size(); ++i, ++k) {
+            if (k >= capacity) {
+                if (particles || ids) return fail(IPIC3D_E_CAPACITY, "output capacity %llu too small",
+                                                  (unsigned long long)capacity);
+                continue;
+            }
+            if (particles) particles[k] = cells[c][i];
+            if (ids) ids[k] = cid[c][i];
+        }
+    }
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_upload_fields(ipic3d_ctx* ctx, const double* field, const double* bcfield, const double* density) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    cudaStream_t st = ctx->stream;
+    if (field) CU(cudaMemcpyAsync(ctx->field, field, ctx->nfield() * 9 * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (bcfield) CU(cudaMemcpyAsync(ctx->bcfield, bcfield, ctx->nbc() * 3 * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (density) {
+        CU(cudaMemcpyAsync(ctx->J, density, ctx->nnode() * 3 * sizeof(double), cudaMemcpyHostToDevice, st));
+        // a supplied J is used as it is while the projector is off
+    }
+    if (field) {
+        int n = launch_node32(ctx->g, ctx->node32, st);
+        if ((rc = check_launch(ctx, n))) return rc;
+    }
+    CU(cudaStreamSynchronize(st));
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_download_fields(ipic3d_ctx* ctx, double* field, double* bcfield, double* density, double* rho) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    cudaStream_t st = ctx->stream;
+    if (field) CU(cudaMemcpyAsync(field, ctx->field, ctx->nfield() * 9 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (bcfield) CU(cudaMemcpyAsync(bcfield, ctx->bcfield, ctx->nbc() * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (density) CU(cudaMemcpyAsync(density, ctx->J, ctx->nnode() * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (rho) CU(cudaMemcpyAsync(rho, ctx->rho, ctx->nnode() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_step(ipic3d_ctx* ctx, uint64_t num_steps) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (num_steps == 0) return IPIC3D_OK;
+    if (ctx->cfg.projector == IPIC3D_PROJECT_CIC && !ctx->j_valid)
+        if ((rc = project_impl(ctx))) return rc;
+    const bool use_graph = (ctx->cfg.flags & IPIC3D_F_USE_GRAPH) != 0;
+    for (uint64_t i = 0; i < num_steps; ++i) {
+        if (use_graph) {
+            if (!ctx->graph_valid) {
+                cudaGraph_t graph = nullptr;
+                CU(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+                const uint64_t before = ctx->launches;
+                rc = enqueue_step(ctx);
+                ctx->graph_kernels = ctx->launches - before;
+                ctx->launches = before;  // capturing runs nothing
+                cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+                if (rc) {
+                    if (graph) cudaGraphDestroy(graph);
+                    return rc;
+                }
+                if (e != cudaSuccess) return fail(IPIC3D_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
+                e = cudaGraphInstantiate(&ctx->graph, graph, 0);
+                cudaGraphDestroy(graph);
+                if (e != cudaSuccess) return fail(IPIC3D_E_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+                ctx->graph_valid = true;
+            }
+            CU(cudaGraphLaunch(ctx->graph, ctx->stream));
+            ctx->launches += ctx->graph_kernels;
+        } else {
+            if ((rc = enqueue_step(ctx))) return rc;
+        }
+        ctx->steps++;
+    }
+    return after_steps(ctx);
+}
+
+int ipic3d_gpu_project(ipic3d_ctx* ctx) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if ((rc = project_impl(ctx))) return rc;
+    CU(cudaStreamSynchronize(ctx->stream));
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_update_boundaries(ipic3d_ctx* ctx) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (ctx->props.size[0] != ctx->props.size[1] || ctx->props.size[1] != ctx->props.size[2])
+        return fail(IPIC3D_E_INVALID, "updateFieldsOnBoundaries assumes a cubic grid (field.h:424)");
+    int n = launch_ghost(ctx->g, ctx->stream);
+    if ((rc = check_launch(ctx, n))) return rc;
+    CU(cudaStreamSynchronize(ctx->stream));
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_solve_fields(ipic3d_ctx* ctx) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if ((rc = solve_impl(ctx))) return rc;
+    CU(cudaStreamSynchronize(ctx->stream));
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_move(ipic3d_ctx* ctx) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if ((rc = move_impl(ctx, false))) return rc;
+    ctx->j_valid = false;
+    k_step_end<<<1, 1, 0, ctx->stream>>>(ctx->d_step);
+    if ((rc = check_launch(ctx, 1))) return rc;
+    return after_steps(ctx);
+}
+
+int ipic3d_gpu_conserved(ipic3d_ctx* ctx, ipic3d_conserved* out) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!out) return fail(IPIC3D_E_INVALID, "out == NULL");
+    cudaStream_t st = ctx->stream;
+    const int nb = reduce_blocks();
+    double res[3] = {0, 0, 0}, fres[2] = {0, 0};
+    double tot[3] = {0, 0, 0};
+    int n = 0;
+    auto one = [&](auto& P) -> int {
+        n += launch_reduce_particles(P.view(), (int)ctx->ncells(), ctx->d_partial, st);
+        n += launch_reduce_final(ctx->d_partial, nb, 3, ctx->d_result, st);
+        CU(cudaMemcpyAsync(res, ctx->d_result, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+        for (int k = 0; k < 3; ++k) tot[k] += res[k];
+        return IPIC3D_OK;
+    };
+    for (auto& P : ctx->p32)
+        if ((rc = one(P))) return rc;
+    for (auto& P : ctx->p64)
+        if ((rc = one(P))) return rc;
+    n += launch_reduce_fields(ctx->g, ctx->d_partial, st);
+    n += launch_reduce_final(ctx->d_partial, nb, 2, ctx->d_result, st);
+    CU(cudaMemcpyAsync(fres, ctx->d_result, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    if ((rc = check_launch(ctx, n))) return rc;
+    out->total_momentum = tot[0];
+    out->kinetic_energy = tot[1];
+    out->total_charge = tot[2];
+    out->e_energy = fres[0];
+    out->b_energy = fres[1];
+    uint64_t np = 0;
+    if ((rc = ipic3d_gpu_particle_count(ctx, &np))) return rc;
+    out->particles = np;
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_synchronize(ipic3d_ctx* ctx) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    CU(cudaStreamSynchronize(ctx->stream));
+    return IPIC3D_OK;
+}
+
+void* ipic3d_gpu_stream(ipic3d_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int ipic3d_gpu_stats(ipic3d_ctx* ctx, ipic3d_stats* out) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!out) return fail(IPIC3D_E_INVALID, "out == NULL");
+    std::memset(out, 0, sizeof(*out));
+    out->steps = ctx->steps;
+    uint64_t np = 0;
+    if ((rc = ipic3d_gpu_particle_count(ctx, &np))) return rc;
+    out->particles = np;
+    for (auto& P : ctx->p32) out->capacity += (uint64_t)P.capacity;
+    for (auto& P : ctx->p64) out->capacity += (uint64_t)P.capacity;
+    out->migrated_last = ctx->last.migrated;
+    out->removed_last = ctx->last.removed;
+    out->injected_last = ctx->last.injected;
+    out->rebuilds = ctx->rebuilds;
+    out->kernel_launches = ctx->launches;
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_boris(ipic3d_particle* particles, uint64_t n, const double E[3], const double B[3], double dt,
+                     uint64_t nsteps, int push_position) {
+    if (!particles || !E || !B) return fail(IPIC3D_E_INVALID, "NULL argument");
+    if (n == 0) return IPIC3D_OK;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(IPIC3D_E_NODEVICE, "no CUDA device");
+    void* d = nullptr;
+    CU(cudaMalloc(&d, n * sizeof(ipic3d_particle)));
+    cudaError_t e = cudaMemcpy(d, particles, n * sizeof(ipic3d_particle), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        launch_boris(d, n, E, B, dt, nsteps, push_position, d, nullptr);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(particles, d, n * sizeof(ipic3d_particle), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(IPIC3D_E_CUDA, "boris: %s", cudaGetErrorString(e));
+    return IPIC3D_OK;
+}
+
+}  // extern "C"

@@ -18,15 +18,15 @@ REFERENCE_ROOT = os.environ.get("IPIC3D_REFERENCE_ROOT", "/root/reference")
 
 
 def build(force=False):
-    src = os.path.join(HERE, "ipic3d_oracle.cpp")
+    srcs = [os.path.join(HERE, "ipic3d_oracle.cpp"), os.path.join(HERE, "ipic3d_oracle_init.cpp")]
     hdrs = [os.path.join(HERE, "ipic3d_oracle.h"), os.path.join(HERE, "..", "include", "ipic3d_gpu.h"),
             os.path.join(HERE, "..", "include", "ipic3d_types.h")]
-    newest = max(os.path.getmtime(p) for p in [src] + hdrs)
+    newest = max(os.path.getmtime(p) for p in srcs + hdrs)
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
         tmp = LIB + ".tmp"
         # -ffp-contract=off: no fused multiply-add, the reference's rounding
         subprocess.check_call(["g++", "-std=c++17", "-O3", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
-                               "-o", tmp, src])
+                               "-o", tmp] + srcs)
         os.replace(tmp, LIB)
     return LIB
 
@@ -68,6 +68,8 @@ def load():
         lib.oracle_boris.argtypes = [vp, C.c_uint64, vp, vp, C.c_double, C.c_uint64, C.c_int]
         lib.oracle_trilinear.argtypes = [vp, vp, C.c_double]
         lib.oracle_trilinear.restype = C.c_double
+        lib.oracle_init_uniform_pos_normal_speed.argtypes = [vp, C.c_uint64, vp, vp, vp, vp, vp, vp, vp]
+        lib.oracle_init_uniform_bench.argtypes = [vp, C.c_uint64, vp, vp]
         _oracle = lib
     return _oracle
 

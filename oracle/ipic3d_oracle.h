@@ -42,6 +42,13 @@ int oracle_conserved(oracle_sim* s, ipic3d_conserved* out);
 /* stats of the last move: particles that changed cell, removed, injected */
 int oracle_last_counts(oracle_sim* s, uint64_t* migrated, uint64_t* removed, uint64_t* injected);
 
+/* the reference's particle initialisations (ipic3d_oracle_init.cpp) */
+int oracle_init_uniform_pos_normal_speed(const ipic3d_props* props, uint64_t numParticles, const double low[3],
+                                         const double hig[3], const double mean[3], const double stddev[3],
+                                         ipic3d_particle* out, uint64_t* counts, uint64_t* n_out);
+int oracle_init_uniform_bench(const ipic3d_props* props, uint64_t numParticles, ipic3d_particle* out,
+                              uint64_t* counts);
+
 int oracle_boris(ipic3d_particle* p, uint64_t n, const double E[3], const double B[3], double dt, uint64_t nsteps,
                  int push_position);
 double oracle_trilinear(const double corners[8], const double pos[3], double vol);

@@ -1,0 +1,227 @@
+"""Generates the golden fixtures in this folder by running the reference's own
+code: the AllScale iPIC3D headers compiled against the AllScale shim into
+oracle/_ref/libipic3d_ref.so (oracle/ref/Makefile; needs the reference
+sources, so this script runs on the build machine only).
+
+    python tests/golden/make_golden.py
+
+Fixtures (all small):
+  inp_runs.json      test.inp / tiny.inp driver runs (src/ipic3d.cxx): the
+                     distribution parameters, sha256 of the initial and final
+                     particle bytes, per-cell counts after ncycles steps and
+                     the conserved quantities.
+  moves_small.npz    seeded scenarios through simulateSteps with the default
+                     policies (mover + export + import): inputs and outputs.
+  project_small.npz  projectToDensityField over all nodes.
+  fields_small.npz   updateFieldsOnBoundaries, two-phase leapfrog, forward
+                     solver at single nodes.
+"""
+import ctypes as C
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+from allscale_ipic3d_gb300 import abi  # noqa: E402
+
+ref = oracle.load_reference()
+if ref is None:
+    sys.exit("the reference library could not be built (reference sources missing?)")
+
+
+def props_to_dict(p):
+    return {"size": list(p.size), "cell_width": list(p.cell_width), "dt": p.dt, "speed_of_light": p.speed_of_light,
+            "planet_radius": p.planet_radius, "object_center": list(p.object_center), "origin": list(p.origin),
+            "external_b": list(p.external_b)}
+
+
+def props_vec(p):
+    """props as a flat float64 vector (size, width, dt, c, R, center, origin, Bext)."""
+    return np.array(list(p.size) + list(p.cell_width) + [p.dt, p.speed_of_light, p.planet_radius] +
+                    list(p.object_center) + list(p.origin) + list(p.external_b), np.float64)
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).view(np.uint8).tobytes()).hexdigest()
+
+
+def ref_simulate(props, parts, counts, steps):
+    n = len(parts)
+    out = np.zeros(n, abi.PARTICLE_DTYPE)
+    oc = np.zeros(props.ncells, np.uint64)
+    ids = np.zeros(n, np.uint32)
+    rc = ref.ref_simulate_default(C.byref(props), abi.vptr(parts), abi.vptr(counts), steps, abi.vptr(out), n,
+                                  abi.vptr(oc), abi.vptr(ids))
+    assert rc == 0
+    m = int(oc.sum())
+    return out[:m].copy(), oc, ids[:m].copy()
+
+
+def inp_runs():
+    res = {}
+    for name in ("test", "tiny"):
+        path = os.path.join(oracle.REFERENCE_ROOT, "inputs", name + ".inp").encode()
+        props = abi.Props()
+        ncyc = C.c_uint64()
+        n = C.c_uint64()
+        ref.ref_init_from_inp(path, C.byref(props), C.byref(ncyc), None, 0, None, C.byref(n), None)
+        N = n.value
+        parts = np.zeros(N, abi.PARTICLE_DTYPE)
+        counts = np.zeros(props.ncells, np.uint64)
+        field = np.zeros(abi.field_shape(props))
+        ref.ref_init_from_inp(path, C.byref(props), C.byref(ncyc), abi.vptr(parts), N, abi.vptr(counts),
+                              C.byref(n), abi.vptr(field))
+        usize = np.array(props.cell_width) * np.array(props.size)
+        low = np.array(props.origin) + 0.125 * usize
+        hig = low + 0.75 * usize
+        c, e, m = 299792458.0, 1.602176565e-19, 1.672621777e-27
+        vmod = c / np.sqrt(1.0 + (m * c * c) / (1e7 * e))
+        steps = ncyc.value
+        out, oc, ids = ref_simulate(props, parts, counts, steps)
+        cons = abi.Conserved()
+        ref.ref_conserved(C.byref(props), abi.vptr(out), abi.vptr(oc), abi.vptr(field), C.byref(cons))
+        res[name] = {
+            "props": props_to_dict(props), "num_particles": N, "ncycles": steps,
+            "low": low.tolist(), "hig": hig.tolist(), "mean": [0.0, 0.0, 0.0], "stddev": [vmod] * 3,
+            "initial_counts_sha256": sha(counts), "initial_particles_sha256": sha(parts),
+            "final_counts": oc.tolist(), "final_total": int(oc.sum()),
+            "final_particles_sha256": sha(out), "final_ids_sha256": sha(ids),
+            "conserved": cons.as_dict(),
+        }
+        print(name, N, "->", int(oc.sum()))
+    with open(os.path.join(HERE, "inp_runs.json"), "w") as f:
+        json.dump(res, f, indent=1)
+
+
+def scatter_into_cells(props, pos, rng_order=None):
+    """Groups particles by the cell their position falls in (row-major)."""
+    s = np.array(props.size)
+    w = np.array(props.cell_width)
+    o = np.array(props.origin)
+    c = np.floor((pos - o) / w).astype(np.int64)
+    c = np.clip(c, 0, s - 1)
+    flat = (c[:, 0] * s[1] + c[:, 1]) * s[2] + c[:, 2]
+    order = np.argsort(flat, kind="stable")
+    counts = np.bincount(flat, minlength=props.ncells).astype(np.uint64)
+    return order, counts
+
+
+def make_scenario(seed, size, width, origin, dt, ppc, vscale, planet=0.0, bz=0.0, qom=1.0, q=1.0, ragged=False):
+    rng = np.random.default_rng(seed)
+    props = abi.Props.make(size=size, cell_width=width, dt=dt, speed_of_light=1.0, planet_radius=planet,
+                           origin=origin, external_b=(0.0, 0.0, bz))
+    s = np.array(size)
+    nc = int(np.prod(s))
+    if ragged:
+        per = rng.integers(0, 2 * ppc + 1, nc)
+        per[rng.random(nc) < 0.2] = 0
+    else:
+        per = np.full(nc, ppc)
+    n = int(per.sum())
+    cell = np.repeat(np.arange(nc), per)
+    cz = cell % s[2]
+    cy = (cell // s[2]) % s[1]
+    cx = cell // (s[1] * s[2])
+    frac = rng.random((n, 3))
+    pos = np.array(origin) + (np.stack([cx, cy, cz], 1) + frac) * np.array(width)
+    parts = np.zeros(n, abi.PARTICLE_DTYPE)
+    parts["position"] = pos
+    parts["velocity"] = rng.normal(0.0, vscale, (n, 3))
+    parts["q"] = q
+    parts["qom"] = qom
+    # two species in some scenarios
+    if seed % 2 == 1 and n:
+        sel = rng.random(n) < 0.3
+        parts["q"][sel] = -q
+        parts["qom"][sel] = -qom * 0.5
+    counts = per.astype(np.uint64)
+    return props, parts, counts
+
+
+SCENARIOS = {
+    # name: (kwargs, steps)
+    "walls": (dict(seed=1, size=(4, 4, 4), width=(1.0, 1.0, 1.0), origin=(0.0, 0.0, 0.0), dt=0.5, ppc=8,
+                   vscale=0.6), 12),
+    "dipole": (dict(seed=2, size=(6, 6, 6), width=(1.0, 1.0, 1.0), origin=(-3.0, -3.0, -3.0), dt=0.1, ppc=8,
+                    vscale=0.3, planet=1.0, bz=2.0, qom=-1.0), 10),
+    "ragged": (dict(seed=3, size=(5, 3, 2), width=(0.5, 1.0, 2.0), origin=(-1.0, 0.5, -2.0), dt=0.2, ppc=10,
+                    vscale=0.8, planet=0.3, bz=1.5, qom=2.0, ragged=True), 8),
+    "single": (dict(seed=4, size=(1, 1, 1), width=(1.0, 1.0, 1.0), origin=(0.0, 0.0, 0.0), dt=0.3, ppc=16,
+                    vscale=1.0), 5),
+    "fast": (dict(seed=5, size=(4, 4, 4), width=(1.0, 1.0, 1.0), origin=(0.0, 0.0, 0.0), dt=1.0, ppc=4,
+                  vscale=1.5), 6),
+    "strong": (dict(seed=7, size=(8, 8, 8), width=(0.5, 0.5, 0.5), origin=(-2.0, -2.0, -2.0), dt=0.05, ppc=6,
+                    vscale=0.5, planet=0.4, bz=40.0, qom=-3.0), 6),
+}
+
+
+def moves_small():
+    out = {}
+    for name, (kw, steps) in SCENARIOS.items():
+        props, parts, counts = make_scenario(**kw)
+        res, rc, ids = ref_simulate(props, parts, counts, steps)
+        out[name + "_props"] = props_vec(props)
+        out[name + "_in"] = parts
+        out[name + "_in_counts"] = counts
+        out[name + "_steps"] = np.array([steps])
+        out[name + "_out"] = res
+        out[name + "_out_counts"] = rc
+        out[name + "_out_ids"] = ids
+        print(name, len(parts), "->", len(res))
+    np.savez_compressed(os.path.join(HERE, "moves_small.npz"), **out)
+
+
+def project_small():
+    out = {}
+    for name, kw in {"p3": dict(seed=11, size=(3, 3, 3), width=(0.5, 0.5, 0.5), origin=(0.0, 0.0, 0.0), dt=0.1,
+                                ppc=6, vscale=1.0),
+                     "p435": dict(seed=12, size=(4, 3, 5), width=(1.0, 2.0, 0.5), origin=(-1.0, 0.0, 1.0), dt=0.1,
+                                  ppc=5, vscale=1.0, ragged=True)}.items():
+        props, parts, counts = make_scenario(**kw)
+        J = np.zeros(abi.density_shape(props))
+        ref.ref_project_current(C.byref(props), abi.vptr(parts), abi.vptr(counts), abi.vptr(J))
+        out[name + "_props"] = props_vec(props)
+        out[name + "_in"] = parts
+        out[name + "_in_counts"] = counts
+        out[name + "_J"] = J
+    np.savez_compressed(os.path.join(HERE, "project_small.npz"), **out)
+
+
+def fields_small():
+    rng = np.random.default_rng(21)
+    out = {}
+    props = abi.Props.make(size=(4, 4, 4), cell_width=(1.0, 0.5, 2.0), dt=0.05, speed_of_light=1.3)
+    f0 = rng.normal(0, 1, abi.field_shape(props))
+    b0 = rng.normal(0, 1, abi.bcfield_shape(props))
+    j0 = rng.normal(0, 1, abi.density_shape(props))
+    f1, b1 = f0.copy(), b0.copy()
+    ref.ref_update_boundaries(C.byref(props), abi.vptr(f1), abi.vptr(b1))
+    f2, b2 = f0.copy(), b0.copy()
+    ref.ref_leapfrog_two_phase(C.byref(props), abi.vptr(f2), abi.vptr(b2), abi.vptr(j0))
+    out.update(props=props_vec(props), field=f0, bcfield=b0, J=j0, bnd_field=f1, bnd_bcfield=b1, lf_field=f2,
+               lf_bcfield=b2)
+    # forward solver at three interior nodes, each on the initial fields
+    nodes = np.array([[2, 2, 2], [1, 3, 2], [4, 4, 1]], np.int64)
+    ff, fb = [], []
+    for nd in nodes:
+        f3, b3 = f0.copy(), b0.copy()
+        ref.ref_solve_forward_at(C.byref(props), abi.vptr(np.ascontiguousarray(nd)), abi.vptr(f3), abi.vptr(b3),
+                                 abi.vptr(j0))
+        ff.append(f3)
+        fb.append(b3)
+    out.update(fw_nodes=nodes, fw_field=np.stack(ff), fw_bcfield=np.stack(fb))
+    np.savez_compressed(os.path.join(HERE, "fields_small.npz"), **out)
+
+
+if __name__ == "__main__":
+    moves_small()
+    project_small()
+    fields_small()
+    inp_runs()
