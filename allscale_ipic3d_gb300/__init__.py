@@ -59,6 +59,8 @@ _SIGNATURES = [
     ("ipic3d_gpu_synchronize", C.c_int, [_vp]),
     ("ipic3d_gpu_stream", _vp, [_vp]),
     ("ipic3d_gpu_stats", C.c_int, [_vp, _vp]),
+    ("ipic3d_gpu_profile", C.c_int, [_vp, C.c_int]),
+    ("ipic3d_gpu_profile_read", C.c_int, [_vp, _vp, C.c_int]),
     ("ipic3d_gpu_boris", C.c_int, [_vp, C.c_uint64, _vp, _vp, C.c_double, C.c_uint64, C.c_int]),
     ("ipic3d_gpu_last_error", C.c_int, [C.c_char_p, C.c_size_t]),
 ]
@@ -224,6 +226,15 @@ class Simulation:
     def stats(self):
         out = Stats()
         _check(library().ipic3d_gpu_stats(self._ctx, C.byref(out)))
+        return out.as_dict()
+
+    def profile(self, enable=True):
+        """Per-phase CUDA-event timing of the following steps (no graph)."""
+        _check(library().ipic3d_gpu_profile(self._ctx, 1 if enable else 0))
+
+    def profile_read(self, reset=True):
+        out = abi.Profile()
+        _check(library().ipic3d_gpu_profile_read(self._ctx, C.byref(out), 1 if reset else 0))
         return out.as_dict()
 
     @property

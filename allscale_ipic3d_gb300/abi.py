@@ -142,6 +142,17 @@ class Stats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+PHASES = ["push", "pending", "inject", "place", "fields", "moments", "unused6", "unused7"]
+
+
+class Profile(C.Structure):
+    _fields_ = [("ms", C.c_double * 8), ("launches", C.c_uint64 * 8), ("particles", C.c_uint64 * 8)]
+
+    def as_dict(self):
+        return {PHASES[i]: {"ms": self.ms[i], "launches": self.launches[i], "particles": self.particles[i]}
+                for i in range(6)}
+
+
 # Particle (particle.h:9-60): 8 doubles, 64 bytes
 PARTICLE_DTYPE = np.dtype([("position", "<f8", (3,)), ("velocity", "<f8", (3,)), ("q", "<f8"), ("qom", "<f8")])
 assert PARTICLE_DTYPE.itemsize == 64

@@ -24,6 +24,7 @@ SOURCES = {
     "particles_fp64.cu": ["-fmad=false"],
     "particles_fp32.cu": [],
     "fields.cu": ["-fmad=false"],
+    "upload.cu": ["-fmad=false"],
 }
 
 

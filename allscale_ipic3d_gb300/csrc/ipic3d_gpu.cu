@@ -20,6 +20,7 @@
 
 #include "../../include/ipic3d_gpu.h"
 #include "launch.h"
+#include "upload.h"
 
 namespace ipg {
 namespace {
@@ -102,6 +103,7 @@ struct PopStore {
 }  // namespace ipg
 
 namespace ipg {
+constexpr int kMaxPops = 16;
 // Advances the device step counter (keys the injection generator).
 __global__ void k_step_end(uint64_t* step) { *step += 1; }
 }  // namespace ipg
@@ -127,6 +129,29 @@ struct ipic3d_ctx {
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
     uint64_t graph_kernels = 0;  // kernels one replay runs
+    // pending-list watch: per step an async copy of the pending counts into
+    // pinned memory, read one step later (ring of two)
+    uint32_t* h_pending = nullptr;  // [2][kMaxPops]
+    cudaEvent_t pend_ev[2] = {nullptr, nullptr};
+    uint64_t particles_hint = 0;
+    // species table of the populations (index = population) and the device
+    // staging buffers of the upload path
+    std::vector<std::pair<double, double>> species;
+    void* st_parts = nullptr;
+    size_t st_parts_cap = 0;
+    uint32_t* st_ids = nullptr;
+    size_t st_ids_cap = 0;
+    uint8_t* st_sid = nullptr;
+    size_t st_sid_cap = 0;
+    int64_t* st_off = nullptr;
+    int32_t* st_cnt = nullptr;
+    int* st_unknown = nullptr;
+    // per-phase event timing
+    bool profiling = false;
+    cudaEvent_t ph_ev[IPIC3D_PHASE_COUNT][2] = {};
+    bool ph_open[IPIC3D_PHASE_COUNT] = {};
+    ipic3d_profile prof{};
+    uint64_t push_particles = 0;
 
     int npops() const { return fp32 ? (int)p32.size() : (int)p64.size(); }
     int64_t nfield() const { return (props.size[0] + 3) * (props.size[1] + 3) * (props.size[2] + 3); }
@@ -167,7 +192,8 @@ int alloc_pop(ipic3d_ctx* ctx, PopStore<T>& P, const std::vector<uint64_t>& coun
     P.h_start.assign(nc + 1, 0);
     for (int64_t c = 0; c < nc; ++c) P.h_start[c + 1] = P.h_start[c] + cell_capacity(ctx->cfg, counts[c]);
     P.capacity = P.h_start[nc];
-    P.pending_cap = (uint32_t)std::min<int64_t>(std::max<int64_t>(1 << 16, P.capacity / 4), 0x7fffffff);
+    // every particle can wait at most once per step: capacity entries suffice
+    P.pending_cap = (uint32_t)std::min<int64_t>(std::max<int64_t>(1 << 12, P.capacity), 0x7fffffff);
     int64_t inject_cap = 0;
     if (ctx->cfg.flags & IPIC3D_F_INJECT_LOW_X)
         inject_cap = (int64_t)(ctx->props.size[1] * ctx->props.size[2]) * ((int64_t)ctx->cfg.inject_per_cell + 1);
@@ -293,6 +319,8 @@ int upload_impl(ipic3d_ctx* ctx, const ipic3d_particle* parts, const uint64_t* c
     }
     drop_graph(ctx);
     release_pops(ctx);
+    ctx->species.clear();
+    for (auto& x : sp) ctx->species.push_back({x.q, x.qom});
     for (size_t s = 0; s < sp.size(); ++s) {
         int rc;
         if (ctx->fp32) {
@@ -312,6 +340,130 @@ int upload_impl(ipic3d_ctx* ctx, const ipic3d_particle* parts, const uint64_t* c
         }
     }
     ctx->j_valid = false;
+    ctx->particles_hint = n;
+    return IPIC3D_OK;
+}
+
+int check_launch(ipic3d_ctx* ctx, int n);
+
+template <typename X>
+int grow(X*& p, size_t& cap, size_t need) {
+    if (need <= cap && p) return IPIC3D_OK;
+    dfree(p);
+    size_t n = std::max<size_t>(need, 1);
+    CU(cudaMalloc(&p, n * sizeof(X)));
+    cap = n;
+    return IPIC3D_OK;
+}
+
+template <typename T>
+int scatter_pops(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, const std::vector<std::vector<uint64_t>>& cnt,
+                 int64_t n, bool have_ids, bool& relaid) {
+    const int64_t nc = ctx->ncells();
+    int rc;
+    relaid = false;
+    for (size_t k = 0; k < pops.size(); ++k) {
+        auto& P = pops[k];
+        bool fits = (int64_t)P.h_start.size() == nc + 1;
+        for (int64_t c = 0; fits && c < nc; ++c) fits = (int64_t)cnt[k][c] <= P.h_start[c + 1] - P.h_start[c];
+        if (!fits) {
+            double q = P.q, qom = P.qom;
+            P.release();
+            P.q = q;
+            P.qom = qom;
+            if ((rc = alloc_pop(ctx, P, cnt[k], 0))) return rc;
+            relaid = true;
+        }
+    }
+    UploadPops<T> U{};
+    U.npop = (int)pops.size();
+    U.relative = std::is_same<T, float>::value ? 1 : 0;
+    for (size_t k = 0; k < pops.size(); ++k) {
+        auto& P = pops[k];
+        U.x[k] = P.x; U.y[k] = P.y; U.z[k] = P.z; U.u[k] = P.u; U.v[k] = P.v; U.w[k] = P.w;
+        U.id[k] = P.id;
+        U.start[k] = P.start;
+        U.count[k] = P.count;
+        cudaStream_t st = ctx->stream;
+        CU(cudaMemsetAsync(P.hole_cnt, 0, nc * sizeof(int32_t), st));
+        CU(cudaMemsetAsync(P.arr_cnt, 0, nc * sizeof(int32_t), st));
+        CU(cudaMemsetAsync(P.pending_in_count, 0, sizeof(uint32_t), st));
+        CU(cudaMemsetAsync(P.ctr, 0, sizeof(StepCounters), st));
+    }
+    UploadGeom g;
+    g.ncells = (int)nc;
+    g.sx = (int)ctx->props.size[0];
+    g.sy = (int)ctx->props.size[1];
+    g.sz = (int)ctx->props.size[2];
+    for (int a = 0; a < 3; ++a) {
+        g.origin[a] = ctx->props.origin[a];
+        g.w[a] = ctx->props.cell_width[a];
+    }
+    int nl = launch_scatter<T>(ctx->st_parts, have_ids ? ctx->st_ids : nullptr, ctx->st_sid, ctx->st_off, U, g,
+                               ctx->stream);
+    (void)n;
+    return check_launch(ctx, nl);
+}
+
+// Upload through the device: one copy of the AoS records, then the species
+// classification and the scatter run on the GPU. Returns 1 when the host
+// path must be taken instead (a species the context does not know yet).
+int upload_device(ipic3d_ctx* ctx, const ipic3d_particle* parts, const uint64_t* cell_counts, const uint32_t* ids) {
+    const int64_t nc = ctx->ncells();
+    const int npop = ctx->npops();
+    if (ctx->species.empty() || npop != (int)ctx->species.size() || npop > kUploadMaxPops) return 1;
+    std::vector<int64_t> off(nc + 1, 0);
+    for (int64_t c = 0; c < nc; ++c) off[c + 1] = off[c] + (int64_t)cell_counts[c];
+    const int64_t n = off[nc];
+    if (n == 0) return 1;
+    int rc;
+    size_t cap_off = 0, cap_cnt = 0, cap_u = 0;
+    if ((rc = grow(reinterpret_cast<char*&>(ctx->st_parts), ctx->st_parts_cap, (size_t)n * sizeof(ipic3d_particle))))
+        return rc;
+    if (ids && (rc = grow(ctx->st_ids, ctx->st_ids_cap, (size_t)n))) return rc;
+    if ((rc = grow(ctx->st_sid, ctx->st_sid_cap, (size_t)n))) return rc;
+    dfree(ctx->st_off);
+    dfree(ctx->st_cnt);
+    if ((rc = grow(ctx->st_off, cap_off, (size_t)nc + 1))) return rc;
+    if ((rc = grow(ctx->st_cnt, cap_cnt, (size_t)nc * npop))) return rc;
+    if (!ctx->st_unknown && (rc = grow(ctx->st_unknown, cap_u, 1))) return rc;
+    cudaStream_t st = ctx->stream;
+    CU(cudaMemcpyAsync(ctx->st_parts, parts, (size_t)n * sizeof(ipic3d_particle), cudaMemcpyHostToDevice, st));
+    if (ids) CU(cudaMemcpyAsync(ctx->st_ids, ids, (size_t)n * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(ctx->st_off, off.data(), (nc + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    CU(cudaMemsetAsync(ctx->st_unknown, 0, sizeof(int), st));
+    SpeciesTable sp{};
+    sp.n = npop;
+    for (int k = 0; k < npop; ++k) {
+        sp.q[k] = ctx->species[k].first;
+        sp.qom[k] = ctx->species[k].second;
+    }
+    int nl = launch_classify(ctx->st_parts, n, sp, ctx->st_sid, ctx->st_unknown, st);
+    std::vector<std::vector<uint64_t>> cnt(npop, std::vector<uint64_t>(nc, 0));
+    if (npop == 1) {
+        for (int64_t c = 0; c < nc; ++c) cnt[0][c] = cell_counts[c];
+    } else {
+        nl += launch_count(ctx->st_sid, ctx->st_off, (int)nc, npop, ctx->st_cnt, st);
+    }
+    if ((rc = check_launch(ctx, nl))) return rc;
+    int unknown = 0;
+    CU(cudaMemcpyAsync(&unknown, ctx->st_unknown, sizeof(int), cudaMemcpyDeviceToHost, st));
+    std::vector<int32_t> hc(npop > 1 ? (size_t)nc * npop : 0);
+    if (npop > 1) CU(cudaMemcpyAsync(hc.data(), ctx->st_cnt, hc.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    if (unknown) return 1;
+    if (npop > 1)
+        for (int k = 0; k < npop; ++k)
+            for (int64_t c = 0; c < nc; ++c) cnt[k][c] = (uint64_t)hc[(size_t)k * nc + c];
+    bool relaid = false;
+    if (ctx->fp32)
+        rc = scatter_pops(ctx, ctx->p32, cnt, n, ids != nullptr, relaid);
+    else
+        rc = scatter_pops(ctx, ctx->p64, cnt, n, ids != nullptr, relaid);
+    if (rc) return rc;
+    if (relaid) drop_graph(ctx);
+    ctx->j_valid = false;
+    ctx->particles_hint = (uint64_t)n;
     return IPIC3D_OK;
 }
 
@@ -440,6 +592,32 @@ int check_launch(ipic3d_ctx* ctx, int n) {
     return IPIC3D_OK;
 }
 
+// Phase brackets: events recorded only while profiling.
+void ph_begin(ipic3d_ctx* ctx, int ph) {
+    if (!ctx->profiling) return;
+    cudaEventRecord(ctx->ph_ev[ph][0], ctx->stream);
+    ctx->ph_open[ph] = true;
+}
+void ph_end(ipic3d_ctx* ctx, int ph) {
+    if (!ctx->profiling || !ctx->ph_open[ph]) return;
+    cudaEventRecord(ctx->ph_ev[ph][1], ctx->stream);
+}
+// After a profiled step: add the closed intervals to the totals.
+int ph_collect(ipic3d_ctx* ctx) {
+    if (!ctx->profiling) return IPIC3D_OK;
+    CU(cudaStreamSynchronize(ctx->stream));
+    for (int ph = 0; ph < IPIC3D_PHASE_COUNT; ++ph) {
+        if (!ctx->ph_open[ph]) continue;
+        float ms = 0.f;
+        CU(cudaEventElapsedTime(&ms, ctx->ph_ev[ph][0], ctx->ph_ev[ph][1]));
+        ctx->prof.ms[ph] += ms;
+        ctx->prof.launches[ph] += 1;
+        ctx->ph_open[ph] = false;
+    }
+    ctx->prof.particles[IPIC3D_PHASE_PUSH] += ctx->push_particles;
+    return IPIC3D_OK;
+}
+
 // projectToDensityField over the stored particles (deposit-only pass).
 int project_impl(ipic3d_ctx* ctx) {
     cudaStream_t st = ctx->stream;
@@ -458,12 +636,14 @@ int project_impl(ipic3d_ctx* ctx) {
 int solve_impl(ipic3d_ctx* ctx) {
     cudaStream_t st = ctx->stream;
     int n = 0;
+    ph_begin(ctx, IPIC3D_PHASE_FIELDS);
     if (ctx->cfg.solver == IPIC3D_SOLVER_LEAPFROG)
         n += launch_leapfrog(ctx->g, (ctx->cfg.flags & IPIC3D_F_REFRESH_NODE_B) != 0, st);
     else if (ctx->cfg.solver == IPIC3D_SOLVER_FORWARD)
         n += launch_forward(ctx->g, st);
     if (ctx->fp32 && ctx->cfg.mover == IPIC3D_MOVER_FIELD && ctx->cfg.solver != IPIC3D_SOLVER_STATIC)
         n += launch_node32(ctx->g, ctx->node32, st);
+    ph_end(ctx, IPIC3D_PHASE_FIELDS);
     return check_launch(ctx, n);
 }
 
@@ -477,23 +657,32 @@ int move_impl(ipic3d_ctx* ctx, bool deposit) {
     for (auto& P : ctx->p32) CU(cudaMemsetAsync(P.ctr, 0, offsetof(StepCounters, lost), st));
     for (auto& P : ctx->p64) CU(cudaMemsetAsync(P.ctr, 0, offsetof(StepCounters, lost), st));
     if (deposit) {
+        ph_begin(ctx, IPIC3D_PHASE_MOMENTS);
         CU(cudaMemsetAsync(ctx->J, 0, ctx->nnode() * 3 * sizeof(double), st));
         CU(cudaMemsetAsync(ctx->rho, 0, ctx->nnode() * sizeof(double), st));
     }
+    ph_begin(ctx, IPIC3D_PHASE_PUSH);
     for (auto& P : ctx->p32) n += launch_push<float>(g, P.view(), 0, st);
     for (auto& P : ctx->p64) n += launch_push<double>(g, P.view(), 0, st);
+    ph_end(ctx, IPIC3D_PHASE_PUSH);
+    ctx->push_particles = ctx->particles_hint;
+    ph_begin(ctx, IPIC3D_PHASE_PENDING);
     for (auto& P : ctx->p32) n += launch_push_pending<float>(g, P.view(), st);
     for (auto& P : ctx->p64) n += launch_push_pending<double>(g, P.view(), st);
+    ph_end(ctx, IPIC3D_PHASE_PENDING);
     const bool inject = (ctx->cfg.flags & IPIC3D_F_INJECT_LOW_X) && ctx->cfg.bc_low[0] == IPIC3D_BC_OPEN &&
                         ctx->cfg.inject_per_cell > 0;
     if (inject) {
+        ph_begin(ctx, IPIC3D_PHASE_INJECT);
         if (ctx->fp32)
             n += launch_inject<float>(g, ctx->p32[0].view(), ctx->cfg.inject_per_cell, ctx->cfg.inject_drift,
                                       ctx->cfg.inject_vth, ctx->cfg.seed, ctx->d_step, st);
         else
             n += launch_inject<double>(g, ctx->p64[0].view(), ctx->cfg.inject_per_cell, ctx->cfg.inject_drift,
                                        ctx->cfg.inject_vth, ctx->cfg.seed, ctx->d_step, st);
+        ph_end(ctx, IPIC3D_PHASE_INJECT);
     }
+    ph_begin(ctx, IPIC3D_PHASE_PLACE);
     for (auto& P : ctx->p32) {
         n += launch_place<float>(g, P.view(), P.sort_tmp, st);
         n += launch_pending_rotate<float>(P.view(), P.pending_in_count, st);
@@ -502,7 +691,11 @@ int move_impl(ipic3d_ctx* ctx, bool deposit) {
         n += launch_place<double>(g, P.view(), P.sort_tmp, st);
         n += launch_pending_rotate<double>(P.view(), P.pending_in_count, st);
     }
-    if (deposit) n += launch_j_finalize(g, (ctx->cfg.flags & IPIC3D_F_J_DIV8) != 0, st);
+    ph_end(ctx, IPIC3D_PHASE_PLACE);
+    if (deposit) {
+        n += launch_j_finalize(g, (ctx->cfg.flags & IPIC3D_F_J_DIV8) != 0, st);
+        ph_end(ctx, IPIC3D_PHASE_MOMENTS);
+    }
     return check_launch(ctx, n);
 }
 
@@ -647,6 +840,9 @@ int ipic3d_gpu_create(const ipic3d_props* props, const ipic3d_config* cfg, ipic3
     CUB(cudaMemsetAsync(ctx->rho, 0, ctx->nnode() * sizeof(double), ctx->stream));
     CUB(cudaMemsetAsync(ctx->node32, 0, ctx->nfield() * 2 * sizeof(float4), ctx->stream));
     CUB(cudaMemsetAsync(ctx->d_step, 0, sizeof(uint64_t), ctx->stream));
+    CUB(cudaMallocHost(&ctx->h_pending, 2 * kMaxPops * sizeof(uint32_t)));
+    std::memset(ctx->h_pending, 0, 2 * kMaxPops * sizeof(uint32_t));
+    for (auto& e : ctx->pend_ev) CUB(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
 #undef CUB
     refresh_geom(ctx);
     // an empty particle set so that every call works before the first upload
@@ -671,6 +867,18 @@ int ipic3d_gpu_destroy(ipic3d_ctx* ctx) {
     dfree(ctx->d_step);
     dfree(ctx->d_partial);
     dfree(ctx->d_result);
+    if (ctx->h_pending) cudaFreeHost(ctx->h_pending);
+    dfree(ctx->st_parts);
+    dfree(ctx->st_ids);
+    dfree(ctx->st_sid);
+    dfree(ctx->st_off);
+    dfree(ctx->st_cnt);
+    dfree(ctx->st_unknown);
+    for (auto& e : ctx->pend_ev)
+        if (e) cudaEventDestroy(e);
+    for (auto& pair : ctx->ph_ev)
+        for (auto& e : pair)
+            if (e) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return IPIC3D_OK;
@@ -681,6 +889,10 @@ int ipic3d_gpu_upload_particles(ipic3d_ctx* ctx, const ipic3d_particle* particle
     int rc = check_ctx(ctx);
     if (rc) return rc;
     if (!cell_counts) return fail(IPIC3D_E_INVALID, "cell_counts == NULL");
+    if (particles) {
+        rc = upload_device(ctx, particles, cell_counts, ids);
+        if (rc <= 0) return rc;  // done (0) or failed (< 0); 1 = take the host path
+    }
     return upload_impl(ctx, particles, cell_counts, ids);
 }
 
@@ -789,8 +1001,11 @@ int ipic3d_gpu_step(ipic3d_ctx* ctx, uint64_t num_steps) {
     if (num_steps == 0) return IPIC3D_OK;
     if (ctx->cfg.projector == IPIC3D_PROJECT_CIC && !ctx->j_valid)
         if ((rc = project_impl(ctx))) return rc;
-    const bool use_graph = (ctx->cfg.flags & IPIC3D_F_USE_GRAPH) != 0;
-    for (uint64_t i = 0; i < num_steps; ++i) {
+    const bool use_graph = (ctx->cfg.flags & IPIC3D_F_USE_GRAPH) != 0 && !ctx->profiling;
+    // re-lay out when more than 0.5% of the particles wait for a slot
+    const uint64_t pend_limit = std::max<uint64_t>(1024, ctx->particles_hint / 200);
+    uint64_t watch_from = 0;  // first step whose pending count is still meaningful
+    for (uint64_t done = 0; done < num_steps;) {
         if (use_graph) {
             if (!ctx->graph_valid) {
                 cudaGraph_t graph = nullptr;
@@ -814,8 +1029,33 @@ int ipic3d_gpu_step(ipic3d_ctx* ctx, uint64_t num_steps) {
             ctx->launches += ctx->graph_kernels;
         } else {
             if ((rc = enqueue_step(ctx))) return rc;
+            if ((rc = ph_collect(ctx))) return rc;
         }
-        ctx->steps++;
+        // this step's pending count -> pinned slot (done & 1)
+        const int slot = (int)(done & 1);
+        int k = 0;
+        for (auto& P : ctx->p32)
+            if (k < kMaxPops)
+                CU(cudaMemcpyAsync(ctx->h_pending + slot * kMaxPops + k++, &P.ctr->pending_out, sizeof(uint32_t),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+        for (auto& P : ctx->p64)
+            if (k < kMaxPops)
+                CU(cudaMemcpyAsync(ctx->h_pending + slot * kMaxPops + k++, &P.ctr->pending_out, sizeof(uint32_t),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+        CU(cudaEventRecord(ctx->pend_ev[slot], ctx->stream));
+        ++done;
+        ++ctx->steps;
+        // the previous step's count (the GPU works on this step meanwhile)
+        if (done >= 2 && done - 2 >= watch_from && done < num_steps) {
+            const int ps = (int)((done - 2) & 1);
+            CU(cudaEventSynchronize(ctx->pend_ev[ps]));
+            uint64_t pend = 0;
+            for (int q = 0; q < k; ++q) pend += ctx->h_pending[ps * kMaxPops + q];
+            if (pend > pend_limit) {
+                if ((rc = after_steps(ctx))) return rc;  // waits, then re-lays out
+                watch_from = done;  // counts recorded before the re-layout are stale
+            }
+        }
     }
     return after_steps(ctx);
 }
@@ -919,6 +1159,25 @@ int ipic3d_gpu_stats(ipic3d_ctx* ctx, ipic3d_stats* out) {
     out->injected_last = ctx->last.injected;
     out->rebuilds = ctx->rebuilds;
     out->kernel_launches = ctx->launches;
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_profile(ipic3d_ctx* ctx, int enable) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (enable && !ctx->ph_ev[0][0])
+        for (auto& pair : ctx->ph_ev)
+            for (auto& e : pair) CU(cudaEventCreate(&e));
+    ctx->profiling = enable != 0;
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_profile_read(ipic3d_ctx* ctx, ipic3d_profile* out, int reset) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!out) return fail(IPIC3D_E_INVALID, "out == NULL");
+    *out = ctx->prof;
+    if (reset) std::memset(&ctx->prof, 0, sizeof(ctx->prof));
     return IPIC3D_OK;
 }
 

@@ -1,0 +1,369 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 particle path: particle-steps/s of the full
+timestep (push + deposit + migrate + field update) on the dipole
+magnetosphere workload:
+
+  32^3 unit cells, 256 particles per cell (8,388,608): a neutral plasma of
+  electrons (q = -1/128, q/m = -1) and ions (q = +1/128, q/m = 0.01), 128 of
+  each per cell, drifting Maxwellian v = (0.02, 0, 0) + N(0, 0.005); a static
+  dipole B at the grid centre, moment set so |B| = 0.5 at 4 cells (B_z = 4,
+  the 2 innermost cells masked: planetRadius = 2); electrons injected at the
+  -x face, outflow at +x, periodic in y and z; dt = 0.05, c = 1.
+  FP32 push/deposit with cell-relative positions (headline) and the FP64 GPU
+  path on the same inputs.
+
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+
+Prints one JSON line. Under torchrun (N > 1) every rank runs an independent
+replica (the path runs on one GPU; no collective on the data path) and rank 0
+prints the whole-job value. `--impl reference` times the reference's CPU
+algorithm (the CPU oracle: a restatement of the reference's timestep with its
+data organisation) on the host cores, rank 0 only.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/sec (push+deposit+migrate), FP32 vs FP64 GPU at stated error"
+UNIT = "particle-steps/s"
+CELLS = 32
+PPC_SPECIES = 128
+DT = 0.05
+DRIFT = (0.02, 0.0, 0.0)
+VTH = 0.005
+WORKLOAD = ("dipole magnetosphere: 32^3 cells x 256 particles/cell (8,388,608; e-/ion 128+128), dipole |B|=0.5 at "
+            "r=4 cells, core r<2 masked, drift vx=0.02 sigma=0.005, inject -x / outflow +x, dt=0.05")
+
+
+def make_workload(seed):
+    from allscale_ipic3d_gb300 import abi
+    n = CELLS
+    props = abi.Props.make(size=(n, n, n), cell_width=(1.0, 1.0, 1.0), dt=DT, speed_of_light=1.0, planet_radius=2.0,
+                           object_center=(0.0, 0.0, 0.0), origin=(-n / 2,) * 3, external_b=(0.0, 0.0, 4.0))
+    rng = np.random.default_rng(seed)
+    nc = n ** 3
+    per = 2 * PPC_SPECIES
+    N = nc * per
+    cell = np.repeat(np.arange(nc), per)
+    cz, cy, cx = cell % n, (cell // n) % n, cell // (n * n)
+    parts = np.zeros(N, abi.PARTICLE_DTYPE)
+    parts["position"] = np.array(props.origin) + np.stack([cx, cy, cz], 1) + rng.random((N, 3))
+    parts["velocity"] = np.array(DRIFT) + rng.normal(0.0, VTH, (N, 3))
+    ion = (np.arange(N) % per) >= PPC_SPECIES
+    parts["q"] = np.where(ion, 1.0, -1.0) / PPC_SPECIES
+    parts["qom"] = np.where(ion, 0.01, -1.0)
+    counts = np.full(nc, per, np.uint64)
+    return props, parts, counts
+
+
+def make_config(precision, graph=True):
+    from allscale_ipic3d_gb300 import abi
+    flags = abi.F_DIPOLE_IN_GATHER | abi.F_REFRESH_NODE_B | abi.F_INJECT_LOW_X
+    if graph:
+        flags |= abi.F_USE_GRAPH
+    return abi.Config.make(precision=precision, mover=abi.MOVER_FIELD, solver=abi.SOLVER_LEAPFROG,
+                           projector=abi.PROJECT_CIC, bc_low=[abi.BC_OPEN, abi.BC_PERIODIC, abi.BC_PERIODIC],
+                           bc_high=[abi.BC_OPEN, abi.BC_PERIODIC, abi.BC_PERIODIC], flags=flags,
+                           inject_per_cell=PPC_SPECIES * DRIFT[0] * DT, inject_q=-1.0 / PPC_SPECIES,
+                           inject_qom=-1.0, inject_drift=DRIFT, inject_vth=(VTH, VTH, VTH), seed=12345)
+
+
+# ---- clocks --------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi samples while the timed region runs."""
+
+    def __init__(self, device=0, interval_ms=50):
+        self.device, self.interval, self.rows, self.proc = device, interval_ms, [], None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", str(self.interval)],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+            time.sleep(0.15)
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.1)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 4 + i and r[4 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# ---- helpers ---------------------------------------------------------------------
+def stream_events(sim):
+    import torch
+    st = torch.cuda.ExternalStream(sim.stream)
+    return st, torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    return 6800.0, "fallback 6.8 TB/s"
+
+
+def profiled_traffic(precision):
+    """DRAM bytes per push launch from the committed ncu summary, if any."""
+    name = os.path.join(ROOT, "profiles", "k_push_%s_dipole32.md" % precision)
+    if not os.path.exists(name):
+        return None
+    for line in open(name):
+        if line.strip().startswith("dram_bytes_per_launch:"):
+            try:
+                return int(float(line.split(":")[1].strip().split()[0]))
+            except ValueError:
+                return None
+    return None
+
+
+def run_timed(sim, warmup, steps, sampler=None):
+    """W untimed steps, then K steps bracketed by CUDA events on the
+    library's stream (synchronised on both sides)."""
+    import torch
+    sim.step(warmup)
+    sim.synchronize()
+    n0 = sim.particle_count()
+    l0 = sim.stats()["kernel_launches"]
+    st, e0, e1 = stream_events(sim)
+    torch.cuda.synchronize()
+    ctx = sampler if sampler is not None else _Null()
+    with ctx:
+        e0.record(st)
+        sim.step(steps)
+        e1.record(st)
+        e1.synchronize()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    n1 = sim.particle_count()
+    launches = sim.stats()["kernel_launches"] - l0
+    return ms, 0.5 * (n0 + n1) * steps, launches, n0
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        pass
+
+
+def push_roofline(sim, precision, nsteps, ncells):
+    """Live per-phase CUDA-event times of eager steps; the push kernel's
+    algorithmic bytes per launch over its duration."""
+    sim.profile(True)
+    sim.step(nsteps)
+    prof = sim.profile_read(reset=True)
+    sim.profile(False)
+    push = prof["push"]
+    ms_per = push["ms"] / max(push["launches"], 1)
+    parts = push["particles"] / max(push["launches"], 1)
+    elem = 4 if precision == "fp32" else 8
+    # read + write of the 6 state components per particle, plus per cell the
+    # node fields read (E,B: 32 B FP32 / 48 B FP64) and the 4 FP64 moments
+    # accumulated (32 B)
+    per_cell = (32 if precision == "fp32" else 48) + 32
+    bytes_per = parts * 12 * elem + ncells * per_cell
+    peak, src = measured_peak()
+    achieved = bytes_per / (ms_per * 1e-3) / 1e9
+    phases = {k: round(v["ms"] / max(v["launches"], 1), 5) for k, v in prof.items() if v["launches"]}
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": profiled_traffic(precision), "kernel": "ipg::k_push<%s>" % ("float" if elem == 4 else "double"),
+            "bytes_per_launch": bytes_per, "ms_per_launch": ms_per, "peak_source": src,
+            "phase_ms_per_step": phases}
+
+
+def cpu_port_run(props, parts, counts, warmup, steps, budget_s):
+    """The CPU oracle on the host cores: warmup steps, then up to `steps`
+    steps or until budget_s seconds."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle
+    from common import OracleSim
+    lib = oracle.load()
+    threads = os.cpu_count() or 1
+    lib.oracle_set_threads(threads)
+    sim = OracleSim(props, make_config(0, graph=False))
+    sim.upload_particles(parts, counts)
+    for _ in range(warmup):
+        sim.step(1)
+    n0 = lib.oracle_particle_count(sim.s)
+    t0 = time.perf_counter()
+    done = 0
+    while done < steps:
+        sim.step(1)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    n1 = lib.oracle_particle_count(sim.s)
+    sim.close()
+    return 0.5 * (n0 + n1) * done / dt, threads, done, dt
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        props, parts, counts = make_workload(12345)
+        value, cores, done, secs = cpu_port_run(props, parts, counts, min(args.warmup, 2), args.steps, 120.0)
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": done, "warmup": args.warmup,
+               "ms_per_step": 1e3 * secs / max(done, 1), "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+               "config": {"workload": WORKLOAD, "cells": CELLS ** 3, "particles": int(len(parts))},
+               "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": "the full workload, %d timed steps (%.1f s) after 2 warm-up steps" %
+                                          (done, secs)},
+               "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return 0
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import allscale_ipic3d_gb300 as g
+    from allscale_ipic3d_gb300 import abi
+
+    props, parts, counts = make_workload(12345 + rank)
+    ncells = props.ncells
+
+    # ---- FP32 headline ----
+    sim32 = g.Simulation(props, make_config(abi.FP32))
+    sim32.upload_particles(parts, counts)
+    if dist:
+        dist.barrier()
+    sampler = ClockSampler(local)
+    ms32, psteps32, launches32, n0 = run_timed(sim32, args.warmup, args.steps, sampler)
+    if dist:
+        dist.barrier()
+        t = torch.tensor([ms32, psteps32], device="cuda", dtype=torch.float64)
+        tmax = t.clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        ms32, psteps32 = float(tmax[0]), float(t[1])
+    value32 = psteps32 / (ms32 * 1e-3)
+    cons32 = sim32.conserved()
+
+    # ---- FP64 GPU path, same inputs and steps ----
+    sim64 = g.Simulation(props, make_config(abi.FP64))
+    sim64.upload_particles(parts, counts)
+    ms64, psteps64, _, _ = run_timed(sim64, args.warmup, args.steps)
+    value64 = psteps64 / (ms64 * 1e-3)
+    cons64 = sim64.conserved()
+    ke_err = abs(cons32["kinetic_energy"] - cons64["kinetic_energy"]) / abs(cons64["kinetic_energy"])
+
+    # ---- live roofline of the push kernel (eager steps, CUDA events) ----
+    roof = push_roofline(sim32, "fp32", 20, ncells)
+    roof64 = push_roofline(sim64, "fp64", 10, ncells)
+    sim64.close()
+
+    # ---- end to end through the public API, host buffers ----
+    host = torch.empty(parts.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(abi.PARTICLE_DTYPE)
+    host[:] = parts
+    e2e = g.Simulation(props, make_config(abi.FP32))
+    e2e.upload_particles(host, counts)
+    e2e.step(1)
+    e2e.cell_counts()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e.upload_particles(host, counts)
+        e2e.step(1)
+        res = e2e.cell_counts()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = len(parts) * args.e2e_steps / e2e_s
+    if dist:
+        t = torch.tensor([e2e_value], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        e2e_value = float(t[0])
+    e2e.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, cores, done, secs = cpu_port_run(props, parts, counts, 1, 50, args.cpu_budget)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": "the full workload (8,388,608 particles), %d timed steps (%.1f s) after 1 warm-up step, "
+                         "all host threads" % (done, secs)}
+
+    out = {
+        "metric": METRIC, "value": value32, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms32 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cells": ncells, "particles": int(n0), "precision":
+                   "fp32 push/deposit (cell-relative), fp64 node moments/fields/reductions",
+                   "l2": "inputs larger than L2: particle state %.0f MB > 129 MB" % (n0 * 24 / 1e6),
+                   "graph": True, "parallelism": "replicas" if world > 1 else "single"},
+        "roofline": roof,
+        "fp64": {"value": value64, "ms_per_step": ms64 / args.steps, "roofline": roof64},
+        "fp32_over_fp64": value32 / value64,
+        "error": {"kinetic_energy_rel_fp32_vs_fp64": ke_err, "steps": args.warmup + args.steps},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(parts.nbytes + counts.nbytes),
+                "d2h_bytes_per_step": int(res.nbytes)},
+        "clocks": sampler.summary(),
+        "gpu_launches": int(launches32),
+    }
+    if rank == 0:
+        print(json.dumps(out))
+    sim32.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

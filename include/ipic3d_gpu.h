@@ -147,7 +147,12 @@ int ipic3d_gpu_download_particles(ipic3d_ctx* ctx, ipic3d_particle* particles, u
 int ipic3d_gpu_cell_counts(ipic3d_ctx* ctx, uint64_t* cell_counts);
 
 /* Field grids in the reference layout (ipic3d_types.h); any pointer may be
- * NULL to skip that grid. rho is (size+1)^3 doubles (download only). */
+ * NULL to skip that grid. rho is (size+1)^3 doubles (download only).
+ * With the CIC projector the deposit is fused into the push, so after
+ * ipic3d_gpu_step J and rho hold the projection of the current particles --
+ * what the reference's projector computes at the start of the next step
+ * (simulator.h:189-194) -- rather than the projection made at the start of
+ * the last step. */
 int ipic3d_gpu_upload_fields(ipic3d_ctx* ctx, const double* field, const double* bcfield, const double* density);
 int ipic3d_gpu_download_fields(ipic3d_ctx* ctx, double* field, double* bcfield, double* density, double* rho);
 
@@ -189,6 +194,27 @@ typedef struct ipic3d_stats {
     uint64_t kernel_launches;   /* kernels launched by this context        */
 } ipic3d_stats;
 int ipic3d_gpu_stats(ipic3d_ctx* ctx, ipic3d_stats* out);
+
+/* ---- per-phase timing (CUDA events on the context's stream) ------------- */
+enum ipic3d_phase {
+    IPIC3D_PHASE_PUSH = 0,     /* fused mover + export + deposit kernel      */
+    IPIC3D_PHASE_PENDING = 1,  /* push of particles that waited for a slot   */
+    IPIC3D_PHASE_INJECT = 2,   /* x = 0 injection                            */
+    IPIC3D_PHASE_PLACE = 3,    /* import: holes / arrivals / compaction      */
+    IPIC3D_PHASE_FIELDS = 4,   /* ghost faces + field solver (+ FP32 copy)   */
+    IPIC3D_PHASE_MOMENTS = 5,  /* J, rho clear + periodic fold + normalise   */
+    IPIC3D_PHASE_COUNT = 8
+};
+typedef struct ipic3d_profile {
+    double ms[IPIC3D_PHASE_COUNT];         /* summed device time per phase     */
+    uint64_t launches[IPIC3D_PHASE_COUNT]; /* timed intervals per phase        */
+    uint64_t particles[IPIC3D_PHASE_COUNT];/* particles processed (push phase) */
+} ipic3d_profile;
+/* enable != 0: later steps run without a CUDA graph and every phase is
+ * bracketed by CUDA events (adds a synchronisation per step). */
+int ipic3d_gpu_profile(ipic3d_ctx* ctx, int enable);
+/* Copies the accumulated times; reset != 0 clears them afterwards. */
+int ipic3d_gpu_profile_read(ipic3d_ctx* ctx, ipic3d_profile* out, int reset);
 
 /* ---- element kernels (the reference's unit-level functions) ------------- */
 /* Particle::updateVelocity + updatePosition (particle.h:24-49) applied
