@@ -73,6 +73,7 @@ struct Pop {
     T *x, *y, *z, *u, *v, *w;
     uint32_t* id;           // nullable
     const int64_t* start;   // [ncells + 1]
+    const int2* cta_cells;  // per push CTA: first cell and number of cells it touches
     int32_t* count;         // [ncells]
     int32_t* hole_cnt;      // [ncells]
     int32_t* hole_list;     // [capacity] holes of cell c at start[c] + k

@@ -60,6 +60,7 @@ struct PopStore {
     T *x = nullptr, *y = nullptr, *z = nullptr, *u = nullptr, *v = nullptr, *w = nullptr;
     uint32_t* id = nullptr;
     int64_t* start = nullptr;
+    int2* cta_cells = nullptr;
     int32_t *count = nullptr, *hole_cnt = nullptr, *arr_cnt = nullptr;
     int32_t *hole_list = nullptr, *arr_list = nullptr, *sort_tmp = nullptr;
     Mover<T>*outbox = nullptr, *pending_in = nullptr, *pending_out = nullptr;
@@ -69,7 +70,7 @@ struct PopStore {
 
     void release() {
         dfree(x); dfree(y); dfree(z); dfree(u); dfree(v); dfree(w); dfree(id);
-        dfree(start); dfree(count); dfree(hole_cnt); dfree(arr_cnt);
+        dfree(start); dfree(cta_cells); dfree(count); dfree(hole_cnt); dfree(arr_cnt);
         dfree(hole_list); dfree(arr_list); dfree(sort_tmp);
         dfree(outbox); dfree(pending_in); dfree(pending_out);
         dfree(pending_in_count); dfree(ctr);
@@ -80,6 +81,7 @@ struct PopStore {
         P.x = x; P.y = y; P.z = z; P.u = u; P.v = v; P.w = w;
         P.id = id;
         P.start = start;
+        P.cta_cells = cta_cells;
         P.count = count;
         P.hole_cnt = hole_cnt;
         P.hole_list = hole_list;
@@ -225,6 +227,21 @@ int alloc_pop(ipic3d_ctx* ctx, PopStore<T>& P, const std::vector<uint64_t>& coun
     CU(cudaMemsetAsync(P.pending_in_count, 0, sizeof(uint32_t), ctx->stream));
     CU(cudaMemsetAsync(P.ctr, 0, sizeof(StepCounters), ctx->stream));
     CU(cudaMemcpyAsync(P.start, P.h_start.data(), (nc + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    // push CTA b covers slots [b*kSlotsPerCta, (b+1)*kSlotsPerCta): its cells
+    const int64_t nb = (P.capacity + kSlotsPerCta - 1) / kSlotsPerCta;
+    std::vector<int2> cc((size_t)std::max<int64_t>(nb, 1));
+    int64_t c = 0;
+    for (int64_t b = 0; b < nb; ++b) {
+        const int64_t first = b * kSlotsPerCta, last = std::min(first + kSlotsPerCta, P.capacity) - 1;
+        while (P.h_start[c + 1] <= first) ++c;
+        int64_t e = c;
+        while (P.h_start[e + 1] <= last) ++e;
+        cc[b] = make_int2((int)c, (int)(e - c + 1));
+        if (e - c + 1 > kMaxCellsPerCta) return fail(IPIC3D_E_INVALID, "layout: a push CTA spans too many cells");
+    }
+    CU(cudaMalloc(&P.cta_cells, cc.size() * sizeof(int2)));
+    CU(cudaMemcpyAsync(P.cta_cells, cc.data(), cc.size() * sizeof(int2), cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));  // cc and h_start copies complete
     return IPIC3D_OK;
 }
 

@@ -360,15 +360,16 @@ __device__ __forceinline__ void deposit_one(const Geom& g, int c, const PState<T
 
 // Warp transpose-reduction: every lane holds 32 values; afterwards lane l
 // holds the warp-wide sum of value l (31 exchanges in total).
-__device__ __forceinline__ double warp_transpose_sum(double (&v)[32]) {
+template <typename T>
+__device__ __forceinline__ T warp_transpose_sum(T (&v)[32]) {
     const int lane = threadIdx.x & 31;
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) {
         const bool upper = (lane & off) != 0;
 #pragma unroll
         for (int i = 0; i < off; ++i) {
-            double send = upper ? v[i] : v[i + off];
-            double keep = upper ? v[i + off] : v[i];
+            T send = upper ? v[i] : v[i + off];
+            T keep = upper ? v[i + off] : v[i];
             v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
         }
     }
@@ -414,26 +415,10 @@ template <typename T>
 __global__ void __launch_bounds__(kPushThreads) k_push(Geom g, Pop<T> P, int mode) {
     __shared__ int64_t s_start[kMaxCellsPerCta + 1];
     __shared__ int s_count[kMaxCellsPerCta];
-    __shared__ int s_c0, s_nc;
     const int64_t base = (int64_t)blockIdx.x * kSlotsPerCta;
-    if (threadIdx.x == 0) {
-        int lo = 0, hi = g.ncells - 1;  // largest c with start[c] <= base
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (P.start[mid] <= base) lo = mid; else hi = mid - 1;
-        }
-        int64_t last = base + kSlotsPerCta - 1;
-        if (last >= P.capacity) last = P.capacity - 1;
-        int lo2 = lo, hi2 = g.ncells - 1;
-        while (lo2 < hi2) {
-            int mid = (lo2 + hi2 + 1) >> 1;
-            if (P.start[mid] <= last) lo2 = mid; else hi2 = mid - 1;
-        }
-        s_c0 = lo;
-        s_nc = lo2 - lo + 1;
-    }
-    __syncthreads();
-    const int c0 = s_c0, nc = s_nc;
+    // the cells this CTA's slots belong to (fixed between re-layouts)
+    const int2 cc = __ldg(P.cta_cells + blockIdx.x);
+    const int c0 = cc.x, nc = cc.y;
     for (int i = threadIdx.x; i <= nc; i += blockDim.x) s_start[i] = P.start[c0 + i];
     for (int i = threadIdx.x; i < nc; i += blockDim.x) s_count[i] = P.count[c0 + i];
     __syncthreads();
@@ -486,9 +471,11 @@ __global__ void __launch_bounds__(kPushThreads) k_push(Geom g, Pop<T> P, int mod
     }
 
     const bool deposit = g.deposit != 0;
-    double acc[32];
+    // per-thread node sums of its (up to 4) staying particles: FP32 for the
+    // FP32 path, FP64 otherwise; the node accumulation itself is FP64
+    T acc[32];
 #pragma unroll
-    for (int l = 0; l < 32; ++l) acc[l] = 0.0;
+    for (int l = 0; l < 32; ++l) acc[l] = T(0);
     bool has_acc = false;
     int outc[kVec], dst[kVec];
 
@@ -514,10 +501,10 @@ __global__ void __launch_bounds__(kPushThreads) k_push(Geom g, Pop<T> P, int mod
                     acc[corner * 4 + 3] += q * fac;
                 } else {
                     const float qf = (float)q;
-                    acc[corner * 4 + 0] += (double)(qf * ps[j].u * fac);
-                    acc[corner * 4 + 1] += (double)(qf * ps[j].v * fac);
-                    acc[corner * 4 + 2] += (double)(qf * ps[j].w * fac);
-                    acc[corner * 4 + 3] += (double)(qf * fac);
+                    acc[corner * 4 + 0] += qf * ps[j].u * fac;
+                    acc[corner * 4 + 1] += qf * ps[j].v * fac;
+                    acc[corner * 4 + 2] += qf * ps[j].w * fac;
+                    acc[corner * 4 + 3] += qf * fac;
                 }
             }
             has_acc = true;
@@ -590,10 +577,10 @@ __global__ void __launch_bounds__(kPushThreads) k_push(Geom g, Pop<T> P, int mod
             const int gcell = __shfl_sync(0xffffffffu, cell, leader);
             const bool mine = has_acc && cell == gcell;
             const unsigned grp = __ballot_sync(0xffffffffu, mine);
-            double v[32];
+            T v[32];
 #pragma unroll
-            for (int l = 0; l < 32; ++l) v[l] = mine ? acc[l] : 0.0;
-            const double tot = warp_transpose_sum(v);
+            for (int l = 0; l < 32; ++l) v[l] = mine ? acc[l] : T(0);
+            const double tot = (double)warp_transpose_sum<T>(v);
             int gx, gy, gz;
             cell_coords(g, gcell, gx, gy, gz);
             node_atomic_add(g, gx, gy, gz, lane, tot);

@@ -3,8 +3,9 @@
 timestep (push + deposit + migrate + field update) on the dipole
 magnetosphere workload:
 
-  32^3 unit cells, 256 particles per cell (8,388,608): a neutral plasma of
-  electrons (q = -1/128, q/m = -1) and ions (q = +1/128, q/m = 0.01), 128 of
+  32^3 unit cells, 256 particles per cell (8,388,608): a neutral low-density
+  plasma (plasma frequency 0.03, Debye length 0.16 cells) of electrons
+  (q = -1e-3/128, q/m = -1) and ions (q = +1e-3/128, q/m = 0.01), 128 of
   each per cell, drifting Maxwellian v = (0.02, 0, 0) + N(0, 0.005); a static
   dipole B at the grid centre, moment set so |B| = 0.5 at 4 cells (B_z = 4,
   the 2 innermost cells masked: planetRadius = 2); electrons injected at the
@@ -41,6 +42,7 @@ PPC_SPECIES = 128
 DT = 0.05
 DRIFT = (0.02, 0.0, 0.0)
 VTH = 0.005
+CHARGE = 1e-3 / PPC_SPECIES  # macro-particle charge: plasma frequency sqrt(128 * CHARGE) = 0.03
 WORKLOAD = ("dipole magnetosphere: 32^3 cells x 256 particles/cell (8,388,608; e-/ion 128+128), dipole |B|=0.5 at "
             "r=4 cells, core r<2 masked, drift vx=0.02 sigma=0.005, inject -x / outflow +x, dt=0.05")
 
@@ -60,7 +62,7 @@ def make_workload(seed):
     parts["position"] = np.array(props.origin) + np.stack([cx, cy, cz], 1) + rng.random((N, 3))
     parts["velocity"] = np.array(DRIFT) + rng.normal(0.0, VTH, (N, 3))
     ion = (np.arange(N) % per) >= PPC_SPECIES
-    parts["q"] = np.where(ion, 1.0, -1.0) / PPC_SPECIES
+    parts["q"] = np.where(ion, 1.0, -1.0) * CHARGE
     parts["qom"] = np.where(ion, 0.01, -1.0)
     counts = np.full(nc, per, np.uint64)
     return props, parts, counts
@@ -74,7 +76,7 @@ def make_config(precision, graph=True):
     return abi.Config.make(precision=precision, mover=abi.MOVER_FIELD, solver=abi.SOLVER_LEAPFROG,
                            projector=abi.PROJECT_CIC, bc_low=[abi.BC_OPEN, abi.BC_PERIODIC, abi.BC_PERIODIC],
                            bc_high=[abi.BC_OPEN, abi.BC_PERIODIC, abi.BC_PERIODIC], flags=flags,
-                           inject_per_cell=PPC_SPECIES * DRIFT[0] * DT, inject_q=-1.0 / PPC_SPECIES,
+                           inject_per_cell=PPC_SPECIES * DRIFT[0] * DT, inject_q=-CHARGE,
                            inject_qom=-1.0, inject_drift=DRIFT, inject_vth=(VTH, VTH, VTH), seed=12345)
 
 
@@ -245,6 +247,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only", default="all", choices=["all", "fp32"],
+                    help="fp32: only the FP32 timed run and its roofline (small profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -283,6 +287,18 @@ def main():
     # ---- FP32 headline ----
     sim32 = g.Simulation(props, make_config(abi.FP32))
     sim32.upload_particles(parts, counts)
+    err = None
+    if args.only == "all":
+        # error of the FP32 path against the FP64 GPU path after 100 steps
+        sim64 = g.Simulation(props, make_config(abi.FP64))
+        sim64.upload_particles(parts, counts)
+        sim32.step(100)
+        sim64.step(100)
+        c32, c64 = sim32.conserved(), sim64.conserved()
+        tot = lambda c: c["kinetic_energy"] + c["e_energy"] + c["b_energy"]
+        err = {"steps": 100, "total_energy_rel": abs(tot(c32) - tot(c64)) / abs(tot(c64)),
+               "kinetic_energy_rel": abs(c32["kinetic_energy"] - c64["kinetic_energy"]) / abs(c64["kinetic_energy"]),
+               "particles_fp32": c32["particles"], "particles_fp64": c64["particles"]}
     if dist:
         dist.barrier()
     sampler = ClockSampler(local)
@@ -295,19 +311,22 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.SUM)
         ms32, psteps32 = float(tmax[0]), float(t[1])
     value32 = psteps32 / (ms32 * 1e-3)
-    cons32 = sim32.conserved()
-
-    # ---- FP64 GPU path, same inputs and steps ----
-    sim64 = g.Simulation(props, make_config(abi.FP64))
-    sim64.upload_particles(parts, counts)
-    ms64, psteps64, _, _ = run_timed(sim64, args.warmup, args.steps)
-    value64 = psteps64 / (ms64 * 1e-3)
-    cons64 = sim64.conserved()
-    ke_err = abs(cons32["kinetic_energy"] - cons64["kinetic_energy"]) / abs(cons64["kinetic_energy"])
+    stats32 = sim32.stats()
 
     # ---- live roofline of the push kernel (eager steps, CUDA events) ----
     roof = push_roofline(sim32, "fp32", 20, ncells)
+    if args.only == "fp32":
+        out = {"metric": METRIC, "value": value32, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "ms_per_step": ms32 / args.steps, "roofline": roof, "stats": stats32, "gpu_launches": int(launches32)}
+        if rank == 0:
+            print(json.dumps(out))
+        return 0
+
+    # ---- FP64 GPU path, same inputs and steps ----
+    ms64, psteps64, _, _ = run_timed(sim64, args.warmup, args.steps)
+    value64 = psteps64 / (ms64 * 1e-3)
     roof64 = push_roofline(sim64, "fp64", 10, ncells)
+    stats64 = sim64.stats()
     sim64.close()
 
     # ---- end to end through the public API, host buffers ----
@@ -348,9 +367,10 @@ def main():
                    "l2": "inputs larger than L2: particle state %.0f MB > 129 MB" % (n0 * 24 / 1e6),
                    "graph": True, "parallelism": "replicas" if world > 1 else "single"},
         "roofline": roof,
-        "fp64": {"value": value64, "ms_per_step": ms64 / args.steps, "roofline": roof64},
+        "fp64": {"value": value64, "ms_per_step": ms64 / args.steps, "roofline": roof64, "stats": stats64},
         "fp32_over_fp64": value32 / value64,
-        "error": {"kinetic_energy_rel_fp32_vs_fp64": ke_err, "steps": args.warmup + args.steps},
+        "error_fp32_vs_fp64": err,
+        "stats": stats32,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(parts.nbytes + counts.nbytes),
                 "d2h_bytes_per_step": int(res.nbytes)},
