@@ -121,6 +121,7 @@ struct ipic3d_ctx {
     Geom g{};
     double *field = nullptr, *bcfield = nullptr, *J = nullptr, *rho = nullptr;
     float4* node32 = nullptr;
+    float* cellcoef = nullptr;  // FP32 field-gather mover: per-cell polynomial
     uint64_t* d_step = nullptr;
     double *d_partial = nullptr, *d_result = nullptr;
     std::vector<PopStore<float>> p32;
@@ -549,7 +550,57 @@ int gather_host(ipic3d_ctx* ctx, std::vector<std::vector<ipic3d_particle>>& cell
     return IPIC3D_OK;
 }
 
-// Re-lays out all particles with fresh slack (after cells overflowed).
+// Device re-layout of one population: new per-cell capacities from the
+// stored counts plus the particles waiting for a slot, then a copy of every
+// cell and the placement of the waiting particles.
+template <typename T>
+int relayout_pop(ipic3d_ctx* ctx, PopStore<T>& P) {
+    const int64_t nc = ctx->ncells();
+    cudaStream_t st = ctx->stream;
+    int32_t* d_pend = nullptr;
+    CU(cudaMalloc(&d_pend, nc * sizeof(int32_t)));
+    CU(cudaMemsetAsync(d_pend, 0, nc * sizeof(int32_t), st));
+    int nl = launch_pending_count<T>(P.view(), d_pend, st);
+    std::vector<int32_t> hcnt(nc), hpend(nc);
+    CU(cudaMemcpyAsync(hcnt.data(), P.count, nc * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(hpend.data(), d_pend, nc * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    cudaFree(d_pend);
+    std::vector<uint64_t> counts(nc);
+    for (int64_t c = 0; c < nc; ++c) counts[c] = (uint64_t)hcnt[c] + (uint64_t)hpend[c];
+    PopStore<T> N;
+    N.q = P.q;
+    N.qom = P.qom;
+    int rc = alloc_pop(ctx, N, counts, 0);
+    if (rc) {
+        N.release();
+        return rc;
+    }
+    nl += launch_relayout<T>(P.view(), N.view(), (int)nc, nullptr, st);
+    if ((rc = check_launch(ctx, nl))) {
+        N.release();
+        return rc;
+    }
+    CU(cudaStreamSynchronize(st));
+    P.release();
+    P = std::move(N);
+    N.x = N.y = N.z = N.u = N.v = N.w = nullptr;  // moved-from: nothing to free
+    return IPIC3D_OK;
+}
+
+// Re-lays out every population on the device (cells ran out of slack).
+int relayout(ipic3d_ctx* ctx) {
+    drop_graph(ctx);
+    int rc;
+    for (auto& P : ctx->p32)
+        if ((rc = relayout_pop(ctx, P))) return rc;
+    for (auto& P : ctx->p64)
+        if ((rc = relayout_pop(ctx, P))) return rc;
+    ctx->rebuilds++;
+    return IPIC3D_OK;
+}
+
+// Re-lays out all particles with fresh slack through the host.
 int rebuild(ipic3d_ctx* ctx) {
     std::vector<std::vector<ipic3d_particle>> cells;
     std::vector<std::vector<uint32_t>> ids;
@@ -600,6 +651,7 @@ void refresh_geom(ipic3d_ctx* ctx) {
     g.J = ctx->J;
     g.rho = ctx->rho;
     g.node32 = ctx->node32;
+    g.cellcoef = ctx->cellcoef;
 }
 
 int check_launch(ipic3d_ctx* ctx, int n) {
@@ -659,7 +711,7 @@ int solve_impl(ipic3d_ctx* ctx) {
     else if (ctx->cfg.solver == IPIC3D_SOLVER_FORWARD)
         n += launch_forward(ctx->g, st);
     if (ctx->fp32 && ctx->cfg.mover == IPIC3D_MOVER_FIELD && ctx->cfg.solver != IPIC3D_SOLVER_STATIC)
-        n += launch_node32(ctx->g, ctx->node32, st);
+        n += launch_cell_coef(ctx->g, ctx->cellcoef, st);
     ph_end(ctx, IPIC3D_PHASE_FIELDS);
     return check_launch(ctx, n);
 }
@@ -732,7 +784,7 @@ int enqueue_step(ipic3d_ctx* ctx) {
 
 // Reads the step counters back; rebuilds the layout when particles wait for
 // a slot; reports lost particles.
-int after_steps(ipic3d_ctx* ctx) {
+int after_steps(ipic3d_ctx* ctx, bool force_relayout = false) {
     CU(cudaStreamSynchronize(ctx->stream));
     StepCounters total{};
     uint32_t pending = 0;
@@ -760,7 +812,10 @@ int after_steps(ipic3d_ctx* ctx) {
     }
     ctx->last = total;
     if (total.lost) return fail(IPIC3D_E_CAPACITY, "%u particles lost: pending list full", total.lost);
-    if (pending) return rebuild(ctx);
+    // waiting particles are pushed and placed again every step; re-lay out
+    // once they exceed 0.1% of the particles (or `force`)
+    if (pending > std::max<uint64_t>(64, ctx->particles_hint / 1000) || (pending && force_relayout))
+        return relayout(ctx);
     return IPIC3D_OK;
 }
 
@@ -848,6 +903,8 @@ int ipic3d_gpu_create(const ipic3d_props* props, const ipic3d_config* cfg, ipic3
     CUB(cudaMalloc(&ctx->J, ctx->nnode() * 3 * sizeof(double)));
     CUB(cudaMalloc(&ctx->rho, ctx->nnode() * sizeof(double)));
     CUB(cudaMalloc(&ctx->node32, ctx->nfield() * 2 * sizeof(float4)));
+    CUB(cudaMalloc(&ctx->cellcoef, ncells * 48 * sizeof(float)));
+    CUB(cudaMemsetAsync(ctx->cellcoef, 0, ncells * 48 * sizeof(float), ctx->stream));
     CUB(cudaMalloc(&ctx->d_step, sizeof(uint64_t)));
     CUB(cudaMalloc(&ctx->d_partial, (size_t)reduce_blocks() * 8 * sizeof(double)));
     CUB(cudaMalloc(&ctx->d_result, 8 * sizeof(double)));
@@ -881,6 +938,7 @@ int ipic3d_gpu_destroy(ipic3d_ctx* ctx) {
     dfree(ctx->J);
     dfree(ctx->rho);
     dfree(ctx->node32);
+    dfree(ctx->cellcoef);
     dfree(ctx->d_step);
     dfree(ctx->d_partial);
     dfree(ctx->d_result);
@@ -992,8 +1050,8 @@ int ipic3d_gpu_upload_fields(ipic3d_ctx* ctx, const double* field, const double*
         CU(cudaMemcpyAsync(ctx->J, density, ctx->nnode() * 3 * sizeof(double), cudaMemcpyHostToDevice, st));
         // a supplied J is used as it is while the projector is off
     }
-    if (field) {
-        int n = launch_node32(ctx->g, ctx->node32, st);
+    if (field && ctx->fp32) {
+        int n = launch_cell_coef(ctx->g, ctx->cellcoef, st);
         if ((rc = check_launch(ctx, n))) return rc;
     }
     CU(cudaStreamSynchronize(st));
@@ -1020,7 +1078,7 @@ int ipic3d_gpu_step(ipic3d_ctx* ctx, uint64_t num_steps) {
         if ((rc = project_impl(ctx))) return rc;
     const bool use_graph = (ctx->cfg.flags & IPIC3D_F_USE_GRAPH) != 0 && !ctx->profiling;
     // re-lay out when more than 0.5% of the particles wait for a slot
-    const uint64_t pend_limit = std::max<uint64_t>(1024, ctx->particles_hint / 200);
+    const uint64_t pend_limit = std::max<uint64_t>(64, ctx->particles_hint / 1000);
     uint64_t watch_from = 0;  // first step whose pending count is still meaningful
     for (uint64_t done = 0; done < num_steps;) {
         if (use_graph) {

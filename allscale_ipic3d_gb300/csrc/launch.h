@@ -20,6 +20,11 @@ template <typename T>
 int launch_place(const Geom& g, const Pop<T>& P, int32_t* sort_tmp, cudaStream_t st);
 template <typename T>
 int launch_pending_rotate(const Pop<T>& P, uint32_t* pending_in_count, cudaStream_t st);
+template <typename T>
+int launch_relayout(const Pop<T>& from, const Pop<T>& to, int ncells, int32_t* pend_per_cell_scratch,
+                    cudaStream_t st);
+template <typename T>
+int launch_pending_count(const Pop<T>& P, int32_t* per_cell, cudaStream_t st);
 
 // fields (fields.cu)
 int launch_ghost(const Geom& g, cudaStream_t st);
@@ -27,6 +32,7 @@ int launch_leapfrog(const Geom& g, bool refresh_node_b, cudaStream_t st);
 int launch_forward(const Geom& g, cudaStream_t st);
 int launch_j_finalize(const Geom& g, bool div8, cudaStream_t st);
 int launch_node32(const Geom& g, float4* node32, cudaStream_t st);
+int launch_cell_coef(const Geom& g, float* coef, cudaStream_t st);  // particles_fp32.cu
 int reduce_blocks();
 template <typename T>
 int launch_reduce_particles(const Pop<T>& P, int ncells, double* partial, cudaStream_t st);

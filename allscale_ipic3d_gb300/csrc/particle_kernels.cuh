@@ -762,4 +762,40 @@ __global__ void k_pending_rotate(Pop<T> P, uint32_t* pending_in_count) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *pending_in_count = n;
 }
 
+// ---- re-layout (cells ran out of slack) ---------------------------------------
+// Pending particles per cell.
+template <typename T>
+__global__ void k_pending_count(const Mover<T>* pend, const uint32_t* n_pend, int32_t* per_cell) {
+    const uint32_t n = *n_pend;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        atomicAdd(per_cell + pend[i].cell, 1);
+}
+
+// One warp per cell: the cell's particles move to the new slot range.
+template <typename T>
+__global__ void k_relayout_copy(Pop<T> from, Pop<T> to, int ncells) {
+    const int c = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (c >= ncells) return;
+    const int64_t a = from.start[c], b = to.start[c];
+    const int n = from.count[c];
+    for (int i = lane; i < n; i += 32) {
+        to.x[b + i] = from.x[a + i]; to.y[b + i] = from.y[a + i]; to.z[b + i] = from.z[a + i];
+        to.u[b + i] = from.u[a + i]; to.v[b + i] = from.v[a + i]; to.w[b + i] = from.w[a + i];
+        if (to.id) to.id[b + i] = from.id[a + i];
+    }
+    if (lane == 0) to.count[c] = n;
+}
+
+// Pending particles go after the copied ones (the new capacities hold them).
+template <typename T>
+__global__ void k_pending_place(const Mover<T>* pend, const uint32_t* n_pend, Pop<T> to) {
+    const uint32_t n = *n_pend;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const Mover<T> m = pend[i];
+        const int k = atomicAdd(to.count + m.cell, 1);
+        write_slot(to, to.start[m.cell] + k, m);
+    }
+}
+
 }  // namespace ipg

@@ -1,12 +1,48 @@
 // FP32 particle kernels: positions relative to the cell origin, FP32 push
 // with fused multiply-adds, FP64 node accumulation of the deposit.
 #include "particles_impl.cuh"
+#include "push32.cuh"
 
 namespace ipg {
-template int launch_push<float>(const Geom&, const Pop<float>&, int, cudaStream_t);
-template int launch_push_pending<float>(const Geom&, const Pop<float>&, cudaStream_t);
+
+namespace {
+Push32Const push32_const(const Geom& g, const Pop<float>& P) {
+    Push32Const pc;
+    pc.qom = (float)P.qom;
+    pc.k_sub = (float)(g.dt * 4.0 * fabs(P.qom) / (3.14159265358979323846 * g.c));
+    pc.q = (float)P.q;
+    return pc;
+}
+}  // namespace
+
+// the FP32 step uses the lean kernels of push32.cuh
+template <>
+int launch_push<float>(const Geom& g, const Pop<float>& P, int mode, cudaStream_t st) {
+    if (P.capacity <= 0) return 0;
+    const int64_t blocks = (P.capacity + kSlotsPerCta - 1) / kSlotsPerCta;
+    k_push32<2><<<(unsigned)blocks, kPushThreads, 0, st>>>(g, P, push32_const(g, P), mode);
+    return 1;
+}
+
+template <>
+int launch_push_pending<float>(const Geom& g, const Pop<float>& P, cudaStream_t st) {
+    k_push_pending32<<<152, 128, 0, st>>>(g, P, push32_const(g, P));
+    return 1;
+}
+
+int launch_cell_coef(const Geom& g, float* coef, cudaStream_t st) {
+    const int64_t n = (int64_t)g.sx * g.sy * g.sz;
+    int64_t blocks = (n + 127) / 128;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    const double scale = (g.flags & 2u) ? 1.0 / g.vol : 1.0;
+    k_cell_coef<<<(unsigned)blocks, 128, 0, st>>>(g.field, g.sx, g.sy, g.sz, scale, coef);
+    return 1;
+}
+
 template int launch_inject<float>(const Geom&, const Pop<float>&, double, const double*, const double*, uint64_t,
                                   const uint64_t*, cudaStream_t);
 template int launch_place<float>(const Geom&, const Pop<float>&, int32_t*, cudaStream_t);
 template int launch_pending_rotate<float>(const Pop<float>&, uint32_t*, cudaStream_t);
+template int launch_relayout<float>(const Pop<float>&, const Pop<float>&, int, int32_t*, cudaStream_t);
+template int launch_pending_count<float>(const Pop<float>&, int32_t*, cudaStream_t);
 }  // namespace ipg

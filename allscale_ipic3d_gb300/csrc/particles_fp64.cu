@@ -4,12 +4,20 @@
 #include "particles_impl.cuh"
 
 namespace ipg {
-template int launch_push<double>(const Geom&, const Pop<double>&, int, cudaStream_t);
-template int launch_push_pending<double>(const Geom&, const Pop<double>&, cudaStream_t);
+template <>
+int launch_push<double>(const Geom& g, const Pop<double>& P, int mode, cudaStream_t st) {
+    return launch_push_generic<double>(g, P, mode, st);
+}
+template <>
+int launch_push_pending<double>(const Geom& g, const Pop<double>& P, cudaStream_t st) {
+    return launch_push_pending_generic<double>(g, P, st);
+}
 template int launch_inject<double>(const Geom&, const Pop<double>&, double, const double*, const double*, uint64_t,
                                    const uint64_t*, cudaStream_t);
 template int launch_place<double>(const Geom&, const Pop<double>&, int32_t*, cudaStream_t);
 template int launch_pending_rotate<double>(const Pop<double>&, uint32_t*, cudaStream_t);
+template int launch_relayout<double>(const Pop<double>&, const Pop<double>&, int, int32_t*, cudaStream_t);
+template int launch_pending_count<double>(const Pop<double>&, int32_t*, cudaStream_t);
 }  // namespace ipg
 
 #include "../../include/ipic3d_types.h"

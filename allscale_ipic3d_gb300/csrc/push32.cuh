@@ -1,0 +1,394 @@
+// The FP32 push kernel: mover + export + deposit for particles stored as
+// FP32 positions relative to their cell origin (in cell widths).
+//
+// Same step as k_push<T> (particle_kernels.cuh), arranged for instruction
+// count:
+//   * fields: per-cell trilinear polynomial f = c0 + c1 x + c2 y + c3 z +
+//     c4 xy + c5 xz + c6 yz + c7 xyz of every E and B component (the
+//     expansion of trilinearInterpolationF2P, cell.h:867-885, with node
+//     values from the cell's 8 corners as in cell.h:905-937), precomputed by
+//     k_cell_coef after every field change: 7 FMAs per component;
+//   * dipole: |r|^-5 from one rsqrt;
+//   * sub-cycles (cell.h:947-952): dt/dt_sub = K |B|^2 with K per species;
+//   * deposit (cell.h:810-816 in scatter form): per thread the monomial
+//     moments sum_p Q m(r_p), Q in {u, v, w, 1}, m in {1, x, y, z, xy, xz,
+//     yz, xyz}; one butterfly per axis turns them into the 8 corner weights
+//     (1-t, t), then a warp transpose-reduction and one FP64 atomic per lane.
+#pragma once
+
+#include "particle_kernels.cuh"
+
+namespace ipg {
+
+struct Push32Const {
+    float qom;        // charge over mass of the species
+    float k_sub;      // dt * 4 |qom| / (pi c): dt / dt_sub = k_sub |B|^2
+    float q;          // charge (deposit)
+};
+
+// E (and B) at cell-relative r from the cell's coefficients: 12 float4 =
+// {E: c0..c7 per component interleaved as (Ex,Ey,Ez,Bx) ... } -- layout in
+// k_cell_coef: coefficient m of component q at coef[m * 6 + q].
+__device__ __forceinline__ void eval_fields(const float* __restrict__ coef, float x, float y, float z, float (&f)[6]) {
+    const float4* c4 = reinterpret_cast<const float4*>(coef);
+    float c[48];
+#pragma unroll
+    for (int i = 0; i < 12; ++i) {
+        float4 v = __ldg(c4 + i);
+        c[4 * i] = v.x; c[4 * i + 1] = v.y; c[4 * i + 2] = v.z; c[4 * i + 3] = v.w;
+    }
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        const float c0 = c[0 * 6 + q], c1 = c[1 * 6 + q], c2 = c[2 * 6 + q], c3 = c[3 * 6 + q];
+        const float c4_ = c[4 * 6 + q], c5 = c[5 * 6 + q], c6 = c[6 * 6 + q], c7 = c[7 * 6 + q];
+        const float a = fmaf(y, c7, c5);        // x z terms
+        float b = fmaf(y, c4_, c1);              // x terms
+        b = fmaf(z, a, b);
+        const float gz = fmaf(z, c6, c2);        // y terms
+        float r = fmaf(y, gz, c0);
+        r = fmaf(z, c3, r);
+        f[q] = fmaf(x, b, r);
+    }
+}
+
+// mover + export of one particle (FP32, cell-relative); same outcomes as
+// step_particle(..., PState<float>&, ...).
+__device__ __forceinline__ int step32(const Geom& g, const Push32Const& pc, const float* __restrict__ coef, int cx,
+                                      int cy, int cz, float ox, float oy, float oz, PState<float>& p, int& dest) {
+    float E[6];
+    if (g.mover == 1) {
+        eval_fields(coef, p.x, p.y, p.z, E);
+    } else {
+#pragma unroll
+        for (int q = 0; q < 6; ++q) E[q] = 0.f;
+    }
+    if (g.mover != 1 || (g.flags & 4u)) {
+        const float w0 = (float)g.w[0], w1 = (float)g.w[1], w2 = (float)g.w[2];
+        const float X = fmaf(p.x, w0, ox), Y = fmaf(p.y, w1, oy), Z = fmaf(p.z, w2, oz);
+        const float r2 = fmaf(X, X, fmaf(Y, Y, Z * Z));
+        const float ir = rsqrtf(r2), ir2 = ir * ir;
+        const float fac1 = (float)g.mft * (ir2 * ir2 * ir);
+        E[3] = fmaf(3.f * X * Z, fac1, E[3]);
+        E[4] = fmaf(3.f * Y * Z, fac1, E[4]);
+        E[5] = fmaf(fmaf(2.f * Z, Z, -fmaf(X, X, Y * Y)), fac1, E[5]);
+    }
+    const float bmag = fmaf(E[3], E[3], fmaf(E[4], E[4], E[5] * E[5]));
+    const float ratio = pc.k_sub * bmag;
+    int ns = 0;
+    if (ratio >= 0.f && ratio < 2147483647.f) {
+        ns = (int)ratio + 1;
+        ns = ns < 100 ? ns : 100;
+    }
+    if (ns > 0) {
+        const float dts = (float)g.dt / (float)ns;
+        const float k = pc.qom * 0.5f * dts;
+        const float tx = k * E[3], ty = k * E[4], tz = k * E[5];
+        const float inv = __frcp_rn(fmaf(tx, tx, fmaf(ty, ty, fmaf(tz, tz, 1.f))));
+        const float sx = 2.f * tx * inv, sy = 2.f * ty * inv, sz = 2.f * tz * inv;
+        const float kex = k * E[0], key = k * E[1], kez = k * E[2];
+        const float ax = dts * (float)g.inv_w[0], ay = dts * (float)g.inv_w[1], az = dts * (float)g.inv_w[2];
+        for (int s = 0; s < ns; ++s) {
+            const float mx = p.u + kex, my = p.v + key, mz = p.w + kez;
+            const float px = mx + (my * tz - mz * ty);
+            const float py = my + (mz * tx - mx * tz);
+            const float pz = mz + (mx * ty - my * tx);
+            p.u = mx + (py * sz - pz * sy) + kex;
+            p.v = my + (pz * sx - px * sz) + key;
+            p.w = mz + (px * sy - py * sx) + kez;
+            p.x = fmaf(p.u, ax, p.x);
+            p.y = fmaf(p.v, ay, p.y);
+            p.z = fmaf(p.w, az, p.z);
+        }
+    }
+    // export (cell.h:1093-1146) in cell-relative coordinates
+    const int pos[3] = {cx, cy, cz};
+    const int size[3] = {g.sx, g.sy, g.sz};
+    float R[3] = {p.x, p.y, p.z};
+    bool invert = false, drop = false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (pos[a] == 0 && R[a] < 0.f) {
+            if (g.bc_lo[a] == 0) { invert = true; R[a] += 0.5f; }
+            else if (g.bc_lo[a] == 2) drop = true;
+        } else if (pos[a] == size[a] - 1 && R[a] > 1.f) {
+            if (g.bc_hi[a] == 0) { invert = true; R[a] -= 0.5f; }
+            else if (g.bc_hi[a] == 2) drop = true;
+        }
+    }
+    if (invert) { p.u = -p.u; p.v = -p.v; p.w = -p.w; }
+    if (drop) return kDrop;
+    {
+        const float w0 = (float)g.w[0], w1 = (float)g.w[1], w2 = (float)g.w[2];
+        const float dx = fmaf(R[0], w0, ox - (float)g.object_center[0]);
+        const float dy = fmaf(R[1], w1, oy - (float)g.object_center[1]);
+        const float dz = fmaf(R[2], w2, oz - (float)g.object_center[2]);
+        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= (float)g.planet_r2) return kDrop;  // cell.h:1123-1128
+    }
+    int d[3];
+    bool out = false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        d[a] = R[a] < 0.f ? -1 : (R[a] > 1.f ? 1 : 0);
+        out |= d[a] != 0;
+        R[a] -= (float)d[a];
+    }
+    p.x = R[0]; p.y = R[1]; p.z = R[2];
+    if (!out) return kStay;
+    int n[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        int t = pos[a] + d[a];
+        n[a] = t < 0 ? t + size[a] : (t >= size[a] ? t - size[a] : t);
+    }
+    dest = cell_id(g, n[0], n[1], n[2]);
+    return kMove;
+}
+
+// Lane l ends with the sum over the lanes with `mine` of value l (masked
+// transpose-reduction; the first exchange applies the mask, so acc stays).
+__device__ __forceinline__ float warp_transpose_masked(const float (&acc)[32], bool mine) {
+    const int lane = threadIdx.x & 31;
+    float v[16];
+    {
+        const bool upper = (lane & 16) != 0;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const float send = mine ? (upper ? acc[i] : acc[i + 16]) : 0.f;
+            const float keep = mine ? (upper ? acc[i + 16] : acc[i]) : 0.f;
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+        }
+    }
+#pragma unroll
+    for (int off = 8; off >= 1; off >>= 1) {
+        const bool upper = (lane & off) != 0;
+#pragma unroll
+        for (int i = 0; i < off; ++i) {
+            const float send = upper ? v[i] : v[i + off];
+            const float keep = upper ? v[i + off] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+        }
+    }
+    return v[0];
+}
+
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kPushThreads, kMinBlocks)
+    k_push32(Geom g, Pop<float> P, Push32Const pc, int mode) {
+    __shared__ int64_t s_start[kMaxCellsPerCta + 1];
+    __shared__ int s_count[kMaxCellsPerCta];
+    const int64_t base = (int64_t)blockIdx.x * kSlotsPerCta;
+    const int2 cc = __ldg(P.cta_cells + blockIdx.x);
+    const int c0 = cc.x, nc = cc.y;
+    for (int i = threadIdx.x; i <= nc; i += blockDim.x) s_start[i] = P.start[c0 + i];
+    for (int i = threadIdx.x; i < nc; i += blockDim.x) s_count[i] = P.count[c0 + i];
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31;
+    const int64_t s0 = base + (int64_t)threadIdx.x * kVec;
+    int lc = 0;
+    {
+        int lo = 0, hi = nc - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_start[mid] <= s0) lo = mid; else hi = mid - 1;
+        }
+        lc = lo;
+    }
+    const int cell = c0 + lc;
+    int nv = 0;
+    if (s0 < P.capacity) {
+        const int64_t e = s_start[lc] + s_count[lc] - s0;
+        nv = e <= 0 ? 0 : (e >= kVec ? kVec : (int)e);
+    }
+    int cx, cy, cz;
+    cell_coords(g, cell, cx, cy, cz);
+    // cell origin relative to the dipole centre (the coordinate origin)
+    const float ox = (float)(g.origin[0] + (double)cx * g.w[0]);
+    const float oy = (float)(g.origin[1] + (double)cy * g.w[1]);
+    const float oz = (float)(g.origin[2] + (double)cz * g.w[2]);
+    const float* coef = g.cellcoef + (size_t)cell * 48;
+
+    PState<float> ps[kVec];
+    if (nv > 0) {
+        const float4 X = *reinterpret_cast<const float4*>(P.x + s0), Y = *reinterpret_cast<const float4*>(P.y + s0),
+                     Z = *reinterpret_cast<const float4*>(P.z + s0), U = *reinterpret_cast<const float4*>(P.u + s0),
+                     V = *reinterpret_cast<const float4*>(P.v + s0), W = *reinterpret_cast<const float4*>(P.w + s0);
+        ps[0] = {X.x, Y.x, Z.x, U.x, V.x, W.x};
+        ps[1] = {X.y, Y.y, Z.y, U.y, V.y, W.y};
+        ps[2] = {X.z, Y.z, Z.z, U.z, V.z, W.z};
+        ps[3] = {X.w, Y.w, Z.w, U.w, V.w, W.w};
+    }
+
+    const bool deposit = g.deposit != 0;
+    // monomial moments: acc[q * 8 + m], q in {u, v, w, 1}, m in {1, x, y, z, xy, xz, yz, xyz}
+    float acc[32];
+#pragma unroll
+    for (int l = 0; l < 32; ++l) acc[l] = 0.f;
+    bool has_acc = false;
+    int outc[kVec], dst[kVec];
+#pragma unroll
+    for (int j = 0; j < kVec; ++j) {
+        outc[j] = -1;
+        dst[j] = cell;
+        if (j >= nv) continue;
+        int dest = cell;
+        const int outcome = mode == 0 ? step32(g, pc, coef, cx, cy, cz, ox, oy, oz, ps[j], dest) : kStay;
+        outc[j] = outcome;
+        dst[j] = dest;
+        if (outcome == kStay && deposit) {
+            const float x = ps[j].x, y = ps[j].y, z = ps[j].z;
+            const float xy = x * y, xz = x * z, yz = y * z, xyz = xy * z;
+            const float Q[4] = {ps[j].u, ps[j].v, ps[j].w, 1.f};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                acc[q * 8 + 0] += Q[q];
+                acc[q * 8 + 1] = fmaf(Q[q], x, acc[q * 8 + 1]);
+                acc[q * 8 + 2] = fmaf(Q[q], y, acc[q * 8 + 2]);
+                acc[q * 8 + 3] = fmaf(Q[q], z, acc[q * 8 + 3]);
+                acc[q * 8 + 4] = fmaf(Q[q], xy, acc[q * 8 + 4]);
+                acc[q * 8 + 5] = fmaf(Q[q], xz, acc[q * 8 + 5]);
+                acc[q * 8 + 6] = fmaf(Q[q], yz, acc[q * 8 + 6]);
+                acc[q * 8 + 7] = fmaf(Q[q], xyz, acc[q * 8 + 7]);
+            }
+            has_acc = true;
+        }
+    }
+
+    uint32_t nmig = 0, nrem = 0;
+#pragma unroll
+    for (int j = 0; j < kVec; ++j) {
+        const bool leave = outc[j] == kMove;
+        const uint32_t o = warp_append(&P.ctr->outbox, leave);
+        if (leave) {
+            Mover<float> m;
+            m.cell = dst[j];
+            m.id = P.id ? P.id[s0 + j] : 0u;
+            m.x = ps[j].x; m.y = ps[j].y; m.z = ps[j].z;
+            m.u = ps[j].u; m.v = ps[j].v; m.w = ps[j].w;
+            if (o < P.outbox_cap) {
+                P.outbox[o] = m;
+                register_arrival(P, o, m);
+            } else {
+                atomicAdd(&P.ctr->lost, 1u);
+            }
+            if (deposit) deposit_one<float>(g, dst[j], ps[j], P.q);
+            ++nmig;
+        }
+        if (outc[j] == kMove || outc[j] == kDrop) {
+            const int k = atomicAdd(P.hole_cnt + cell, 1);
+            P.hole_list[s_start[lc] + k] = (int32_t)(s0 + j);
+            if (outc[j] == kDrop) ++nrem;
+        }
+    }
+    nmig = __reduce_add_sync(0xffffffffu, nmig);
+    nrem = __reduce_add_sync(0xffffffffu, nrem);
+    if (lane == 0) {
+        if (nmig) atomicAdd(&P.ctr->migrated, nmig);
+        if (nrem) atomicAdd(&P.ctr->removed, nrem);
+    }
+
+    if (mode == 0 && nv > 0) {
+        *reinterpret_cast<float4*>(P.x + s0) = make_float4(ps[0].x, ps[1].x, ps[2].x, ps[3].x);
+        *reinterpret_cast<float4*>(P.y + s0) = make_float4(ps[0].y, ps[1].y, ps[2].y, ps[3].y);
+        *reinterpret_cast<float4*>(P.z + s0) = make_float4(ps[0].z, ps[1].z, ps[2].z, ps[3].z);
+        *reinterpret_cast<float4*>(P.u + s0) = make_float4(ps[0].u, ps[1].u, ps[2].u, ps[3].u);
+        *reinterpret_cast<float4*>(P.v + s0) = make_float4(ps[0].v, ps[1].v, ps[2].v, ps[3].v);
+        *reinterpret_cast<float4*>(P.w + s0) = make_float4(ps[0].w, ps[1].w, ps[2].w, ps[3].w);
+    }
+
+    if (deposit) {
+        // monomials -> corner weights: along each axis (a, b) -> (a - b, b),
+        // i.e. sum Q (1 - t) and sum Q t; corner bits (i, j, k) = (x, y, z)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            float* m = acc + q * 8;
+            // m: [1, x, y, z, xy, xz, yz, xyz] -> node order c = i*4 + j*2 + k
+            const float a000 = m[0], a100 = m[1], a010 = m[2], a001 = m[3];
+            const float a110 = m[4], a101 = m[5], a011 = m[6], a111 = m[7];
+            // x axis
+            const float b000 = a000 - a100, b100 = a100, b010 = a010 - a110, b110 = a110;
+            const float b001 = a001 - a101, b101 = a101, b011 = a011 - a111, b111 = a111;
+            // y axis
+            const float c000 = b000 - b010, c010 = b010, c100 = b100 - b110, c110 = b110;
+            const float c001 = b001 - b011, c011 = b011, c101 = b101 - b111, c111 = b111;
+            // z axis
+            m[0] = c000 - c001; m[1] = c001;  // corners (0,0,0), (0,0,1)
+            m[2] = c010 - c011; m[3] = c011;  // (0,1,0), (0,1,1)
+            m[4] = c100 - c101; m[5] = c101;  // (1,0,0), (1,0,1)
+            m[6] = c110 - c111; m[7] = c111;  // (1,1,0), (1,1,1)
+        }
+        // value index of lane l in the transpose: l = q * 8 + corner; the
+        // node_atomic_add index is corner * 4 + comp with comp = q
+        unsigned todo = __ballot_sync(0xffffffffu, has_acc);
+        while (todo) {
+            const int leader = __ffs(todo) - 1;
+            const int gcell = __shfl_sync(0xffffffffu, cell, leader);
+            const bool mine = has_acc && cell == gcell;
+            const unsigned grp = __ballot_sync(0xffffffffu, mine);
+            const float tot = warp_transpose_masked(acc, mine);
+            int gx, gy, gz;
+            cell_coords(g, gcell, gx, gy, gz);
+            const int q = lane >> 3, corner = lane & 7;
+            node_atomic_add(g, gx, gy, gz, corner * 4 + q, (double)tot * P.q);
+            todo &= ~grp;
+        }
+    }
+}
+
+// Pending particles (no slot last step) with the same physics.
+__global__ void k_push_pending32(Geom g, Pop<float> P, Push32Const pc) {
+    const uint32_t n = *P.pending_in_count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        Mover<float> m = P.pending_in[i];
+        PState<float> p = {m.x, m.y, m.z, m.u, m.v, m.w};
+        int cx, cy, cz;
+        cell_coords(g, m.cell, cx, cy, cz);
+        const float ox = (float)(g.origin[0] + (double)cx * g.w[0]);
+        const float oy = (float)(g.origin[1] + (double)cy * g.w[1]);
+        const float oz = (float)(g.origin[2] + (double)cz * g.w[2]);
+        int dest = m.cell;
+        const int outcome = step32(g, pc, g.cellcoef + (size_t)m.cell * 48, cx, cy, cz, ox, oy, oz, p, dest);
+        if (outcome == kDrop) {
+            atomicAdd(&P.ctr->removed, 1u);
+            continue;
+        }
+        if (outcome == kMove) atomicAdd(&P.ctr->migrated, 1u);
+        Mover<float> o = {dest, m.id, p.x, p.y, p.z, p.u, p.v, p.w};
+        const uint32_t k = atomicAdd(&P.ctr->outbox, 1u);
+        if (k < P.outbox_cap) {
+            P.outbox[k] = o;
+            register_arrival(P, k, o);
+        } else {
+            atomicAdd(&P.ctr->lost, 1u);
+        }
+        if (g.deposit) deposit_one<float>(g, dest, p, P.q);
+    }
+}
+
+// Cell coefficients of the trilinear field polynomial (FP64 sums, stored
+// FP32): coefficient m of component q (Ex, Ey, Ez, Bx, By, Bz) of cell c at
+// coef[c * 48 + m * 6 + q]; monomials m = 1, x, y, z, xy, xz, yz, xyz.
+__global__ void k_cell_coef(const double* __restrict__ field, int sx, int sy, int sz, double scale, float* coef) {
+    const int64_t total = (int64_t)sx * sy * sz;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < total; c += (int64_t)gridDim.x * blockDim.x) {
+        const int z = (int)(c % sz), y = (int)((c / sz) % sy), x = (int)(c / ((int64_t)sy * sz));
+        for (int q = 0; q < 6; ++q) {
+            double f[2][2][2];
+            for (int i = 0; i < 2; ++i)
+                for (int j = 0; j < 2; ++j)
+                    for (int k = 0; k < 2; ++k)
+                        f[i][j][k] = field[9 * (((int64_t)(x + i + 1) * (sy + 3) + (y + j + 1)) * (sz + 3) + (z + k + 1)) + q];
+            const double m0 = f[0][0][0];
+            const double mx = f[1][0][0] - f[0][0][0], my = f[0][1][0] - f[0][0][0], mz = f[0][0][1] - f[0][0][0];
+            const double mxy = f[1][1][0] - f[1][0][0] - f[0][1][0] + f[0][0][0];
+            const double mxz = f[1][0][1] - f[1][0][0] - f[0][0][1] + f[0][0][0];
+            const double myz = f[0][1][1] - f[0][1][0] - f[0][0][1] + f[0][0][0];
+            const double mxyz = f[1][1][1] - f[1][1][0] - f[1][0][1] - f[0][1][1] + f[1][0][0] + f[0][1][0] +
+                                f[0][0][1] - f[0][0][0];
+            const double m[8] = {m0, mx, my, mz, mxy, mxz, myz, mxyz};
+            for (int k = 0; k < 8; ++k) coef[c * 48 + k * 6 + q] = (float)(m[k] * scale);
+        }
+    }
+}
+
+}  // namespace ipg
