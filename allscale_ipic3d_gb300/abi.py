@@ -136,7 +136,8 @@ class Conserved(C.Structure):
 
 class Stats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("steps", "particles", "capacity", "migrated_last", "removed_last",
-                                            "injected_last", "rebuilds", "kernel_launches")]
+                                            "injected_last", "rebuilds", "kernel_launches", "pending_last",
+                                            "relayout_steps")]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

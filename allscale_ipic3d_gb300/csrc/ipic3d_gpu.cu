@@ -128,6 +128,7 @@ struct ipic3d_ctx {
     std::vector<PopStore<double>> p64;
     bool j_valid = false;
     uint64_t steps = 0, launches = 0, rebuilds = 0;
+    uint64_t pending_last = 0, relayout_steps = 0;
     StepCounters last{};
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
@@ -600,27 +601,6 @@ int relayout(ipic3d_ctx* ctx) {
     return IPIC3D_OK;
 }
 
-// Re-lays out all particles with fresh slack through the host.
-int rebuild(ipic3d_ctx* ctx) {
-    std::vector<std::vector<ipic3d_particle>> cells;
-    std::vector<std::vector<uint32_t>> ids;
-    int rc = gather_host(ctx, cells, ids);
-    if (rc) return rc;
-    std::vector<ipic3d_particle> flat;
-    std::vector<uint32_t> fid;
-    std::vector<uint64_t> counts(ctx->ncells());
-    for (int64_t c = 0; c < ctx->ncells(); ++c) {
-        counts[c] = cells[c].size();
-        flat.insert(flat.end(), cells[c].begin(), cells[c].end());
-        fid.insert(fid.end(), ids[c].begin(), ids[c].end());
-    }
-    bool valid = ctx->j_valid;
-    rc = upload_impl(ctx, flat.data(), counts.data(), fid.data());
-    ctx->j_valid = valid;  // particles are unchanged: J still holds their deposit
-    ctx->rebuilds++;
-    return rc;
-}
-
 void refresh_geom(ipic3d_ctx* ctx) {
     Geom& g = ctx->g;
     const ipic3d_props& p = ctx->props;
@@ -811,6 +791,7 @@ int after_steps(ipic3d_ctx* ctx, bool force_relayout = false) {
         acc(c, pin);
     }
     ctx->last = total;
+    ctx->pending_last = pending;
     if (total.lost) return fail(IPIC3D_E_CAPACITY, "%u particles lost: pending list full", total.lost);
     // waiting particles are pushed and placed again every step; re-lay out
     // once they exceed 0.1% of the particles (or `force`)
@@ -1127,6 +1108,7 @@ int ipic3d_gpu_step(ipic3d_ctx* ctx, uint64_t num_steps) {
             uint64_t pend = 0;
             for (int q = 0; q < k; ++q) pend += ctx->h_pending[ps * kMaxPops + q];
             if (pend > pend_limit) {
+                ctx->relayout_steps += 1;
                 if ((rc = after_steps(ctx))) return rc;  // waits, then re-lays out
                 watch_from = done;  // counts recorded before the re-layout are stale
             }
@@ -1234,6 +1216,8 @@ int ipic3d_gpu_stats(ipic3d_ctx* ctx, ipic3d_stats* out) {
     out->injected_last = ctx->last.injected;
     out->rebuilds = ctx->rebuilds;
     out->kernel_launches = ctx->launches;
+    out->pending_last = ctx->pending_last;
+    out->relayout_steps = ctx->relayout_steps;
     return IPIC3D_OK;
 }
 

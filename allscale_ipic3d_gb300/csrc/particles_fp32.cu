@@ -10,7 +10,15 @@ Push32Const push32_const(const Geom& g, const Pop<float>& P) {
     Push32Const pc;
     pc.qom = (float)P.qom;
     pc.k_sub = (float)(g.dt * 4.0 * fabs(P.qom) / (3.14159265358979323846 * g.c));
-    pc.q = (float)P.q;
+    pc.dt = (float)g.dt;
+    pc.mft = (float)g.mft;
+    pc.planet_r2 = (float)g.planet_r2;
+    for (int a = 0; a < 3; ++a) {
+        pc.w[a] = (float)g.w[a];
+        pc.inv_w[a] = (float)g.inv_w[a];
+        pc.origin[a] = (float)g.origin[a];
+        pc.center[a] = (float)g.object_center[a];
+    }
     return pc;
 }
 }  // namespace

@@ -20,33 +20,35 @@
 
 namespace ipg {
 
+// Every constant of the step in FP32, computed on the host: the kernel runs
+// no FP64 instruction per particle (GB300's FP64 rate is a small fraction of
+// its FP32 rate).
 struct Push32Const {
     float qom;        // charge over mass of the species
     float k_sub;      // dt * 4 |qom| / (pi c): dt / dt_sub = k_sub |B|^2
-    float q;          // charge (deposit)
+    float dt;
+    float mft;        // -Bext.z R^3
+    float planet_r2;
+    float w[3], inv_w[3];
+    float origin[3];  // domain origin relative to the dipole centre (0,0,0)
+    float center[3];  // object centre (planet)
 };
 
-// E (and B) at cell-relative r from the cell's coefficients: 12 float4 =
-// {E: c0..c7 per component interleaved as (Ex,Ey,Ez,Bx) ... } -- layout in
-// k_cell_coef: coefficient m of component q at coef[m * 6 + q].
+// E (and B) at cell-relative r from the cell's coefficients: component q
+// (Ex, Ey, Ez, Bx, By, Bz) owns coef[q * 8 + m], m = 1, x, y, z, xy, xz, yz,
+// xyz: two float4 per component, evaluated one component at a time.
 __device__ __forceinline__ void eval_fields(const float* __restrict__ coef, float x, float y, float z, float (&f)[6]) {
     const float4* c4 = reinterpret_cast<const float4*>(coef);
-    float c[48];
-#pragma unroll
-    for (int i = 0; i < 12; ++i) {
-        float4 v = __ldg(c4 + i);
-        c[4 * i] = v.x; c[4 * i + 1] = v.y; c[4 * i + 2] = v.z; c[4 * i + 3] = v.w;
-    }
 #pragma unroll
     for (int q = 0; q < 6; ++q) {
-        const float c0 = c[0 * 6 + q], c1 = c[1 * 6 + q], c2 = c[2 * 6 + q], c3 = c[3 * 6 + q];
-        const float c4_ = c[4 * 6 + q], c5 = c[5 * 6 + q], c6 = c[6 * 6 + q], c7 = c[7 * 6 + q];
-        const float a = fmaf(y, c7, c5);        // x z terms
-        float b = fmaf(y, c4_, c1);              // x terms
+        const float4 lo = __ldg(c4 + 2 * q), hi = __ldg(c4 + 2 * q + 1);
+        // lo = (c0, cx, cy, cz), hi = (cxy, cxz, cyz, cxyz)
+        const float a = fmaf(y, hi.w, hi.y);     // x z terms
+        float b = fmaf(y, hi.x, lo.y);           // x terms
         b = fmaf(z, a, b);
-        const float gz = fmaf(z, c6, c2);        // y terms
-        float r = fmaf(y, gz, c0);
-        r = fmaf(z, c3, r);
+        const float gz = fmaf(z, hi.z, lo.z);    // y terms
+        float r = fmaf(y, gz, lo.x);
+        r = fmaf(z, lo.w, r);
         f[q] = fmaf(x, b, r);
     }
 }
@@ -63,11 +65,10 @@ __device__ __forceinline__ int step32(const Geom& g, const Push32Const& pc, cons
         for (int q = 0; q < 6; ++q) E[q] = 0.f;
     }
     if (g.mover != 1 || (g.flags & 4u)) {
-        const float w0 = (float)g.w[0], w1 = (float)g.w[1], w2 = (float)g.w[2];
-        const float X = fmaf(p.x, w0, ox), Y = fmaf(p.y, w1, oy), Z = fmaf(p.z, w2, oz);
+        const float X = fmaf(p.x, pc.w[0], ox), Y = fmaf(p.y, pc.w[1], oy), Z = fmaf(p.z, pc.w[2], oz);
         const float r2 = fmaf(X, X, fmaf(Y, Y, Z * Z));
         const float ir = rsqrtf(r2), ir2 = ir * ir;
-        const float fac1 = (float)g.mft * (ir2 * ir2 * ir);
+        const float fac1 = pc.mft * (ir2 * ir2 * ir);
         E[3] = fmaf(3.f * X * Z, fac1, E[3]);
         E[4] = fmaf(3.f * Y * Z, fac1, E[4]);
         E[5] = fmaf(fmaf(2.f * Z, Z, -fmaf(X, X, Y * Y)), fac1, E[5]);
@@ -80,13 +81,13 @@ __device__ __forceinline__ int step32(const Geom& g, const Push32Const& pc, cons
         ns = ns < 100 ? ns : 100;
     }
     if (ns > 0) {
-        const float dts = (float)g.dt / (float)ns;
+        const float dts = pc.dt / (float)ns;
         const float k = pc.qom * 0.5f * dts;
         const float tx = k * E[3], ty = k * E[4], tz = k * E[5];
         const float inv = __frcp_rn(fmaf(tx, tx, fmaf(ty, ty, fmaf(tz, tz, 1.f))));
         const float sx = 2.f * tx * inv, sy = 2.f * ty * inv, sz = 2.f * tz * inv;
         const float kex = k * E[0], key = k * E[1], kez = k * E[2];
-        const float ax = dts * (float)g.inv_w[0], ay = dts * (float)g.inv_w[1], az = dts * (float)g.inv_w[2];
+        const float ax = dts * pc.inv_w[0], ay = dts * pc.inv_w[1], az = dts * pc.inv_w[2];
         for (int s = 0; s < ns; ++s) {
             const float mx = p.u + kex, my = p.v + key, mz = p.w + kez;
             const float px = mx + (my * tz - mz * ty);
@@ -118,11 +119,10 @@ __device__ __forceinline__ int step32(const Geom& g, const Push32Const& pc, cons
     if (invert) { p.u = -p.u; p.v = -p.v; p.w = -p.w; }
     if (drop) return kDrop;
     {
-        const float w0 = (float)g.w[0], w1 = (float)g.w[1], w2 = (float)g.w[2];
-        const float dx = fmaf(R[0], w0, ox - (float)g.object_center[0]);
-        const float dy = fmaf(R[1], w1, oy - (float)g.object_center[1]);
-        const float dz = fmaf(R[2], w2, oz - (float)g.object_center[2]);
-        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= (float)g.planet_r2) return kDrop;  // cell.h:1123-1128
+        const float dx = fmaf(R[0], pc.w[0], ox - pc.center[0]);
+        const float dy = fmaf(R[1], pc.w[1], oy - pc.center[1]);
+        const float dz = fmaf(R[2], pc.w[2], oz - pc.center[2]);
+        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= pc.planet_r2) return kDrop;  // cell.h:1123-1128
     }
     int d[3];
     bool out = false;
@@ -203,9 +203,9 @@ __global__ void __launch_bounds__(kPushThreads, kMinBlocks)
     int cx, cy, cz;
     cell_coords(g, cell, cx, cy, cz);
     // cell origin relative to the dipole centre (the coordinate origin)
-    const float ox = (float)(g.origin[0] + (double)cx * g.w[0]);
-    const float oy = (float)(g.origin[1] + (double)cy * g.w[1]);
-    const float oz = (float)(g.origin[2] + (double)cz * g.w[2]);
+    const float ox = fmaf((float)cx, pc.w[0], pc.origin[0]);
+    const float oy = fmaf((float)cy, pc.w[1], pc.origin[1]);
+    const float oz = fmaf((float)cz, pc.w[2], pc.origin[2]);
     const float* coef = g.cellcoef + (size_t)cell * 48;
 
     PState<float> ps[kVec];
@@ -230,28 +230,36 @@ __global__ void __launch_bounds__(kPushThreads, kMinBlocks)
     for (int j = 0; j < kVec; ++j) {
         outc[j] = -1;
         dst[j] = cell;
-        if (j >= nv) continue;
-        int dest = cell;
-        const int outcome = mode == 0 ? step32(g, pc, coef, cx, cy, cz, ox, oy, oz, ps[j], dest) : kStay;
-        outc[j] = outcome;
-        dst[j] = dest;
-        if (outcome == kStay && deposit) {
-            const float x = ps[j].x, y = ps[j].y, z = ps[j].z;
-            const float xy = x * y, xz = x * z, yz = y * z, xyz = xy * z;
-            const float Q[4] = {ps[j].u, ps[j].v, ps[j].w, 1.f};
+    }
+    // one particle per iteration, not unrolled: the physics is emitted once;
+    // the four register slots rotate so every index stays static
+#pragma unroll 1
+    for (int j = 0; j < kVec; ++j) {
+        PState<float> p = ps[0];
+        int outcome = -1, dest = cell;
+        if (j < nv) {
+            outcome = mode == 0 ? step32(g, pc, coef, cx, cy, cz, ox, oy, oz, p, dest) : kStay;
+            if (outcome == kStay && deposit) {
+                const float x = p.x, y = p.y, z = p.z;
+                const float xy = x * y, xz = x * z, yz = y * z, xyz = xy * z;
+                const float Q[4] = {p.u, p.v, p.w, 1.f};
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                acc[q * 8 + 0] += Q[q];
-                acc[q * 8 + 1] = fmaf(Q[q], x, acc[q * 8 + 1]);
-                acc[q * 8 + 2] = fmaf(Q[q], y, acc[q * 8 + 2]);
-                acc[q * 8 + 3] = fmaf(Q[q], z, acc[q * 8 + 3]);
-                acc[q * 8 + 4] = fmaf(Q[q], xy, acc[q * 8 + 4]);
-                acc[q * 8 + 5] = fmaf(Q[q], xz, acc[q * 8 + 5]);
-                acc[q * 8 + 6] = fmaf(Q[q], yz, acc[q * 8 + 6]);
-                acc[q * 8 + 7] = fmaf(Q[q], xyz, acc[q * 8 + 7]);
+                for (int q = 0; q < 4; ++q) {
+                    acc[q * 8 + 0] += Q[q];
+                    acc[q * 8 + 1] = fmaf(Q[q], x, acc[q * 8 + 1]);
+                    acc[q * 8 + 2] = fmaf(Q[q], y, acc[q * 8 + 2]);
+                    acc[q * 8 + 3] = fmaf(Q[q], z, acc[q * 8 + 3]);
+                    acc[q * 8 + 4] = fmaf(Q[q], xy, acc[q * 8 + 4]);
+                    acc[q * 8 + 5] = fmaf(Q[q], xz, acc[q * 8 + 5]);
+                    acc[q * 8 + 6] = fmaf(Q[q], yz, acc[q * 8 + 6]);
+                    acc[q * 8 + 7] = fmaf(Q[q], xyz, acc[q * 8 + 7]);
+                }
+                has_acc = true;
             }
-            has_acc = true;
         }
+        ps[0] = ps[1]; ps[1] = ps[2]; ps[2] = ps[3]; ps[3] = p;
+        outc[0] = outc[1]; outc[1] = outc[2]; outc[2] = outc[3]; outc[3] = outcome;
+        dst[0] = dst[1]; dst[1] = dst[2]; dst[2] = dst[3]; dst[3] = dest;
     }
 
     uint32_t nmig = 0, nrem = 0;
@@ -343,9 +351,9 @@ __global__ void k_push_pending32(Geom g, Pop<float> P, Push32Const pc) {
         PState<float> p = {m.x, m.y, m.z, m.u, m.v, m.w};
         int cx, cy, cz;
         cell_coords(g, m.cell, cx, cy, cz);
-        const float ox = (float)(g.origin[0] + (double)cx * g.w[0]);
-        const float oy = (float)(g.origin[1] + (double)cy * g.w[1]);
-        const float oz = (float)(g.origin[2] + (double)cz * g.w[2]);
+        const float ox = fmaf((float)cx, pc.w[0], pc.origin[0]);
+        const float oy = fmaf((float)cy, pc.w[1], pc.origin[1]);
+        const float oz = fmaf((float)cz, pc.w[2], pc.origin[2]);
         int dest = m.cell;
         const int outcome = step32(g, pc, g.cellcoef + (size_t)m.cell * 48, cx, cy, cz, ox, oy, oz, p, dest);
         if (outcome == kDrop) {
@@ -367,7 +375,7 @@ __global__ void k_push_pending32(Geom g, Pop<float> P, Push32Const pc) {
 
 // Cell coefficients of the trilinear field polynomial (FP64 sums, stored
 // FP32): coefficient m of component q (Ex, Ey, Ez, Bx, By, Bz) of cell c at
-// coef[c * 48 + m * 6 + q]; monomials m = 1, x, y, z, xy, xz, yz, xyz.
+// coef[c * 48 + q * 8 + m]; monomials m = 1, x, y, z, xy, xz, yz, xyz.
 __global__ void k_cell_coef(const double* __restrict__ field, int sx, int sy, int sz, double scale, float* coef) {
     const int64_t total = (int64_t)sx * sy * sz;
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < total; c += (int64_t)gridDim.x * blockDim.x) {
@@ -386,7 +394,7 @@ __global__ void k_cell_coef(const double* __restrict__ field, int sx, int sy, in
             const double mxyz = f[1][1][1] - f[1][1][0] - f[1][0][1] - f[0][1][1] + f[1][0][0] + f[0][1][0] +
                                 f[0][0][1] - f[0][0][0];
             const double m[8] = {m0, mx, my, mz, mxy, mxz, myz, mxyz};
-            for (int k = 0; k < 8; ++k) coef[c * 48 + k * 6 + q] = (float)(m[k] * scale);
+            for (int k = 0; k < 8; ++k) coef[c * 48 + q * 8 + k] = (float)(m[k] * scale);
         }
     }
 }

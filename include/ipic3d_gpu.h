@@ -192,6 +192,8 @@ typedef struct ipic3d_stats {
     uint64_t injected_last;     /* particles injected, last step           */
     uint64_t rebuilds;          /* storage re-layouts (overflow of a cell) */
     uint64_t kernel_launches;   /* kernels launched by this context        */
+    uint64_t pending_last;      /* particles waiting for a slot, last step */
+    uint64_t relayout_steps;    /* steps after which a re-layout ran       */
 } ipic3d_stats;
 int ipic3d_gpu_stats(ipic3d_ctx* ctx, ipic3d_stats* out);
 

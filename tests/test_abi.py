@@ -37,7 +37,7 @@ def test_struct_layouts_match_header():
     assert C.sizeof(abi.Props) == 3 * 8 + 3 * 8 + 3 * 8 + 9 * 8
     assert abi.PARTICLE_DTYPE.itemsize == 64
     assert C.sizeof(abi.Conserved) == 6 * 8
-    assert C.sizeof(abi.Stats) == 8 * 8
+    assert C.sizeof(abi.Stats) == 10 * 8
 
 
 def test_config_default_matches_reference_policies():
