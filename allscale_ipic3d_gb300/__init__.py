@@ -61,6 +61,7 @@ _SIGNATURES = [
     ("ipic3d_gpu_stats", C.c_int, [_vp, _vp]),
     ("ipic3d_gpu_profile", C.c_int, [_vp, C.c_int]),
     ("ipic3d_gpu_profile_read", C.c_int, [_vp, _vp, C.c_int]),
+    ("ipic3d_gpu_project_noalloc", C.c_int, [_vp, C.c_uint32, _vp, _vp, _vp, _vp, _vp]),
     ("ipic3d_gpu_boris", C.c_int, [_vp, C.c_uint64, _vp, _vp, C.c_double, C.c_uint64, C.c_int]),
     ("ipic3d_gpu_last_error", C.c_int, [C.c_char_p, C.c_size_t]),
 ]
@@ -108,6 +109,13 @@ def boris(particles, E, B, dt, nsteps=1, push_position=True):
     if p is not particles:
         particles[...] = p
     return particles
+
+
+def project_noalloc(props, flags, d_particles, d_cell_offsets, d_J, d_rho=None, stream=None):
+    """ipic3d_gpu_project_noalloc on caller-owned device buffers (integer
+    device addresses): the current projection without any allocation."""
+    _check(library().ipic3d_gpu_project_noalloc(C.byref(props), int(flags), d_particles, d_cell_offsets, d_J,
+                                                d_rho, stream))
 
 
 class Simulation:

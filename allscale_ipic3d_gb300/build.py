@@ -25,6 +25,7 @@ SOURCES = {
     "particles_fp32.cu": [],
     "fields.cu": ["-fmad=false"],
     "upload.cu": ["-fmad=false"],
+    "noalloc.cu": ["-fmad=false"],
 }
 
 

@@ -38,6 +38,12 @@ int fail(int status, const char* fmt, ...) {
     return status;
 }
 
+}  // namespace
+
+int set_last_error(int status, const char* msg) { return fail(status, "%s", msg); }
+
+namespace {
+
 #define CU(call)                                                                                              \
     do {                                                                                                      \
         cudaError_t e_ = (call);                                                                              \

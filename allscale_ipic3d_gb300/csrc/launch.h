@@ -40,6 +40,8 @@ int launch_reduce_fields(const Geom& g, double* partial, cudaStream_t st);
 int launch_reduce_final(const double* partial, int blocks, int kq, double* out, cudaStream_t st);
 
 // misc (ipic3d_gpu.cu)
+// records a status and message for ipic3d_gpu_last_error (this thread)
+int set_last_error(int status, const char* msg);
 int launch_boris(const void* parts, uint64_t n, const double E[3], const double B[3], double dt, uint64_t nsteps,
                  int push_position, void* out, cudaStream_t st);
 

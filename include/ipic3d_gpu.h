@@ -226,6 +226,24 @@ int ipic3d_gpu_profile_read(ipic3d_ctx* ctx, ipic3d_profile* out, int reset);
 int ipic3d_gpu_boris(ipic3d_particle* particles, uint64_t n, const double E[3], const double B[3], double dt,
                      uint64_t nsteps, int push_position);
 
+/* ---- projection without allocation -------------------------------------- */
+/* No counterpart in the reference. The current projection of
+ * ipic3d_gpu_project (projectToDensityField over all nodes, cell.h:787-824)
+ * for callers that cannot allocate device memory: hosts that hand out every
+ * byte of device memory from their own pool, or loops where a cudaMalloc
+ * would synchronise the device. Nothing here allocates: the caller passes
+ * device pointers to the particles (grouped by cell, d_cell_offsets[c] ..
+ * d_cell_offsets[c+1] for cell c, ncells + 1 entries), J ((size+1)^3 x 3
+ * doubles) and rho ((size+1)^3 doubles, may be NULL); the FP64 node sums in
+ * between live in one fixed device array of the library, sized for grids of
+ * at most 32^3 cells (larger grids return IPIC3D_E_CAPACITY). The first call
+ * on a device looks up that array's device address, so make it once before
+ * any stream capture. Every call shares the array: calls that overlap on
+ * the GPU (other streams, other host threads) race. flags: IPIC3D_F_J_DIV8.
+ * Work is enqueued on `stream` (a cudaStream_t, NULL = default stream). */
+int ipic3d_gpu_project_noalloc(const ipic3d_props* props, uint32_t flags, const ipic3d_particle* d_particles,
+                               const uint64_t* d_cell_offsets, double* d_J, double* d_rho, void* stream);
+
 /* ---- errors -------------------------------------------------------------- */
 /* Copies the message of the last failure on this thread into buf. Returns
  * the last status. */
