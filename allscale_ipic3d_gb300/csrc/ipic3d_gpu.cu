@@ -799,9 +799,9 @@ int after_steps(ipic3d_ctx* ctx, bool force_relayout = false) {
     ctx->last = total;
     ctx->pending_last = pending;
     if (total.lost) return fail(IPIC3D_E_CAPACITY, "%u particles lost: pending list full", total.lost);
-    // waiting particles are pushed and placed again every step; re-lay out
-    // once they exceed 0.1% of the particles (or `force`)
-    if (pending > std::max<uint64_t>(64, ctx->particles_hint / 1000) || (pending && force_relayout))
+    // waiting particles are pushed and placed again every step (a cheap
+    // path); re-lay out once they exceed 0.5% of the particles (or `force`)
+    if (pending > std::max<uint64_t>(64, ctx->particles_hint / 200) || (pending && force_relayout))
         return relayout(ctx);
     return IPIC3D_OK;
 }
@@ -1065,7 +1065,7 @@ int ipic3d_gpu_step(ipic3d_ctx* ctx, uint64_t num_steps) {
         if ((rc = project_impl(ctx))) return rc;
     const bool use_graph = (ctx->cfg.flags & IPIC3D_F_USE_GRAPH) != 0 && !ctx->profiling;
     // re-lay out when more than 0.5% of the particles wait for a slot
-    const uint64_t pend_limit = std::max<uint64_t>(64, ctx->particles_hint / 1000);
+    const uint64_t pend_limit = std::max<uint64_t>(64, ctx->particles_hint / 200);
     uint64_t watch_from = 0;  // first step whose pending count is still meaningful
     for (uint64_t done = 0; done < num_steps;) {
         if (use_graph) {
