@@ -22,7 +22,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = {
     "ipic3d_gpu.cu": [],
     "particles_fp64.cu": ["-fmad=false"],
-    "particles_fp32.cu": [],
+    # FP32 push: flush denormals, approximate division / sqrt (the error bar
+    # of the FP32 path is stated against the FP64 path)
+    "particles_fp32.cu": ["--ftz=true", "--prec-div=false", "--prec-sqrt=false"],
     "fields.cu": ["-fmad=false"],
     "upload.cu": ["-fmad=false"],
     "noalloc.cu": ["-fmad=false"],

@@ -110,6 +110,15 @@ __device__ __forceinline__ void cell_coords(const Geom& g, int c, int& x, int& y
 }
 __device__ __forceinline__ int cell_id(const Geom& g, int x, int y, int z) { return (x * g.sy + y) * g.sz + z; }
 
+// q = a / d, r = a % d for 0 <= a < 2^24 and 0 < d < 2^12 through a float
+// reciprocal and one correction step (no integer division)
+__device__ __forceinline__ int fast_div(int a, int d, float inv_d) {
+    int q = __float2int_rz(__int2float_rn(a) * inv_d);
+    const int r = a - q * d;
+    q += (r >= d) - (r < 0);
+    return q;
+}
+
 // Warp-aggregated atomic increment: one atomic per warp for all active
 // lanes with pred set; returns this lane's slot (or undefined if !pred).
 __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {

@@ -19,6 +19,8 @@ Push32Const push32_const(const Geom& g, const Pop<float>& P) {
         pc.origin[a] = (float)g.origin[a];
         pc.center[a] = (float)g.object_center[a];
     }
+    pc.inv_sy = 1.0f / (float)g.sy;
+    pc.inv_sz = 1.0f / (float)g.sz;
     return pc;
 }
 }  // namespace
@@ -28,7 +30,7 @@ template <>
 int launch_push<float>(const Geom& g, const Pop<float>& P, int mode, cudaStream_t st) {
     if (P.capacity <= 0) return 0;
     const int64_t blocks = (P.capacity + kSlotsPerCta - 1) / kSlotsPerCta;
-    k_push32<2><<<(unsigned)blocks, kPushThreads, 0, st>>>(g, P, push32_const(g, P), mode);
+    k_push32<3><<<(unsigned)blocks, kPushThreads, 0, st>>>(g, P, push32_const(g, P), mode);
     return 1;
 }
 

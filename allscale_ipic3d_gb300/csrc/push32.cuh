@@ -32,6 +32,7 @@ struct Push32Const {
     float w[3], inv_w[3];
     float origin[3];  // domain origin relative to the dipole centre (0,0,0)
     float center[3];  // object centre (planet)
+    float inv_sy, inv_sz;  // 1 / cells along y and z (cell index -> coordinates)
 };
 
 // E (and B) at cell-relative r from the cell's coefficients: component q
@@ -81,10 +82,10 @@ __device__ __forceinline__ int step32(const Geom& g, const Push32Const& pc, cons
         ns = ns < 100 ? ns : 100;
     }
     if (ns > 0) {
-        const float dts = pc.dt / (float)ns;
+        const float dts = __fdividef(pc.dt, (float)ns);
         const float k = pc.qom * 0.5f * dts;
         const float tx = k * E[3], ty = k * E[4], tz = k * E[5];
-        const float inv = __frcp_rn(fmaf(tx, tx, fmaf(ty, ty, fmaf(tz, tz, 1.f))));
+        const float inv = __fdividef(1.f, fmaf(tx, tx, fmaf(ty, ty, fmaf(tz, tz, 1.f))));
         const float sx = 2.f * tx * inv, sy = 2.f * ty * inv, sz = 2.f * tz * inv;
         const float kex = k * E[0], key = k * E[1], kez = k * E[2];
         const float ax = dts * pc.inv_w[0], ay = dts * pc.inv_w[1], az = dts * pc.inv_w[2];
@@ -201,7 +202,14 @@ __global__ void __launch_bounds__(kPushThreads, kMinBlocks)
         nv = e <= 0 ? 0 : (e >= kVec ? kVec : (int)e);
     }
     int cx, cy, cz;
-    cell_coords(g, cell, cx, cy, cz);
+    if (g.ncells < (1 << 24) && g.sy < 4096 && g.sz < 4096) {
+        const int t = fast_div(cell, g.sz, pc.inv_sz);
+        cz = cell - t * g.sz;
+        cx = fast_div(t, g.sy, pc.inv_sy);
+        cy = t - cx * g.sy;
+    } else {
+        cell_coords(g, cell, cx, cy, cz);
+    }
     // cell origin relative to the dipole centre (the coordinate origin)
     const float ox = fmaf((float)cx, pc.w[0], pc.origin[0]);
     const float oy = fmaf((float)cy, pc.w[1], pc.origin[1]);
