@@ -85,7 +85,9 @@ __device__ __forceinline__ int step32(const Geom& g, const Push32Const& pc, cons
         const float dts = __fdividef(pc.dt, (float)ns);
         const float k = pc.qom * 0.5f * dts;
         const float tx = k * E[3], ty = k * E[4], tz = k * E[5];
-        const float inv = __fdividef(1.f, fmaf(tx, tx, fmaf(ty, ty, fmaf(tz, tz, 1.f))));
+        // the rotation factor 2 / (1 + |t|^2) keeps |v| through the rotation:
+        // correctly rounded reciprocal here
+        const float inv = __frcp_rn(fmaf(tx, tx, fmaf(ty, ty, fmaf(tz, tz, 1.f))));
         const float sx = 2.f * tx * inv, sy = 2.f * ty * inv, sz = 2.f * tz * inv;
         const float kex = k * E[0], key = k * E[1], kez = k * E[2];
         const float ax = dts * pc.inv_w[0], ay = dts * pc.inv_w[1], az = dts * pc.inv_w[2];
