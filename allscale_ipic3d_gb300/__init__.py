@@ -19,8 +19,8 @@ from .abi import (BC_OPEN, BC_PERIODIC, BC_REFLECT, FP32, FP64, MOVER_DIPOLE, MO
                   PROJECT_CIC, PROJECT_NONE, SOLVER_FORWARD, SOLVER_LEAPFROG, SOLVER_STATIC, Config, Conserved,
                   Props, Stats)
 
-__all__ = ["Simulation", "Props", "Config", "Conserved", "Stats", "PARTICLE_DTYPE", "GpuPathError", "library",
-           "library_path", "boris", "EXPORTED_SYMBOLS"]
+__all__ = ["Simulation", "Batch", "Props", "Config", "Conserved", "Stats", "PARTICLE_DTYPE", "GpuPathError",
+           "library", "library_path", "boris", "EXPORTED_SYMBOLS"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -63,6 +63,14 @@ _SIGNATURES = [
     ("ipic3d_gpu_profile_read", C.c_int, [_vp, _vp, C.c_int]),
     ("ipic3d_gpu_project_noalloc", C.c_int, [_vp, C.c_uint32, _vp, _vp, _vp, _vp, _vp]),
     ("ipic3d_gpu_boris", C.c_int, [_vp, C.c_uint64, _vp, _vp, C.c_double, C.c_uint64, C.c_int]),
+    ("ipic3d_gpu_batch_create", C.c_int, [C.c_uint32, _vp, _vp, C.POINTER(_vp)]),
+    ("ipic3d_gpu_batch_destroy", C.c_int, [_vp]),
+    ("ipic3d_gpu_batch_size", C.c_int, [_vp, C.POINTER(C.c_uint32)]),
+    ("ipic3d_gpu_batch_universe", C.c_int, [_vp, C.c_uint32, C.POINTER(_vp)]),
+    ("ipic3d_gpu_batch_step", C.c_int, [_vp, C.c_uint64]),
+    ("ipic3d_gpu_batch_synchronize", C.c_int, [_vp]),
+    ("ipic3d_gpu_batch_stream", _vp, [_vp]),
+    ("ipic3d_gpu_batch_stats", C.c_int, [_vp, _vp]),
     ("ipic3d_gpu_last_error", C.c_int, [C.c_char_p, C.c_size_t]),
 ]
 EXPORTED_SYMBOLS = [s[0] for s in _SIGNATURES]
@@ -125,19 +133,25 @@ class Simulation:
     ``config`` the simulateSteps policies (simulator.h:42-47,244-276).
     """
 
-    def __init__(self, props, config=None):
+    def __init__(self, props, config=None, _lent=None):
         self.props = props
         self.config = config if config is not None else Config.make()
+        self.ncells = props.ncells
+        if _lent is not None:  # a universe of a Batch (freed with the batch)
+            self._ctx = _lent
+            self._owner = False
+            return
         lib = library()
         ctx = C.c_void_p()
         _check(lib.ipic3d_gpu_create(C.byref(self.props), C.byref(self.config), C.byref(ctx)))
         self._ctx = ctx
-        self.ncells = props.ncells
+        self._owner = True
 
     # -- lifetime --
     def close(self):
         if getattr(self, "_ctx", None):
-            library().ipic3d_gpu_destroy(self._ctx)
+            if getattr(self, "_owner", False):
+                library().ipic3d_gpu_destroy(self._ctx)
             self._ctx = None
 
     def __enter__(self):
@@ -248,3 +262,65 @@ class Simulation:
     @property
     def stream(self):
         return library().ipic3d_gpu_stream(self._ctx)
+
+
+class Batch:
+    """Independent universes advanced together, one launch per kernel of the
+    timestep (ipic3d_gpu_batch_*). ``props`` is a sequence of Props (one per
+    universe, sizes may differ); ``config`` is shared. ``universe(i)`` is a
+    Simulation view of universe i for uploads, downloads and diagnostics; it
+    stays valid until the batch is closed."""
+
+    def __init__(self, props, config=None):
+        self.props = list(props)
+        self.config = config if config is not None else Config.make()
+        arr = (Props * len(self.props))(*self.props)
+        b = C.c_void_p()
+        _check(library().ipic3d_gpu_batch_create(len(self.props), arr, C.byref(self.config), C.byref(b)))
+        self._b = b
+        self._views = {}
+
+    def __len__(self):
+        return len(self.props)
+
+    def close(self):
+        if getattr(self, "_b", None):
+            for v in self._views.values():
+                v._ctx = None
+            self._views = {}
+            library().ipic3d_gpu_batch_destroy(self._b)
+            self._b = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def universe(self, i):
+        if i not in self._views:
+            ctx = C.c_void_p()
+            _check(library().ipic3d_gpu_batch_universe(self._b, int(i), C.byref(ctx)))
+            self._views[i] = Simulation(self.props[i], self.config, _lent=ctx)
+        return self._views[i]
+
+    def step(self, n=1):
+        _check(library().ipic3d_gpu_batch_step(self._b, int(n)))
+
+    def synchronize(self):
+        _check(library().ipic3d_gpu_batch_synchronize(self._b))
+
+    def stats(self):
+        out = Stats()
+        _check(library().ipic3d_gpu_batch_stats(self._b, C.byref(out)))
+        return out.as_dict()
+
+    @property
+    def stream(self):
+        return library().ipic3d_gpu_batch_stream(self._b)

@@ -91,6 +91,52 @@ struct Pop {
     double q, qom;
 };
 
+// Every constant of the step in FP32, computed on the host: the kernel runs
+// no FP64 instruction per particle (GB300's FP64 rate is a small fraction of
+// its FP32 rate).
+struct Push32Const {
+    float qom;        // charge over mass of the species
+    float k_sub;      // dt * 4 |qom| / (pi c): dt / dt_sub = k_sub |B|^2
+    float dt;
+    float mft;        // -Bext.z R^3
+    float planet_r2;
+    float w[3], inv_w[3];
+    float origin[3];  // domain origin relative to the dipole centre (0,0,0)
+    float center[3];  // object centre (planet)
+    float inv_sy, inv_sz;  // 1 / cells along y and z (cell index -> coordinates)
+};
+
+// ---- batched ensemble ------------------------------------------------------
+// One population of one universe of a batch: everything a batched particle
+// kernel needs, read from a device table indexed by job.
+template <typename T>
+struct PopJob {
+    Geom g;
+    Pop<T> P;
+    Push32Const pc;         // FP32 populations: the push constants
+    int32_t* sort_tmp;      // placement scratch [capacity]
+    uint32_t* pend_count;   // P.pending_in_count (written by the rotation)
+};
+
+// One universe of a batch (field-level kernels, counters).
+struct InstJob {
+    Geom g;
+    uint64_t* step;         // device step counter
+    int job0, njobs;        // its populations: PopJob entries [job0, job0 + njobs)
+    uint32_t pend_limit;    // waiting particles above which it is re-laid out
+    int div8;               // J = Js / vol / 8
+    int refresh_b;          // leapfrog refreshes node B from Bc
+    float* cellcoef;        // FP32 field-gather coefficients (writable view)
+    double coef_scale;      // 1 / vol with the gather normalisation, else 1
+};
+
+// Per-job counters as read back after a batched step.
+struct JobStatus {
+    StepCounters c;
+    uint32_t pending_in;
+    uint32_t pad;
+};
+
 // ---- small helpers --------------------------------------------------------
 
 __device__ __forceinline__ int64_t field_index(const Geom& g, int x, int y, int z) {

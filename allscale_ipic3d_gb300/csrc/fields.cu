@@ -25,10 +25,10 @@ __device__ __forceinline__ int64_t fidx(int n, int x, int y, int z) { return ((i
 
 // Copies the six ghost faces of a cubic grid of n^3 records of `per` doubles:
 // index (a, b) in [1, n-1)^2 of each face (edges and corners stay).
-__global__ void k_ghost(double* g, int n, int per) {
+__device__ __forceinline__ void ghost_body(double* g, int n, int per, int64_t t0, int64_t stride) {
     const int end = n - 1;
     const int64_t m = (int64_t)(end - 1) * (end - 1);
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m * per; t += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t t = t0; t < m * per; t += stride) {
         const int comp = (int)(t % per);
         const int64_t ab = t / per;
         const int a = 1 + (int)(ab / (end - 1)), b = 1 + (int)(ab % (end - 1));
@@ -51,11 +51,11 @@ struct SolverArgs {
 };
 
 // E at pos in [1, s+2)^3 from Bc(pos), Bc(pos - e_i) and J(pos - 1).
-__global__ void k_leapfrog_e(SolverArgs A) {
+__device__ __forceinline__ void leapfrog_e_body(SolverArgs A, int64_t t0, int64_t stride) {
     const int n = A.s + 1;  // nodes per axis in the updated box
     const int64_t total = (int64_t)n * n * n;
     const double c2 = A.c * A.c;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t t = t0; t < total; t += stride) {
         const int x = 1 + (int)(t / ((int64_t)n * n)), y = 1 + (int)((t / n) % n), z = 1 + (int)(t % n);
         const int nb = A.s + 2, nf = A.s + 3, nd = A.s + 1;
         const double* B0 = A.bc + 3 * fidx(nb, x, y, z);
@@ -71,10 +71,10 @@ __global__ void k_leapfrog_e(SolverArgs A) {
 }
 
 // Bc at pos in [1, s+1)^3 from the new E at pos and pos + e_i.
-__global__ void k_leapfrog_b(SolverArgs A) {
+__device__ __forceinline__ void leapfrog_b_body(SolverArgs A, int64_t t0, int64_t stride) {
     const int n = A.s;
     const int64_t total = (int64_t)n * n * n;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t t = t0; t < total; t += stride) {
         const int x = 1 + (int)(t / ((int64_t)n * n)), y = 1 + (int)((t / n) % n), z = 1 + (int)(t % n);
         const int nb = A.s + 2, nf = A.s + 3;
         const double* E0 = A.field + 9 * fidx(nf, x, y, z);
@@ -137,10 +137,10 @@ __device__ __forceinline__ void curl_e(const SolverArgs& A, int x, int y, int z,
     cz = ydx - xdy;
 }
 
-__global__ void k_forward_e(SolverArgs A) {
+__device__ __forceinline__ void forward_e_body(SolverArgs A, int64_t t0, int64_t stride) {
     const int n = A.s + 1;
     const int64_t total = (int64_t)n * n * n;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t t = t0; t < total; t += stride) {
         const int x = 1 + (int)(t / ((int64_t)n * n)), y = 1 + (int)((t / n) % n), z = 1 + (int)(t % n);
         double cx, cy, cz;
         curl_b(A, x, y, z, cx, cy, cz);
@@ -152,10 +152,10 @@ __global__ void k_forward_e(SolverArgs A) {
     }
 }
 
-__global__ void k_forward_b(SolverArgs A) {
+__device__ __forceinline__ void forward_b_body(SolverArgs A, int64_t t0, int64_t stride) {
     const int n = A.s;
     const int64_t total = (int64_t)n * n * n;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t t = t0; t < total; t += stride) {
         const int x = 1 + (int)(t / ((int64_t)n * n)), y = 1 + (int)((t / n) % n), z = 1 + (int)(t % n);
         double cx, cy, cz;
         curl_e(A, x, y, z, cx, cy, cz);
@@ -167,10 +167,10 @@ __global__ void k_forward_b(SolverArgs A) {
 }
 
 // node B at pos in [1, s+2)^3 = 1/8 sum of Bc at pos - (i,j,k)
-__global__ void k_interp_c2n(SolverArgs A) {
+__device__ __forceinline__ void interp_c2n_body(SolverArgs A, int64_t t0, int64_t stride) {
     const int n = A.s + 1;
     const int64_t total = (int64_t)n * n * n;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t t = t0; t < total; t += stride) {
         const int x = 1 + (int)(t / ((int64_t)n * n)), y = 1 + (int)((t / n) % n), z = 1 + (int)(t % n);
         double a0 = 0.0, a1 = 0.0, a2 = 0.0;
         for (int i = 0; i < 2; i++)
@@ -188,10 +188,11 @@ __global__ void k_interp_c2n(SolverArgs A) {
 // axis, the same two cells (periodic wrap of the cell index): the final value
 // of a node is the sum of the raw deposits over its image set {0, s} on every
 // axis where it lies on the boundary. Then J = (Js / vol) [/ 8].
-__global__ void k_j_finalize(int sx, int sy, int sz, double* J, double* rho, double vol, int div8) {
+__device__ __forceinline__ void j_finalize_body(int sx, int sy, int sz, double* J, double* rho, double vol, int div8,
+                                                int64_t t0, int64_t stride) {
     const int64_t total = (int64_t)sx * sy * sz;
     const int ny = sy + 1, nz = sz + 1;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t t = t0; t < total; t += stride) {
         const int x = (int)(t / ((int64_t)sy * sz)), y = (int)((t / sz) % sy), z = (int)(t % sz);
         const int nxs = x == 0 ? 2 : 1, nys = y == 0 ? 2 : 1, nzs = z == 0 ? 2 : 1;
         double a[4] = {0.0, 0.0, 0.0, 0.0};
@@ -220,6 +221,61 @@ __global__ void k_node32(const double* field, float4* node32, int64_t nodes) {
         node32[2 * t] = make_float4((float)f[0], (float)f[1], (float)f[2], 0.f);
         node32[2 * t + 1] = make_float4((float)f[3], (float)f[4], (float)f[5], 0.f);
     }
+}
+
+__device__ __forceinline__ int64_t grid_t0() { return blockIdx.x * (int64_t)blockDim.x + threadIdx.x; }
+__device__ __forceinline__ int64_t grid_stride() { return (int64_t)gridDim.x * blockDim.x; }
+
+__host__ __device__ inline SolverArgs solver_args(const Geom& g) {
+    SolverArgs A;
+    A.s = g.sx;
+    A.dt = g.dt;
+    A.c = g.c;
+    A.wx = g.w[0];
+    A.wy = g.w[1];
+    A.wz = g.w[2];
+    A.field = g.field;
+    A.bc = g.bcfield;
+    A.J = g.J;
+    return A;
+}
+
+// single-universe kernels
+__global__ void k_ghost(double* g, int n, int per) { ghost_body(g, n, per, grid_t0(), grid_stride()); }
+__global__ void k_leapfrog_e(SolverArgs A) { leapfrog_e_body(A, grid_t0(), grid_stride()); }
+__global__ void k_leapfrog_b(SolverArgs A) { leapfrog_b_body(A, grid_t0(), grid_stride()); }
+__global__ void k_forward_e(SolverArgs A) { forward_e_body(A, grid_t0(), grid_stride()); }
+__global__ void k_forward_b(SolverArgs A) { forward_b_body(A, grid_t0(), grid_stride()); }
+__global__ void k_interp_c2n(SolverArgs A) { interp_c2n_body(A, grid_t0(), grid_stride()); }
+__global__ void k_j_finalize(int sx, int sy, int sz, double* J, double* rho, double vol, int div8) {
+    j_finalize_body(sx, sy, sz, J, rho, vol, div8, grid_t0(), grid_stride());
+}
+
+// batched kernels: blockIdx.y is the universe, blockIdx.x strides over its
+// items (the grid is sized for the largest universe of the batch)
+__global__ void k_ghost_batch(const InstJob* jobs) {
+    const Geom& g = jobs[blockIdx.y].g;
+    ghost_body(g.field, g.sx + 3, 9, grid_t0(), grid_stride());
+    ghost_body(g.bcfield, g.sx + 2, 3, grid_t0(), grid_stride());
+}
+__global__ void k_leapfrog_e_batch(const InstJob* jobs) {
+    leapfrog_e_body(solver_args(jobs[blockIdx.y].g), grid_t0(), grid_stride());
+}
+__global__ void k_leapfrog_b_batch(const InstJob* jobs) {
+    leapfrog_b_body(solver_args(jobs[blockIdx.y].g), grid_t0(), grid_stride());
+}
+__global__ void k_forward_e_batch(const InstJob* jobs) {
+    forward_e_body(solver_args(jobs[blockIdx.y].g), grid_t0(), grid_stride());
+}
+__global__ void k_forward_b_batch(const InstJob* jobs) {
+    forward_b_body(solver_args(jobs[blockIdx.y].g), grid_t0(), grid_stride());
+}
+__global__ void k_interp_c2n_batch(const InstJob* jobs) {
+    interp_c2n_body(solver_args(jobs[blockIdx.y].g), grid_t0(), grid_stride());
+}
+__global__ void k_j_finalize_batch(const InstJob* jobs) {
+    const InstJob& b = jobs[blockIdx.y];
+    j_finalize_body(b.g.sx, b.g.sy, b.g.sz, b.g.J, b.g.rho, b.g.vol, b.div8, grid_t0(), grid_stride());
 }
 
 // ---- compensated reductions ----------------------------------------------------
@@ -325,26 +381,13 @@ __global__ void k_reduce_final(const double* partial, int blocks, int kq, double
     }
 }
 
-inline int grid_for(int64_t n, int threads) {
+inline int grid_for(int64_t n, int threads, int64_t max_blocks = 152 * 32) {
     int64_t b = (n + threads - 1) / threads;
     if (b < 1) b = 1;
-    if (b > 152 * 32) b = 152 * 32;
+    if (b > max_blocks) b = max_blocks;
     return (int)b;
 }
 
-SolverArgs solver_args(const Geom& g) {
-    SolverArgs A;
-    A.s = g.sx;
-    A.dt = g.dt;
-    A.c = g.c;
-    A.wx = g.w[0];
-    A.wy = g.w[1];
-    A.wz = g.w[2];
-    A.field = g.field;
-    A.bc = g.bcfield;
-    A.J = g.J;
-    return A;
-}
 
 }  // namespace
 
@@ -387,6 +430,37 @@ int launch_j_finalize(const Geom& g, bool div8, cudaStream_t st) {
 int launch_node32(const Geom& g, float4* node32, cudaStream_t st) {
     const int64_t nodes = (int64_t)(g.sx + 3) * (g.sy + 3) * (g.sz + 3);
     k_node32<<<grid_for(nodes, 256), 256, 0, st>>>(g.field, node32, nodes);
+    return 1;
+}
+
+// batched launchers: `ninst` universes, `max_s` the largest cells per axis
+int launch_ghost_batch(const InstJob* jobs, int ninst, int max_s, cudaStream_t st) {
+    const int64_t m = (int64_t)(max_s + 1) * (max_s + 1) * 9;
+    k_ghost_batch<<<dim3(grid_for(m, 256, 64), ninst), 256, 0, st>>>(jobs);
+    return 1;
+}
+
+int launch_leapfrog_batch(const InstJob* jobs, int ninst, int max_s, bool refresh_node_b, cudaStream_t st) {
+    const int64_t ne = (int64_t)(max_s + 1) * (max_s + 1) * (max_s + 1);
+    const unsigned gx = grid_for(ne, 256, 64);
+    k_leapfrog_e_batch<<<dim3(gx, ninst), 256, 0, st>>>(jobs);
+    k_leapfrog_b_batch<<<dim3(gx, ninst), 256, 0, st>>>(jobs);
+    if (!refresh_node_b) return 2;
+    k_interp_c2n_batch<<<dim3(gx, ninst), 256, 0, st>>>(jobs);
+    return 3;
+}
+
+int launch_forward_batch(const InstJob* jobs, int ninst, int max_s, cudaStream_t st) {
+    const int64_t ne = (int64_t)(max_s + 1) * (max_s + 1) * (max_s + 1);
+    const unsigned gx = grid_for(ne, 256, 64);
+    k_forward_e_batch<<<dim3(gx, ninst), 256, 0, st>>>(jobs);
+    k_forward_b_batch<<<dim3(gx, ninst), 256, 0, st>>>(jobs);
+    k_interp_c2n_batch<<<dim3(gx, ninst), 256, 0, st>>>(jobs);
+    return 3;
+}
+
+int launch_j_finalize_batch(const InstJob* jobs, int ninst, int64_t max_cells, cudaStream_t st) {
+    k_j_finalize_batch<<<dim3(grid_for(max_cells, 256, 64), ninst), 256, 0, st>>>(jobs);
     return 1;
 }
 

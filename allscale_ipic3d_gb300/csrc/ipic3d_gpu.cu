@@ -123,6 +123,8 @@ struct ipic3d_ctx {
     ipic3d_config cfg;
     int device = 0;
     cudaStream_t stream = nullptr;
+    bool own_stream = true;  // false: the stream of the batch that owns this context
+    bool lent = false;       // a universe of a batch (destroyed with the batch)
     bool fp32 = false;
     Geom g{};
     double *field = nullptr, *bcfield = nullptr, *J = nullptr, *rho = nullptr;
@@ -813,31 +815,41 @@ int check_ctx(ipic3d_ctx* ctx) {
     return IPIC3D_OK;
 }
 
-}  // namespace
-
-// ============================================================================
-extern "C" {
-
-void ipic3d_gpu_config_default(ipic3d_config* cfg) {
-    if (!cfg) return;
-    std::memset(cfg, 0, sizeof(*cfg));
-    cfg->precision = IPIC3D_FP64;
-    cfg->mover = IPIC3D_MOVER_DIPOLE;
-    cfg->solver = IPIC3D_SOLVER_STATIC;
-    cfg->projector = IPIC3D_PROJECT_NONE;
-    for (int a = 0; a < 3; ++a) cfg->bc_low[a] = cfg->bc_high[a] = IPIC3D_BC_REFLECT;
-    cfg->seed = 12345;
+int destroy_impl(ipic3d_ctx* ctx) {
+    if (!ctx) return IPIC3D_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    drop_graph(ctx);
+    release_pops(ctx);
+    dfree(ctx->field);
+    dfree(ctx->bcfield);
+    dfree(ctx->J);
+    dfree(ctx->rho);
+    dfree(ctx->node32);
+    dfree(ctx->cellcoef);
+    dfree(ctx->d_step);
+    dfree(ctx->d_partial);
+    dfree(ctx->d_result);
+    if (ctx->h_pending) cudaFreeHost(ctx->h_pending);
+    dfree(ctx->st_parts);
+    dfree(ctx->st_ids);
+    dfree(ctx->st_sid);
+    dfree(ctx->st_off);
+    dfree(ctx->st_cnt);
+    dfree(ctx->st_unknown);
+    for (auto& e : ctx->pend_ev)
+        if (e) cudaEventDestroy(e);
+    for (auto& pair : ctx->ph_ev)
+        for (auto& e : pair)
+            if (e) cudaEventDestroy(e);
+    if (ctx->stream && ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return IPIC3D_OK;
 }
 
-int ipic3d_gpu_last_error(char* buf, size_t len) {
-    if (buf && len) {
-        std::strncpy(buf, g_last_msg, len - 1);
-        buf[len - 1] = 0;
-    }
-    return g_last_status;
-}
-
-int ipic3d_gpu_create(const ipic3d_props* props, const ipic3d_config* cfg, ipic3d_ctx** out) {
+// Creates a context; `shared` != NULL puts it on that stream (a universe of
+// a batch), else it owns a new stream.
+int create_impl(const ipic3d_props* props, const ipic3d_config* cfg, cudaStream_t shared, ipic3d_ctx** out) {
     if (!props || !cfg || !out) return fail(IPIC3D_E_INVALID, "NULL argument");
     *out = nullptr;
     for (int a = 0; a < 3; ++a) {
@@ -874,7 +886,7 @@ int ipic3d_gpu_create(const ipic3d_props* props, const ipic3d_config* cfg, ipic3
     ctx->device = dev;
     ctx->fp32 = cfg->precision == IPIC3D_FP32;
     auto bail = [&](int rc) {
-        ipic3d_gpu_destroy(ctx);
+        destroy_impl(ctx);
         return rc;
     };
 #define CUB(call)                                                                                         \
@@ -884,7 +896,12 @@ int ipic3d_gpu_create(const ipic3d_props* props, const ipic3d_config* cfg, ipic3
             return bail(fail(e_ == cudaErrorMemoryAllocation ? IPIC3D_E_NOMEM : IPIC3D_E_CUDA, "%s: %s", #call, \
                              cudaGetErrorString(e_)));                                                    \
     } while (0)
-    CUB(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    if (shared) {
+        ctx->stream = shared;
+        ctx->own_stream = false;
+    } else {
+        CUB(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    }
     CUB(cudaMalloc(&ctx->field, ctx->nfield() * 9 * sizeof(double)));
     CUB(cudaMalloc(&ctx->bcfield, ctx->nbc() * 3 * sizeof(double)));
     CUB(cudaMalloc(&ctx->J, ctx->nnode() * 3 * sizeof(double)));
@@ -914,36 +931,38 @@ int ipic3d_gpu_create(const ipic3d_props* props, const ipic3d_config* cfg, ipic3
     return IPIC3D_OK;
 }
 
+}  // namespace
+
+// ============================================================================
+extern "C" {
+
+void ipic3d_gpu_config_default(ipic3d_config* cfg) {
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->precision = IPIC3D_FP64;
+    cfg->mover = IPIC3D_MOVER_DIPOLE;
+    cfg->solver = IPIC3D_SOLVER_STATIC;
+    cfg->projector = IPIC3D_PROJECT_NONE;
+    for (int a = 0; a < 3; ++a) cfg->bc_low[a] = cfg->bc_high[a] = IPIC3D_BC_REFLECT;
+    cfg->seed = 12345;
+}
+
+int ipic3d_gpu_last_error(char* buf, size_t len) {
+    if (buf && len) {
+        std::strncpy(buf, g_last_msg, len - 1);
+        buf[len - 1] = 0;
+    }
+    return g_last_status;
+}
+
+int ipic3d_gpu_create(const ipic3d_props* props, const ipic3d_config* cfg, ipic3d_ctx** out) {
+    return create_impl(props, cfg, nullptr, out);
+}
+
 int ipic3d_gpu_destroy(ipic3d_ctx* ctx) {
-    if (!ctx) return IPIC3D_OK;
-    cudaSetDevice(ctx->device);
-    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    drop_graph(ctx);
-    release_pops(ctx);
-    dfree(ctx->field);
-    dfree(ctx->bcfield);
-    dfree(ctx->J);
-    dfree(ctx->rho);
-    dfree(ctx->node32);
-    dfree(ctx->cellcoef);
-    dfree(ctx->d_step);
-    dfree(ctx->d_partial);
-    dfree(ctx->d_result);
-    if (ctx->h_pending) cudaFreeHost(ctx->h_pending);
-    dfree(ctx->st_parts);
-    dfree(ctx->st_ids);
-    dfree(ctx->st_sid);
-    dfree(ctx->st_off);
-    dfree(ctx->st_cnt);
-    dfree(ctx->st_unknown);
-    for (auto& e : ctx->pend_ev)
-        if (e) cudaEventDestroy(e);
-    for (auto& pair : ctx->ph_ev)
-        for (auto& e : pair)
-            if (e) cudaEventDestroy(e);
-    if (ctx->stream) cudaStreamDestroy(ctx->stream);
-    delete ctx;
-    return IPIC3D_OK;
+    if (ctx && ctx->lent)
+        return fail(IPIC3D_E_STATE, "this context is a universe of a batch: ipic3d_gpu_batch_destroy frees it");
+    return destroy_impl(ctx);
 }
 
 int ipic3d_gpu_upload_particles(ipic3d_ctx* ctx, const ipic3d_particle* particles, const uint64_t* cell_counts,
@@ -1262,6 +1281,427 @@ int ipic3d_gpu_boris(ipic3d_particle* particles, uint64_t n, const double E[3], 
     if (e == cudaSuccess) e = cudaMemcpy(particles, d, n * sizeof(ipic3d_particle), cudaMemcpyDeviceToHost);
     cudaFree(d);
     if (e != cudaSuccess) return fail(IPIC3D_E_CUDA, "boris: %s", cudaGetErrorString(e));
+    return IPIC3D_OK;
+}
+
+}  // extern "C"
+
+// ============================================================================
+// Batched ensemble: independent universes advanced by one launch per kernel.
+//
+// Each universe is an ordinary context on the batch's stream. Before a
+// batched step the host lists every (universe, species) population as a
+// PopJob (its Geom, its Pop view and push constants) and every universe as
+// an InstJob, plus two block maps: push CTA -> (job, CTA of the job) and
+// placement block -> (job, first cell). The tables are rebuilt only when a
+// population's layout changed (upload, re-layout): the host compares the
+// job records byte for byte.
+
+struct ipic3d_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    ipic3d_config cfg{};
+    bool fp32 = false;
+    std::vector<ipic3d_ctx*> inst;
+    // host copies of the device tables
+    std::vector<PopJob<float>> j32;
+    std::vector<PopJob<double>> j64;
+    std::vector<InstJob> ij;
+    char* d_jobs = nullptr;
+    size_t d_jobs_cap = 0;
+    InstJob* d_inst = nullptr;
+    size_t d_inst_cap = 0;
+    int2* d_cta = nullptr;
+    size_t d_cta_cap = 0;
+    int2* d_place = nullptr;
+    size_t d_place_cap = 0;
+    JobStatus* d_status = nullptr;
+    size_t d_status_cap = 0;
+    uint32_t* d_flag = nullptr;  // universes over their pending limit (this step)
+    uint32_t* h_flag = nullptr;  // pinned ring of two
+    cudaEvent_t flag_ev[2] = {nullptr, nullptr};
+    int64_t nctas = 0, nplace = 0;
+    int max_s = 0;
+    int64_t max_cells = 0, max_nodes = 0;
+    bool tables = false;
+    cudaGraphExec_t graph = nullptr;
+    bool graph_valid = false;
+    uint64_t graph_kernels = 0;
+    uint64_t steps = 0, launches = 0;
+};
+
+namespace {
+
+void batch_drop_graph(ipic3d_batch* b) {
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    b->graph_valid = false;
+}
+
+template <typename T>
+std::vector<PopStore<T>>& pops_of(ipic3d_ctx* c);
+template <>
+std::vector<PopStore<float>>& pops_of<float>(ipic3d_ctx* c) { return c->p32; }
+template <>
+std::vector<PopStore<double>>& pops_of<double>(ipic3d_ctx* c) { return c->p64; }
+
+template <typename T>
+std::vector<PopJob<T>>& jobs_of(ipic3d_batch* b);
+template <>
+std::vector<PopJob<float>>& jobs_of<float>(ipic3d_batch* b) { return b->j32; }
+template <>
+std::vector<PopJob<double>>& jobs_of<double>(ipic3d_batch* b) { return b->j64; }
+
+template <typename T>
+void fill_consts(PopJob<T>& J);
+template <>
+void fill_consts<float>(PopJob<float>& J) { J.pc = push32_const(J.g, J.P); }
+template <>
+void fill_consts<double>(PopJob<double>&) {}
+
+// Builds the job records; uploads them (and the block maps) when they differ
+// from the ones on the device.
+template <typename T>
+int batch_tables(ipic3d_batch* b) {
+    std::vector<PopJob<T>> nj;
+    std::vector<InstJob> ni(b->inst.size());
+    const ipic3d_config& cfg = b->cfg;
+    for (size_t i = 0; i < b->inst.size(); ++i) {
+        ipic3d_ctx* c = b->inst[i];
+        InstJob& I = ni[i];
+        std::memset(&I, 0, sizeof(I));
+        I.g = c->g;
+        I.g.deposit = cfg.projector == IPIC3D_PROJECT_CIC ? 1 : 0;
+        I.step = c->d_step;
+        I.job0 = (int)nj.size();
+        I.njobs = (int)pops_of<T>(c).size();
+        I.pend_limit = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(64, c->particles_hint / 200), 0xffffffffu);
+        I.div8 = (cfg.flags & IPIC3D_F_J_DIV8) ? 1 : 0;
+        I.refresh_b = (cfg.flags & IPIC3D_F_REFRESH_NODE_B) ? 1 : 0;
+        I.cellcoef = c->cellcoef;
+        I.coef_scale = (cfg.flags & IPIC3D_F_GATHER_DIV_VOL) ? 1.0 / c->g.vol : 1.0;
+        for (auto& P : pops_of<T>(c)) {
+            PopJob<T> J;
+            std::memset(&J, 0, sizeof(J));
+            J.g = I.g;
+            J.P = P.view();
+            fill_consts<T>(J);
+            J.sort_tmp = P.sort_tmp;
+            J.pend_count = P.pending_in_count;
+            nj.push_back(J);
+        }
+    }
+    auto& cur = jobs_of<T>(b);
+    if (b->tables && cur.size() == nj.size() && b->ij.size() == ni.size() &&
+        std::memcmp(cur.data(), nj.data(), nj.size() * sizeof(PopJob<T>)) == 0 &&
+        std::memcmp(b->ij.data(), ni.data(), ni.size() * sizeof(InstJob)) == 0)
+        return IPIC3D_OK;
+    if (nj.size() > 65535) return fail(IPIC3D_E_INVALID, "batch: more than 65535 populations");
+    std::vector<int2> cta, place;
+    int max_s = 1;
+    int64_t max_cells = 1, max_nodes = 1;
+    for (size_t j = 0; j < nj.size(); ++j) {
+        const int64_t nb = (nj[j].P.capacity + kSlotsPerCta - 1) / kSlotsPerCta;
+        for (int64_t k = 0; k < nb; ++k) cta.push_back(make_int2((int)j, (int)k));
+        const int nc = nj[j].g.ncells;
+        for (int c0 = 0; c0 < nc; c0 += 8) place.push_back(make_int2((int)j, c0));
+    }
+    for (auto& I : ni) {
+        max_s = std::max(max_s, std::max(I.g.sx, std::max(I.g.sy, I.g.sz)));
+        max_cells = std::max<int64_t>(max_cells, I.g.ncells);
+        max_nodes = std::max<int64_t>(max_nodes, (int64_t)(I.g.sx + 1) * (I.g.sy + 1) * (I.g.sz + 1));
+    }
+    if (cta.size() > 0x7fffffffu || place.size() > 0x7fffffffu) return fail(IPIC3D_E_INVALID, "batch too large");
+    int rc;
+    size_t jb = b->d_jobs_cap;
+    if ((rc = grow(b->d_jobs, jb, std::max<size_t>(1, nj.size()) * sizeof(PopJob<T>)))) return rc;
+    b->d_jobs_cap = jb;
+    if ((rc = grow(b->d_inst, b->d_inst_cap, ni.size()))) return rc;
+    if ((rc = grow(b->d_cta, b->d_cta_cap, std::max<size_t>(1, cta.size())))) return rc;
+    if ((rc = grow(b->d_place, b->d_place_cap, std::max<size_t>(1, place.size())))) return rc;
+    if ((rc = grow(b->d_status, b->d_status_cap, std::max<size_t>(1, nj.size())))) return rc;
+    cudaStream_t st = b->stream;
+    CU(cudaMemcpyAsync(b->d_jobs, nj.data(), nj.size() * sizeof(PopJob<T>), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(b->d_inst, ni.data(), ni.size() * sizeof(InstJob), cudaMemcpyHostToDevice, st));
+    if (!cta.empty()) CU(cudaMemcpyAsync(b->d_cta, cta.data(), cta.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+    if (!place.empty())
+        CU(cudaMemcpyAsync(b->d_place, place.data(), place.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+    CU(cudaStreamSynchronize(st));  // the host vectors die here
+    cur.swap(nj);
+    b->ij.swap(ni);
+    b->nctas = (int64_t)cta.size();
+    b->nplace = (int64_t)place.size();
+    b->max_s = max_s;
+    b->max_cells = max_cells;
+    b->max_nodes = max_nodes;
+    b->tables = true;
+    batch_drop_graph(b);
+    return IPIC3D_OK;
+}
+
+// One batched timestep (the body the graph captures); the kernel order of
+// enqueue_step per universe.
+template <typename T>
+int batch_enqueue_step(ipic3d_batch* b) {
+    cudaStream_t st = b->stream;
+    const ipic3d_config& cfg = b->cfg;
+    const PopJob<T>* jobs = reinterpret_cast<const PopJob<T>*>(b->d_jobs);
+    const int ni = (int)b->inst.size(), nj = (int)jobs_of<T>(b).size();
+    const int deposit = cfg.projector == IPIC3D_PROJECT_CIC ? 1 : 0;
+    int n = 0;
+    if (cfg.solver != IPIC3D_SOLVER_STATIC) {
+        n += launch_ghost_batch(b->d_inst, ni, b->max_s, st);
+        if (cfg.solver == IPIC3D_SOLVER_LEAPFROG)
+            n += launch_leapfrog_batch(b->d_inst, ni, b->max_s, (cfg.flags & IPIC3D_F_REFRESH_NODE_B) != 0, st);
+        else
+            n += launch_forward_batch(b->d_inst, ni, b->max_s, st);
+        if (b->fp32 && cfg.mover == IPIC3D_MOVER_FIELD) n += launch_cell_coef_batch(b->d_inst, ni, b->max_cells, st);
+    }
+    n += launch_batch_begin<T>(jobs, nj, b->d_inst, ni, b->max_nodes, deposit, b->d_flag, st);
+    if (nj > 0) {
+        n += launch_push_batch<T>(jobs, b->d_cta, b->nctas, 0, st);
+        n += launch_push_pending_batch<T>(jobs, nj, st);
+        n += launch_place_batch<T>(jobs, b->d_place, b->nplace, st);
+        n += launch_pending_rotate_batch<T>(jobs, nj, st);
+    }
+    if (deposit) n += launch_j_finalize_batch(b->d_inst, ni, b->max_cells, st);
+    n += launch_batch_end<T>(jobs, b->d_inst, ni, b->d_flag, st);
+    b->launches += (uint64_t)n;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(IPIC3D_E_CUDA, "batched kernel launch: %s", cudaGetErrorString(e));
+    return IPIC3D_OK;
+}
+
+// Reads every job's counters back; per universe: the step statistics, lost
+// particles (an error) and the re-layout when too many particles wait.
+template <typename T>
+int batch_after(ipic3d_batch* b) {
+    const auto& jobs = jobs_of<T>(b);
+    const int nj = (int)jobs.size();
+    if (nj == 0) return IPIC3D_OK;
+    cudaStream_t st = b->stream;
+    std::vector<JobStatus> hs(nj);
+    int n = launch_batch_status<T>(reinterpret_cast<const PopJob<T>*>(b->d_jobs), nj, b->d_status, st);
+    b->launches += (uint64_t)n;
+    CU(cudaMemcpyAsync(hs.data(), b->d_status, nj * sizeof(JobStatus), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    for (size_t i = 0; i < b->inst.size(); ++i) {
+        ipic3d_ctx* c = b->inst[i];
+        const InstJob& I = b->ij[i];
+        StepCounters tot{};
+        uint64_t pending = 0;
+        for (int j = I.job0; j < I.job0 + I.njobs; ++j) {
+            const StepCounters& s = hs[j].c;
+            tot.removed += s.removed;
+            tot.migrated += s.migrated;
+            tot.injected += s.injected;
+            tot.lost += s.lost;
+            tot.pending_out += s.pending_out;
+            pending += hs[j].pending_in;
+        }
+        c->last = tot;
+        c->pending_last = pending;
+        if (tot.lost) return fail(IPIC3D_E_CAPACITY, "universe %zu: %u particles lost: pending list full", i, tot.lost);
+        if (pending > I.pend_limit) {
+            c->relayout_steps += 1;
+            int rc = relayout(c);
+            if (rc) return rc;
+        }
+    }
+    return IPIC3D_OK;
+}
+
+template <typename T>
+int batch_run(ipic3d_batch* b, uint64_t num_steps) {
+    int rc;
+    if ((rc = batch_tables<T>(b))) return rc;
+    const bool use_graph = (b->cfg.flags & IPIC3D_F_USE_GRAPH) != 0;
+    cudaStream_t st = b->stream;
+    uint64_t watch_from = 0;
+    for (uint64_t done = 0; done < num_steps;) {
+        if (use_graph) {
+            if (!b->graph_valid) {
+                cudaGraph_t graph = nullptr;
+                CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                const uint64_t before = b->launches;
+                rc = batch_enqueue_step<T>(b);
+                b->graph_kernels = b->launches - before;
+                b->launches = before;  // capturing runs nothing
+                cudaError_t e = cudaStreamEndCapture(st, &graph);
+                if (rc) {
+                    if (graph) cudaGraphDestroy(graph);
+                    return rc;
+                }
+                if (e != cudaSuccess) return fail(IPIC3D_E_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
+                e = cudaGraphInstantiate(&b->graph, graph, 0);
+                cudaGraphDestroy(graph);
+                if (e != cudaSuccess) return fail(IPIC3D_E_CUDA, "batch graph instantiate: %s", cudaGetErrorString(e));
+                b->graph_valid = true;
+            }
+            CU(cudaGraphLaunch(b->graph, st));
+            b->launches += b->graph_kernels;
+        } else if ((rc = batch_enqueue_step<T>(b))) {
+            return rc;
+        }
+        const int slot = (int)(done & 1);
+        CU(cudaMemcpyAsync(b->h_flag + slot, b->d_flag, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        CU(cudaEventRecord(b->flag_ev[slot], st));
+        ++done;
+        ++b->steps;
+        for (auto* c : b->inst) ++c->steps;
+        // the previous step's flag (this step runs meanwhile)
+        if (done >= 2 && done - 2 >= watch_from && done < num_steps) {
+            const int ps = (int)((done - 2) & 1);
+            CU(cudaEventSynchronize(b->flag_ev[ps]));
+            if (b->h_flag[ps]) {
+                if ((rc = batch_after<T>(b))) return rc;
+                if ((rc = batch_tables<T>(b))) return rc;
+                watch_from = done;
+            }
+        }
+    }
+    return batch_after<T>(b);
+}
+
+int batch_check(ipic3d_batch* b) {
+    if (!b) return fail(IPIC3D_E_INVALID, "batch is NULL");
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e != cudaSuccess) return fail(IPIC3D_E_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+    return IPIC3D_OK;
+}
+
+void batch_free(ipic3d_batch* b) {
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    batch_drop_graph(b);
+    for (auto* c : b->inst) {
+        c->lent = false;
+        destroy_impl(c);
+    }
+    b->inst.clear();
+    dfree(b->d_jobs);
+    dfree(b->d_inst);
+    dfree(b->d_cta);
+    dfree(b->d_place);
+    dfree(b->d_status);
+    dfree(b->d_flag);
+    if (b->h_flag) cudaFreeHost(b->h_flag);
+    for (auto& e : b->flag_ev)
+        if (e) cudaEventDestroy(e);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ipic3d_gpu_batch_create(uint32_t count, const ipic3d_props* props, const ipic3d_config* cfg,
+                            ipic3d_batch** out) {
+    if (!props || !cfg || !out) return fail(IPIC3D_E_INVALID, "NULL argument");
+    *out = nullptr;
+    if (count == 0 || count > 65535) return fail(IPIC3D_E_INVALID, "batch of %u universes (1 to 65535)", count);
+    if (cfg->flags & IPIC3D_F_INJECT_LOW_X) return fail(IPIC3D_E_INVALID, "injection is not supported in a batch");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(IPIC3D_E_NODEVICE, "no CUDA device");
+    auto* b = new (std::nothrow) ipic3d_batch();
+    if (!b) return fail(IPIC3D_E_NOMEM, "host allocation");
+    cudaGetDevice(&b->device);
+    b->cfg = *cfg;
+    b->fp32 = cfg->precision == IPIC3D_FP32;
+    auto bail = [&](int rc) {
+        batch_free(b);
+        return rc;
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_flag, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_flag, 0, sizeof(uint32_t), b->stream);
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_flag, 2 * sizeof(uint32_t));
+    for (auto& ev : b->flag_ev)
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e != cudaSuccess)
+        return bail(fail(e == cudaErrorMemoryAllocation ? IPIC3D_E_NOMEM : IPIC3D_E_CUDA, "batch: %s",
+                         cudaGetErrorString(e)));
+    b->h_flag[0] = b->h_flag[1] = 0;
+    b->inst.reserve(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        ipic3d_ctx* c = nullptr;
+        int rc = create_impl(props + i, cfg, b->stream, &c);
+        if (rc) {
+            char msg[512];
+            std::snprintf(msg, sizeof msg, "universe %u: %s", i, g_last_msg);
+            bail(rc);
+            return fail(rc, "%s", msg);
+        }
+        c->lent = true;
+        b->inst.push_back(c);
+    }
+    *out = b;
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_batch_destroy(ipic3d_batch* b) {
+    if (!b) return IPIC3D_OK;
+    batch_free(b);
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_batch_size(ipic3d_batch* b, uint32_t* count) {
+    int rc = batch_check(b);
+    if (rc) return rc;
+    if (!count) return fail(IPIC3D_E_INVALID, "count == NULL");
+    *count = (uint32_t)b->inst.size();
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_batch_universe(ipic3d_batch* b, uint32_t index, ipic3d_ctx** out) {
+    int rc = batch_check(b);
+    if (rc) return rc;
+    if (!out) return fail(IPIC3D_E_INVALID, "out == NULL");
+    if (index >= b->inst.size()) return fail(IPIC3D_E_INVALID, "universe %u of %zu", index, b->inst.size());
+    *out = b->inst[index];
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_batch_step(ipic3d_batch* b, uint64_t num_steps) {
+    int rc = batch_check(b);
+    if (rc) return rc;
+    if (num_steps == 0) return IPIC3D_OK;
+    // universes whose J is stale get their projection first, as in ipic3d_gpu_step
+    if (b->cfg.projector == IPIC3D_PROJECT_CIC)
+        for (auto* c : b->inst)
+            if (!c->j_valid && (rc = project_impl(c))) return rc;
+    return b->fp32 ? batch_run<float>(b, num_steps) : batch_run<double>(b, num_steps);
+}
+
+int ipic3d_gpu_batch_synchronize(ipic3d_batch* b) {
+    int rc = batch_check(b);
+    if (rc) return rc;
+    CU(cudaStreamSynchronize(b->stream));
+    return IPIC3D_OK;
+}
+
+void* ipic3d_gpu_batch_stream(ipic3d_batch* b) { return b ? (void*)b->stream : nullptr; }
+
+int ipic3d_gpu_batch_stats(ipic3d_batch* b, ipic3d_stats* out) {
+    int rc = batch_check(b);
+    if (rc) return rc;
+    if (!out) return fail(IPIC3D_E_INVALID, "out == NULL");
+    std::memset(out, 0, sizeof(*out));
+    for (auto* c : b->inst) {
+        ipic3d_stats s;
+        if ((rc = ipic3d_gpu_stats(c, &s))) return rc;
+        out->particles += s.particles;
+        out->capacity += s.capacity;
+        out->migrated_last += s.migrated_last;
+        out->removed_last += s.removed_last;
+        out->injected_last += s.injected_last;
+        out->rebuilds += s.rebuilds;
+        out->pending_last += s.pending_last;
+        out->relayout_steps += s.relayout_steps;
+    }
+    out->steps = b->steps;
+    out->kernel_launches = b->launches;
     return IPIC3D_OK;
 }
 

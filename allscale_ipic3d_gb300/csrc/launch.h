@@ -26,6 +26,29 @@ int launch_relayout(const Pop<T>& from, const Pop<T>& to, int ncells, int32_t* p
 template <typename T>
 int launch_pending_count(const Pop<T>& P, int32_t* per_cell, cudaStream_t st);
 
+// batched ensemble: job tables built by the host (particles_fp64/32.cu)
+template <typename T>
+int launch_push_batch(const PopJob<T>* jobs, const int2* cta_job, int64_t nctas, int mode, cudaStream_t st);
+template <typename T>
+int launch_push_pending_batch(const PopJob<T>* jobs, int njobs, cudaStream_t st);
+template <typename T>
+int launch_place_batch(const PopJob<T>* jobs, const int2* blk_job, int64_t nblocks, cudaStream_t st);
+template <typename T>
+int launch_pending_rotate_batch(const PopJob<T>* jobs, int njobs, cudaStream_t st);
+template <typename T>
+int launch_batch_begin(const PopJob<T>* jobs, int njobs, const InstJob* inst, int ninst, int64_t max_nodes,
+                       int deposit, uint32_t* flagged, cudaStream_t st);
+template <typename T>
+int launch_batch_end(const PopJob<T>* jobs, const InstJob* inst, int ninst, uint32_t* flagged, cudaStream_t st);
+template <typename T>
+int launch_batch_status(const PopJob<T>* jobs, int njobs, JobStatus* out, cudaStream_t st);
+int launch_cell_coef_batch(const InstJob* inst, int ninst, int64_t max_cells, cudaStream_t st);  // particles_fp32.cu
+Push32Const push32_const(const Geom& g, const Pop<float>& P);                                    // particles_fp32.cu
+int launch_ghost_batch(const InstJob* jobs, int ninst, int max_s, cudaStream_t st);              // fields.cu
+int launch_leapfrog_batch(const InstJob* jobs, int ninst, int max_s, bool refresh_node_b, cudaStream_t st);
+int launch_forward_batch(const InstJob* jobs, int ninst, int max_s, cudaStream_t st);
+int launch_j_finalize_batch(const InstJob* jobs, int ninst, int64_t max_cells, cudaStream_t st);
+
 // fields (fields.cu)
 int launch_ghost(const Geom& g, cudaStream_t st);
 int launch_leapfrog(const Geom& g, bool refresh_node_b, cudaStream_t st);

@@ -411,13 +411,15 @@ __device__ __forceinline__ void register_arrival(const Pop<T>& P, uint32_t o, co
 // thread t the 4 slots from 4t (one cell, start[] is 4-aligned). mode 0 =
 // step (mover + export + deposit), mode 1 = deposit only (the projector over
 // the stored particles, cell.h:787-824).
+// push_body is the work of CTA `blk`; the single-universe kernel passes its
+// block index, the batched kernel the block index within its job.
 template <typename T>
-__global__ void __launch_bounds__(kPushThreads) k_push(Geom g, Pop<T> P, int mode) {
+__device__ __forceinline__ void push_body(const Geom& g, const Pop<T>& P, int64_t blk, int mode) {
     __shared__ int64_t s_start[kMaxCellsPerCta + 1];
     __shared__ int s_count[kMaxCellsPerCta];
-    const int64_t base = (int64_t)blockIdx.x * kSlotsPerCta;
+    const int64_t base = blk * kSlotsPerCta;
     // the cells this CTA's slots belong to (fixed between re-layouts)
-    const int2 cc = __ldg(P.cta_cells + blockIdx.x);
+    const int2 cc = __ldg(P.cta_cells + blk);
     const int c0 = cc.x, nc = cc.y;
     for (int i = threadIdx.x; i <= nc; i += blockDim.x) s_start[i] = P.start[c0 + i];
     for (int i = threadIdx.x; i < nc; i += blockDim.x) s_count[i] = P.count[c0 + i];
@@ -589,12 +591,18 @@ __global__ void __launch_bounds__(kPushThreads) k_push(Geom g, Pop<T> P, int mod
     }
 }
 
-// ---- particles that waited for a slot --------------------------------------
 template <typename T>
-__global__ void k_push_pending(Geom g, Pop<T> P) {
+__global__ void __launch_bounds__(kPushThreads) k_push(Geom g, Pop<T> P, int mode) {
+    push_body<T>(g, P, blockIdx.x, mode);
+}
+
+// ---- particles that waited for a slot --------------------------------------
+// Entries t0, t0 + stride, ... of the pending list.
+template <typename T>
+__device__ __forceinline__ void push_pending_body(const Geom& g, const Pop<T>& P, uint32_t t0, uint32_t stride) {
     const uint32_t n = *P.pending_in_count;
     const double q = P.q;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (uint32_t i = t0; i < n; i += stride) {
         Mover<T> m = P.pending_in[i];
         PState<T> p = {m.x, m.y, m.z, m.u, m.v, m.w};
         int cx, cy, cz;
@@ -616,6 +624,11 @@ __global__ void k_push_pending(Geom g, Pop<T> P) {
         }
         if (g.deposit) deposit_one<T>(g, dest, p, q);
     }
+}
+
+template <typename T>
+__global__ void k_push_pending(Geom g, Pop<T> P) {
+    push_pending_body<T>(g, P, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 // ---- injection at the x = 0 face (not in the reference) ---------------------
@@ -686,9 +699,9 @@ __global__ void k_inject(Geom g, Pop<T> P, InjectParams ip) {
 // arrivals append after the last particle, surplus holes are closed by moving
 // the cell's last particles into them. Arrivals beyond the cell's slots go to
 // the pending list and are pushed and placed again next step.
+// place_body is the work of the warp of cell c (warp-uniform c).
 template <typename T>
-__global__ void k_place(Geom g, Pop<T> P, int32_t* sort_tmp) {
-    const int c = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+__device__ __forceinline__ void place_body(const Geom& g, const Pop<T>& P, int32_t* sort_tmp, int c) {
     const int lane = threadIdx.x & 31;
     if (c >= g.ncells) return;
     const int nh = P.hole_cnt[c], na_all = P.arr_cnt[c];
@@ -752,14 +765,25 @@ __global__ void k_place(Geom g, Pop<T> P, int32_t* sort_tmp) {
     }
 }
 
-// Moves this step's pending list to the next step's input.
 template <typename T>
-__global__ void k_pending_rotate(Pop<T> P, uint32_t* pending_in_count) {
+__global__ void k_place(Geom g, Pop<T> P, int32_t* sort_tmp) {
+    place_body<T>(g, P, sort_tmp, (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5));
+}
+
+// Moves this step's pending list to the next step's input (thread t0 = 0
+// also sets the count).
+template <typename T>
+__device__ __forceinline__ void pending_rotate_body(const Pop<T>& P, uint32_t* pending_in_count, uint32_t t0,
+                                                    uint32_t stride) {
     uint32_t n = P.ctr->pending_out;
     if (n > P.pending_cap) n = P.pending_cap;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        P.pending_in[i] = P.pending_out[i];
-    if (blockIdx.x == 0 && threadIdx.x == 0) *pending_in_count = n;
+    for (uint32_t i = t0; i < n; i += stride) P.pending_in[i] = P.pending_out[i];
+    if (t0 == 0) *pending_in_count = n;
+}
+
+template <typename T>
+__global__ void k_pending_rotate(Pop<T> P, uint32_t* pending_in_count) {
+    pending_rotate_body<T>(P, pending_in_count, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 // ---- re-layout (cells ran out of slack) ---------------------------------------

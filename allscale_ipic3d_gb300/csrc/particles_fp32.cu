@@ -5,7 +5,6 @@
 
 namespace ipg {
 
-namespace {
 Push32Const push32_const(const Geom& g, const Pop<float>& P) {
     Push32Const pc;
     pc.qom = (float)P.qom;
@@ -23,7 +22,6 @@ Push32Const push32_const(const Geom& g, const Pop<float>& P) {
     pc.inv_sz = 1.0f / (float)g.sz;
     return pc;
 }
-}  // namespace
 
 // the FP32 step uses the lean kernels of push32.cuh
 template <>
@@ -49,6 +47,33 @@ int launch_cell_coef(const Geom& g, float* coef, cudaStream_t st) {
     return 1;
 }
 
+template <>
+int launch_push_batch<float>(const PopJob<float>* jobs, const int2* cta_job, int64_t nctas, int mode,
+                             cudaStream_t st) {
+    if (nctas <= 0) return 0;
+    k_push32_batch<3><<<(unsigned)nctas, kPushThreads, 0, st>>>(jobs, cta_job, mode);
+    return 1;
+}
+
+template <>
+int launch_push_pending_batch<float>(const PopJob<float>* jobs, int njobs, cudaStream_t st) {
+    k_push_pending32_batch<<<dim3(2, njobs), 128, 0, st>>>(jobs);
+    return 1;
+}
+
+int launch_cell_coef_batch(const InstJob* inst, int ninst, int64_t max_cells, cudaStream_t st) {
+    int64_t blocks = (max_cells + 127) / 128;
+    if (blocks > 64) blocks = 64;
+    k_cell_coef_batch<<<dim3((unsigned)blocks, ninst), 128, 0, st>>>(inst);
+    return 1;
+}
+
+template int launch_place_batch<float>(const PopJob<float>*, const int2*, int64_t, cudaStream_t);
+template int launch_pending_rotate_batch<float>(const PopJob<float>*, int, cudaStream_t);
+template int launch_batch_begin<float>(const PopJob<float>*, int, const InstJob*, int, int64_t, int, uint32_t*,
+                                       cudaStream_t);
+template int launch_batch_end<float>(const PopJob<float>*, const InstJob*, int, uint32_t*, cudaStream_t);
+template int launch_batch_status<float>(const PopJob<float>*, int, JobStatus*, cudaStream_t);
 template int launch_inject<float>(const Geom&, const Pop<float>&, double, const double*, const double*, uint64_t,
                                   const uint64_t*, cudaStream_t);
 template int launch_place<float>(const Geom&, const Pop<float>&, int32_t*, cudaStream_t);

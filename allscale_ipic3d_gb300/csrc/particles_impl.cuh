@@ -72,4 +72,142 @@ int launch_pending_count(const Pop<T>& P, int32_t* per_cell, cudaStream_t st) {
     return 1;
 }
 
+// ---- batched ensemble ------------------------------------------------------
+// cta_job[b] = (job, CTA of the job) for the push, blk_job[b] = (job, first
+// cell) for the placement (8 cells of one job per 256-thread block).
+template <typename T>
+__global__ void __launch_bounds__(kPushThreads) k_push_batch(const PopJob<T>* __restrict__ jobs,
+                                                             const int2* __restrict__ cta_job, int mode) {
+    const int2 cj = __ldg(cta_job + blockIdx.x);
+    const PopJob<T>& J = jobs[cj.x];
+    push_body<T>(J.g, J.P, cj.y, mode);
+}
+
+template <typename T>
+__global__ void k_push_pending_batch(const PopJob<T>* __restrict__ jobs) {
+    const PopJob<T>& J = jobs[blockIdx.y];
+    push_pending_body<T>(J.g, J.P, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
+template <typename T>
+__global__ void k_place_batch(const PopJob<T>* __restrict__ jobs, const int2* __restrict__ blk_job) {
+    const int2 bj = __ldg(blk_job + blockIdx.x);
+    const PopJob<T>& J = jobs[bj.x];
+    place_body<T>(J.g, J.P, J.sort_tmp, bj.y + (int)(threadIdx.x >> 5));
+}
+
+template <typename T>
+__global__ void k_pending_rotate_batch(const PopJob<T>* __restrict__ jobs) {
+    const PopJob<T>& J = jobs[blockIdx.y];
+    pending_rotate_body<T>(J.P, J.pend_count, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
+// Start of a batched step: blockIdx.y < ninst clears universe y's J and rho
+// (when depositing), blockIdx.y == ninst the step counters of every job and
+// the re-layout flag.
+template <typename T>
+__global__ void k_batch_begin(const PopJob<T>* __restrict__ jobs, int njobs, const InstJob* __restrict__ inst,
+                              int ninst, int deposit, uint32_t* flagged) {
+    const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    if ((int)blockIdx.y == ninst) {
+        for (int64_t j = t0; j < njobs; j += stride) {
+            StepCounters* c = jobs[j].P.ctr;
+            c->outbox = 0; c->pending_out = 0; c->deferred = 0;
+            c->removed = 0; c->migrated = 0; c->injected = 0;
+        }
+        if (t0 == 0) *flagged = 0;
+        return;
+    }
+    if (!deposit) return;
+    const Geom& g = inst[blockIdx.y].g;
+    const int64_t nn = (int64_t)(g.sx + 1) * (g.sy + 1) * (g.sz + 1);
+    for (int64_t t = t0; t < 4 * nn; t += stride) {
+        if (t < 3 * nn) g.J[t] = 0.0;
+        else g.rho[t - 3 * nn] = 0.0;
+    }
+}
+
+// End of a batched step: every universe's step counter advances; universes
+// whose waiting particles exceed their limit, or that lost particles, are
+// counted in *flagged.
+template <typename T>
+__global__ void k_batch_end(const PopJob<T>* __restrict__ jobs, const InstJob* __restrict__ inst, int ninst,
+                            uint32_t* flagged) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ninst) return;
+    const InstJob& b = inst[i];
+    *b.step += 1;
+    uint32_t pend = 0, lost = 0;
+    for (int j = b.job0; j < b.job0 + b.njobs; ++j) {
+        pend += jobs[j].P.ctr->pending_out;
+        lost += jobs[j].P.ctr->lost;
+    }
+    if (pend > b.pend_limit || lost) atomicAdd(flagged, 1u);
+}
+
+template <typename T>
+__global__ void k_batch_status(const PopJob<T>* __restrict__ jobs, int njobs, JobStatus* out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= njobs) return;
+    JobStatus s;
+    s.c = *jobs[j].P.ctr;
+    s.pending_in = *jobs[j].pend_count;
+    s.pad = 0;
+    out[j] = s;
+}
+
+template <typename T>
+int launch_push_batch(const PopJob<T>* jobs, const int2* cta_job, int64_t nctas, int mode, cudaStream_t st);
+
+template <typename T>
+int launch_push_batch_generic(const PopJob<T>* jobs, const int2* cta_job, int64_t nctas, int mode, cudaStream_t st) {
+    if (nctas <= 0) return 0;
+    k_push_batch<T><<<(unsigned)nctas, kPushThreads, 0, st>>>(jobs, cta_job, mode);
+    return 1;
+}
+
+template <typename T>
+int launch_push_pending_batch(const PopJob<T>* jobs, int njobs, cudaStream_t st);
+
+template <typename T>
+int launch_push_pending_batch_generic(const PopJob<T>* jobs, int njobs, cudaStream_t st) {
+    k_push_pending_batch<T><<<dim3(2, njobs), 128, 0, st>>>(jobs);
+    return 1;
+}
+
+template <typename T>
+int launch_place_batch(const PopJob<T>* jobs, const int2* blk_job, int64_t nblocks, cudaStream_t st) {
+    if (nblocks <= 0) return 0;
+    k_place_batch<T><<<(unsigned)nblocks, 256, 0, st>>>(jobs, blk_job);
+    return 1;
+}
+
+template <typename T>
+int launch_pending_rotate_batch(const PopJob<T>* jobs, int njobs, cudaStream_t st) {
+    k_pending_rotate_batch<T><<<dim3(2, njobs), 256, 0, st>>>(jobs);
+    return 1;
+}
+
+template <typename T>
+int launch_batch_begin(const PopJob<T>* jobs, int njobs, const InstJob* inst, int ninst, int64_t max_nodes,
+                       int deposit, uint32_t* flagged, cudaStream_t st) {
+    int64_t gx = (4 * max_nodes + 255) / 256;
+    if (gx < 1) gx = 1;
+    if (gx > 64) gx = 64;
+    k_batch_begin<T><<<dim3((unsigned)gx, ninst + 1), 256, 0, st>>>(jobs, njobs, inst, ninst, deposit, flagged);
+    return 1;
+}
+
+template <typename T>
+int launch_batch_end(const PopJob<T>* jobs, const InstJob* inst, int ninst, uint32_t* flagged, cudaStream_t st) {
+    k_batch_end<T><<<(ninst + 127) / 128, 128, 0, st>>>(jobs, inst, ninst, flagged);
+    return 1;
+}
+
+template <typename T>
+int launch_batch_status(const PopJob<T>* jobs, int njobs, JobStatus* out, cudaStream_t st) {
+    k_batch_status<T><<<(njobs + 127) / 128, 128, 0, st>>>(jobs, njobs, out);
+    return 1;
+}
+
 }  // namespace ipg

@@ -20,21 +20,6 @@
 
 namespace ipg {
 
-// Every constant of the step in FP32, computed on the host: the kernel runs
-// no FP64 instruction per particle (GB300's FP64 rate is a small fraction of
-// its FP32 rate).
-struct Push32Const {
-    float qom;        // charge over mass of the species
-    float k_sub;      // dt * 4 |qom| / (pi c): dt / dt_sub = k_sub |B|^2
-    float dt;
-    float mft;        // -Bext.z R^3
-    float planet_r2;
-    float w[3], inv_w[3];
-    float origin[3];  // domain origin relative to the dipole centre (0,0,0)
-    float center[3];  // object centre (planet)
-    float inv_sy, inv_sz;  // 1 / cells along y and z (cell index -> coordinates)
-};
-
 // E (and B) at cell-relative r from the cell's coefficients: component q
 // (Ex, Ey, Ez, Bx, By, Bz) owns coef[q * 8 + m], m = 1, x, y, z, xy, xz, yz,
 // xyz: two float4 per component, evaluated one component at a time.
@@ -174,13 +159,15 @@ __device__ __forceinline__ float warp_transpose_masked(const float (&acc)[32], b
     return v[0];
 }
 
-template <int kMinBlocks>
-__global__ void __launch_bounds__(kPushThreads, kMinBlocks)
-    k_push32(Geom g, Pop<float> P, Push32Const pc, int mode) {
+// The body of the FP32 push for CTA `blk` of population P (shared by the
+// single-universe kernel and the batched one, which loads g / P / pc from
+// its job table).
+__device__ __forceinline__ void push32_body(const Geom& g, const Pop<float>& P, const Push32Const& pc, int64_t blk,
+                                            int mode) {
     __shared__ int64_t s_start[kMaxCellsPerCta + 1];
     __shared__ int s_count[kMaxCellsPerCta];
-    const int64_t base = (int64_t)blockIdx.x * kSlotsPerCta;
-    const int2 cc = __ldg(P.cta_cells + blockIdx.x);
+    const int64_t base = blk * kSlotsPerCta;
+    const int2 cc = __ldg(P.cta_cells + blk);
     const int c0 = cc.x, nc = cc.y;
     for (int i = threadIdx.x; i <= nc; i += blockDim.x) s_start[i] = P.start[c0 + i];
     for (int i = threadIdx.x; i < nc; i += blockDim.x) s_count[i] = P.count[c0 + i];
@@ -353,10 +340,18 @@ __global__ void __launch_bounds__(kPushThreads, kMinBlocks)
     }
 }
 
-// Pending particles (no slot last step) with the same physics.
-__global__ void k_push_pending32(Geom g, Pop<float> P, Push32Const pc) {
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kPushThreads, kMinBlocks)
+    k_push32(Geom g, Pop<float> P, Push32Const pc, int mode) {
+    push32_body(g, P, pc, blockIdx.x, mode);
+}
+
+// Pending particles (no slot last step) with the same physics; threads
+// t0, t0 + stride, ... of the pending list.
+__device__ __forceinline__ void push_pending32_body(const Geom& g, const Pop<float>& P, const Push32Const& pc,
+                                                    uint32_t t0, uint32_t stride) {
     const uint32_t n = *P.pending_in_count;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (uint32_t i = t0; i < n; i += stride) {
         Mover<float> m = P.pending_in[i];
         PState<float> p = {m.x, m.y, m.z, m.u, m.v, m.w};
         int cx, cy, cz;
@@ -383,12 +378,17 @@ __global__ void k_push_pending32(Geom g, Pop<float> P, Push32Const pc) {
     }
 }
 
+__global__ void k_push_pending32(Geom g, Pop<float> P, Push32Const pc) {
+    push_pending32_body(g, P, pc, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
 // Cell coefficients of the trilinear field polynomial (FP64 sums, stored
 // FP32): coefficient m of component q (Ex, Ey, Ez, Bx, By, Bz) of cell c at
 // coef[c * 48 + q * 8 + m]; monomials m = 1, x, y, z, xy, xz, yz, xyz.
-__global__ void k_cell_coef(const double* __restrict__ field, int sx, int sy, int sz, double scale, float* coef) {
+__device__ __forceinline__ void cell_coef_body(const double* __restrict__ field, int sx, int sy, int sz, double scale,
+                                               float* coef, int64_t t0, int64_t stride) {
     const int64_t total = (int64_t)sx * sy * sz;
-    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < total; c += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t c = t0; c < total; c += stride) {
         const int z = (int)(c % sz), y = (int)((c / sz) % sy), x = (int)(c / ((int64_t)sy * sz));
         for (int q = 0; q < 6; ++q) {
             double f[2][2][2];
@@ -407,6 +407,32 @@ __global__ void k_cell_coef(const double* __restrict__ field, int sx, int sy, in
             for (int k = 0; k < 8; ++k) coef[c * 48 + q * 8 + k] = (float)(m[k] * scale);
         }
     }
+}
+
+__global__ void k_cell_coef(const double* __restrict__ field, int sx, int sy, int sz, double scale, float* coef) {
+    cell_coef_body(field, sx, sy, sz, scale, coef, blockIdx.x * (int64_t)blockDim.x + threadIdx.x,
+                   (int64_t)gridDim.x * blockDim.x);
+}
+
+// ---- batched ensemble (tables as in particles_impl.cuh) ---------------------
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kPushThreads, kMinBlocks)
+    k_push32_batch(const PopJob<float>* __restrict__ jobs, const int2* __restrict__ cta_job, int mode) {
+    const int2 cj = __ldg(cta_job + blockIdx.x);
+    const PopJob<float>& J = jobs[cj.x];
+    push32_body(J.g, J.P, J.pc, cj.y, mode);
+}
+
+__global__ void k_push_pending32_batch(const PopJob<float>* __restrict__ jobs) {
+    const PopJob<float>& J = jobs[blockIdx.y];
+    push_pending32_body(J.g, J.P, J.pc, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
+// blockIdx.y = universe
+__global__ void k_cell_coef_batch(const InstJob* __restrict__ inst) {
+    const InstJob& b = inst[blockIdx.y];
+    cell_coef_body(b.g.field, b.g.sx, b.g.sy, b.g.sz, b.coef_scale, b.cellcoef,
+                   blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
 }
 
 }  // namespace ipg

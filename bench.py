@@ -238,6 +238,140 @@ def cpu_port_run(props, parts, counts, warmup, steps, budget_s):
     return 0.5 * (n0 + n1) * done / dt, threads, done, dt
 
 
+# ---- batched ensemble -----------------------------------------------------------
+ENS_SIZES = (8, 12, 16, 20, 24)
+ENS_PPC = (16, 32, 64, 128, 256)
+ENS_WORKLOAD = ("batched ensemble: 256 independent periodic universes, n^3 cells with n in {8,12,16,20,24} and "
+                "ppc in {16,32,64,128,256} drawn uniformly (seed 12345+i), uniform B (|B| in [0.02,0.2], random "
+                "direction) and E (|E| <= 0.02), Maxwellian sigma in [0.005,0.02], one species (q=-1/ppc, q/m=-1), "
+                "dt=0.1, field-gather Boris mover + CIC deposit of J/rho + migration, fields static")
+
+
+def universe_props(i):
+    from allscale_ipic3d_gb300 import abi
+    rng = np.random.default_rng(12345 + i)
+    n = int(rng.choice(ENS_SIZES))
+    return abi.Props.make(size=(n, n, n), cell_width=(1.0, 1.0, 1.0), dt=0.1, speed_of_light=1.0)
+
+
+def make_universe(i):
+    """Universe i of the ensemble: props, particles grouped by cell, counts,
+    field grids."""
+    from allscale_ipic3d_gb300 import abi
+    rng = np.random.default_rng(12345 + i)
+    n = int(rng.choice(ENS_SIZES))
+    ppc = int(rng.choice(ENS_PPC))
+    d = rng.normal(size=3)
+    B = d / np.linalg.norm(d) * rng.uniform(0.02, 0.2)
+    e = rng.normal(size=3)
+    E = e / np.linalg.norm(e) * rng.uniform(0.0, 0.02)
+    sigma = rng.uniform(0.005, 0.02)
+    props = universe_props(i)
+    nc = n ** 3
+    N = nc * ppc
+    cell = np.repeat(np.arange(nc), ppc)
+    parts = np.zeros(N, abi.PARTICLE_DTYPE)
+    parts["position"] = np.stack([cell // (n * n), (cell // n) % n, cell % n], 1) + rng.random((N, 3))
+    parts["velocity"] = rng.normal(0.0, sigma, (N, 3))
+    parts["q"] = -1.0 / ppc
+    parts["qom"] = -1.0
+    f = np.zeros(abi.field_shape(props))
+    f[..., 0:3] = E
+    f[..., 3:6] = B
+    bc = np.zeros(abi.bcfield_shape(props))
+    bc[..., :] = B
+    return props, parts, np.full(nc, ppc, np.uint64), f, bc
+
+
+def ensemble_config(precision):
+    from allscale_ipic3d_gb300 import abi
+    return abi.Config.make(precision=precision, mover=abi.MOVER_FIELD, solver=abi.SOLVER_STATIC,
+                           projector=abi.PROJECT_CIC, bc=abi.BC_PERIODIC, flags=abi.F_USE_GRAPH)
+
+
+def timed_batch(batch, warmup, steps, sampler=None):
+    import torch
+    batch.step(warmup)
+    batch.synchronize()
+    st = torch.cuda.ExternalStream(batch.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n0 = batch.stats()["particles"]
+    l0 = batch.stats()["kernel_launches"]
+    torch.cuda.synchronize()
+    with (sampler if sampler is not None else _Null()):
+        e0.record(st)
+        batch.step(steps)
+        e1.record(st)
+        e1.synchronize()
+    torch.cuda.synchronize()
+    s = batch.stats()
+    return e0.elapsed_time(e1), 0.5 * (n0 + s["particles"]) * steps, s["kernel_launches"] - l0
+
+
+def timed_plain(batch, count, steps):
+    """The plain (one universe at a time) form on the batch's universes: each
+    universe's own graph, back to back on the batch's stream."""
+    import torch
+    st = torch.cuda.ExternalStream(batch.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    us = [batch.universe(i) for i in range(count)]
+    n0 = sum(u.particle_count() for u in us)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for u in us:
+        u.step(steps)
+    e1.record(st)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    n1 = sum(u.particle_count() for u in us)
+    return e0.elapsed_time(e1), 0.5 * (n0 + n1) * steps
+
+
+def run_ensemble(count, warmup, steps, local):
+    """The batched ensemble in FP32 and FP64 (one launch per kernel per step
+    for all universes), the plain FP64 form (one universe at a time), and the
+    FP32 error against FP64 per universe."""
+    import allscale_ipic3d_gb300 as g
+    from allscale_ipic3d_gb300 import abi
+    t_setup = time.perf_counter()
+    props = [universe_props(i) for i in range(count)]
+    b32 = g.Batch(props, ensemble_config(abi.FP32))
+    b64 = g.Batch(props, ensemble_config(abi.FP64))
+    total = 0
+    for i in range(count):
+        _, parts, counts, f, bc = make_universe(i)
+        total += len(parts)
+        for b in (b32, b64):
+            b.universe(i).upload_fields(f, bc, None)
+            b.universe(i).upload_particles(parts, counts)
+    cells = int(sum(p.ncells for p in props))
+    setup_s = time.perf_counter() - t_setup
+    sampler = ClockSampler(local)
+    ms32, ps32, launches32 = timed_batch(b32, warmup, steps, sampler)
+    ms64, ps64, _ = timed_batch(b64, warmup, steps)
+    rel = []
+    for i in range(count):
+        c32, c64 = b32.universe(i).conserved(), b64.universe(i).conserved()
+        rel.append(abs(c32["kinetic_energy"] - c64["kinetic_energy"]) / abs(c64["kinetic_energy"]))
+    rel = np.array(rel)
+    msp64, psp64 = timed_plain(b64, count, steps)
+    msp32, psp32 = timed_plain(b32, count, steps)
+    v32, v64 = ps32 / (ms32 * 1e-3), ps64 / (ms64 * 1e-3)
+    vp64, vp32 = psp64 / (msp64 * 1e-3), psp32 / (msp32 * 1e-3)
+    b32.close()
+    b64.close()
+    return {"workload": ENS_WORKLOAD, "universes": count, "cells": cells, "particles": total,
+            "steps": steps, "warmup": warmup, "setup_s": round(setup_s, 1),
+            "fp32_batched": {"value": v32, "ms_per_step": ms32 / steps, "gpu_launches": int(launches32)},
+            "fp64_batched": {"value": v64, "ms_per_step": ms64 / steps},
+            "fp64_plain": {"value": vp64, "ms_per_step": msp64 / steps},
+            "fp32_plain": {"value": vp32, "ms_per_step": msp32 / steps},
+            "fp32_batched_over_fp64_plain": v32 / vp64, "fp32_batched_over_fp64_batched": v32 / v64,
+            "kinetic_energy_rel_fp32_vs_fp64": {"after_steps": warmup + steps, "max": float(rel.max()),
+                                                "median": float(np.median(rel))},
+            "clocks": sampler.summary(), "unit": UNIT}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -247,8 +381,12 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", default="all", choices=["all", "fp32"],
-                    help="fp32: only the FP32 timed run and its roofline (small profiling runs)")
+    ap.add_argument("--only", default="all", choices=["all", "fp32", "ensemble"],
+                    help="fp32: only the FP32 timed run and its roofline (small profiling runs); "
+                         "ensemble: only the batched ensemble")
+    ap.add_argument("--universes", type=int, default=256, help="universes of the batched ensemble")
+    ap.add_argument("--ensemble-steps", type=int, default=100)
+    ap.add_argument("--no-ensemble", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -280,6 +418,12 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     import allscale_ipic3d_gb300 as g
     from allscale_ipic3d_gb300 import abi
+
+    if args.only == "ensemble":
+        ens = run_ensemble(args.universes, args.warmup, args.ensemble_steps, local)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "ensemble": ens}))
+        return 0
 
     props, parts, counts = make_workload(12345 + rank)
     ncells = props.ncells
@@ -350,6 +494,10 @@ def main():
         e2e_value = float(t[0])
     e2e.close()
 
+    ens = None
+    if not args.no_ensemble:
+        ens = run_ensemble(args.universes, args.warmup, args.ensemble_steps, local)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, cores, done, secs = cpu_port_run(props, parts, counts, 1, 50, args.cpu_budget)
@@ -371,6 +519,7 @@ def main():
         "error_fp32_vs_fp64": err,
         "stats": stats32,
         "cpu_baseline": cpu,
+        "ensemble": ens,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(parts.nbytes + counts.nbytes),
                 "d2h_bytes_per_step": int(res.nbytes)},
         "clocks": sampler.summary(),

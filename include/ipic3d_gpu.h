@@ -226,6 +226,36 @@ int ipic3d_gpu_profile_read(ipic3d_ctx* ctx, ipic3d_profile* out, int reset);
 int ipic3d_gpu_boris(ipic3d_particle* particles, uint64_t n, const double E[3], const double B[3], double dt,
                      uint64_t nsteps, int push_position);
 
+/* ---- batched ensemble ----------------------------------------------------- */
+/* No counterpart in the reference, which runs one Universe per process
+ * (ipic3d.cxx:94, simulator.h:127-242). A batch holds `count` independent
+ * universes of possibly different sizes and advances all of them with one
+ * launch per kernel of the timestep: every kernel reads a device table of
+ * (universe, species) jobs, so a step costs the same dozen launches for 1
+ * or 10,000 universes (count <= 65535, species per universe <= 16).
+ *
+ * props[i] describes universe i; `cfg` is shared by all of them (precision,
+ * mover, solver, projector, boundaries, flags; IPIC3D_F_INJECT_LOW_X is not
+ * supported in a batch). IPIC3D_F_USE_GRAPH captures one batched step as a
+ * CUDA graph. Each universe is an ordinary context owned by the batch, on
+ * the batch's stream: ipic3d_gpu_batch_universe() lends it out for uploads,
+ * downloads, conserved quantities and counters (ipic3d_gpu_destroy refuses
+ * a lent context with IPIC3D_E_STATE). */
+typedef struct ipic3d_batch ipic3d_batch;
+int ipic3d_gpu_batch_create(uint32_t count, const ipic3d_props* props, const ipic3d_config* cfg,
+                            ipic3d_batch** out);
+int ipic3d_gpu_batch_destroy(ipic3d_batch* batch);
+int ipic3d_gpu_batch_size(ipic3d_batch* batch, uint32_t* count);
+int ipic3d_gpu_batch_universe(ipic3d_batch* batch, uint32_t index, ipic3d_ctx** out);
+/* num_steps timesteps of every universe; the same sequence as
+ * ipic3d_gpu_step per universe, with its counters and re-layouts. */
+int ipic3d_gpu_batch_step(ipic3d_batch* batch, uint64_t num_steps);
+int ipic3d_gpu_batch_synchronize(ipic3d_batch* batch);
+void* ipic3d_gpu_batch_stream(ipic3d_batch* batch);
+/* Sums over the universes (steps = batched steps taken, kernel_launches =
+ * the batch's own launches). */
+int ipic3d_gpu_batch_stats(ipic3d_batch* batch, ipic3d_stats* out);
+
 /* ---- projection without allocation -------------------------------------- */
 /* No counterpart in the reference. The current projection of
  * ipic3d_gpu_project (projectToDensityField over all nodes, cell.h:787-824)

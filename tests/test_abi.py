@@ -68,3 +68,20 @@ def test_create_without_gpu_fails_loudly():
     buf = C.create_string_buffer(256)
     assert lib.ipic3d_gpu_last_error(buf, 256) == abi.E_NODEVICE
     assert buf.value
+
+
+def test_batch_create_without_gpu_fails_loudly():
+    try:
+        import torch
+        if torch.cuda.is_available():
+            import pytest
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    lib = pkg.library(build_if_missing=True)
+    b = C.c_void_p()
+    props = (abi.Props * 2)(abi.Props.make(size=(2, 2, 2)), abi.Props.make(size=(3, 3, 3)))
+    cfg = abi.Config.make()
+    assert lib.ipic3d_gpu_batch_create(2, props, C.byref(cfg), C.byref(b)) == abi.E_NODEVICE
+    assert lib.ipic3d_gpu_batch_create(0, props, C.byref(cfg), C.byref(b)) == abi.E_INVALID
+    assert not b.value
