@@ -324,25 +324,33 @@ __device__ void block_merge(Neu (&acc)[kQ], double* out) {
 }
 
 // Particle sums of one population: sum (q/qom)|v|, sum 1/2 (q/qom)|v|^2,
-// sum q (cell.h:1315-1338). Slots beyond count[c] are skipped.
+// sum q (cell.h:1315-1338), over the particles in slots (slots beyond
+// count[c] are skipped) and those waiting in the pending list.
+template <typename T>
+__device__ __forceinline__ void add_particle(Neu (&acc)[3], double m, double q, T u, T v, T w) {
+    const double a = (double)u, b = (double)v, d = (double)w;
+    double ss = a * a;
+    ss += b * b;
+    ss += d * d;
+    acc[0].add(m * sqrt(ss));
+    acc[1].add(0.5 * m * ss);
+    acc[2].add(q);
+}
+
 template <typename T>
 __global__ void k_reduce_particles(const T* u, const T* v, const T* w, const int64_t* start, const int32_t* count,
-                                   int ncells, double q, double qom, double* partial) {
+                                   int ncells, const Mover<T>* pend, const uint32_t* npend, double q, double qom,
+                                   double* partial) {
     Neu acc[3] = {{0, 0}, {0, 0}, {0, 0}};
     const double m = q / qom;
     for (int c = blockIdx.x; c < ncells; c += gridDim.x) {
         const int64_t s0 = start[c];
         const int n = count[c];
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            const double a = (double)u[s0 + i], b = (double)v[s0 + i], d = (double)w[s0 + i];
-            double ss = a * a;
-            ss += b * b;
-            ss += d * d;
-            acc[0].add(m * sqrt(ss));
-            acc[1].add(0.5 * m * ss);
-            acc[2].add(q);
-        }
+        for (int i = threadIdx.x; i < n; i += blockDim.x) add_particle<T>(acc, m, q, u[s0 + i], v[s0 + i], w[s0 + i]);
     }
+    const uint32_t np = *npend;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x)
+        add_particle<T>(acc, m, q, pend[i].u, pend[i].v, pend[i].w);
     block_merge<3>(acc, partial + 6 * blockIdx.x);
 }
 
@@ -468,8 +476,8 @@ int reduce_blocks() { return 152 * 4; }
 
 template <typename T>
 int launch_reduce_particles(const Pop<T>& P, int ncells, double* partial, cudaStream_t st) {
-    k_reduce_particles<T><<<reduce_blocks(), 256, 0, st>>>(P.u, P.v, P.w, P.start, P.count, ncells, P.q, P.qom,
-                                                            partial);
+    k_reduce_particles<T><<<reduce_blocks(), 256, 0, st>>>(P.u, P.v, P.w, P.start, P.count, ncells, P.pending_in,
+                                                            P.pending_in_count, P.q, P.qom, partial);
     return 1;
 }
 template int launch_reduce_particles<float>(const Pop<float>&, int, double*, cudaStream_t);

@@ -188,11 +188,16 @@ void release_pops(ipic3d_ctx* ctx) {
 }
 
 // Slots reserved for a cell holding n particles: n plus the slack, rounded up
-// to a multiple of 4 (one vector group), at least 4.
+// to a multiple of 4 (one vector group), at least 4. The slack is the largest
+// of slack_min, slack * n and 2 sqrt(n): a thermal plasma that starts with
+// equal counts per cell relaxes to Poisson counts (standard deviation
+// sqrt(n)), and two deviations keep all but a few percent of the cells
+// inside their slots, so few arrivals wait in the pending list.
 int64_t cell_capacity(const ipic3d_config& cfg, uint64_t n) {
     double slack = cfg.slack > 0 ? cfg.slack : 0.125;
     int64_t smin = cfg.slack_min > 0 ? cfg.slack_min : 8;
     int64_t extra = std::max<int64_t>(smin, (int64_t)std::ceil(slack * (double)n));
+    extra = std::max<int64_t>(extra, (int64_t)std::ceil(2.0 * std::sqrt((double)n)));
     int64_t cap = (int64_t)n + extra;
     cap = (cap + 3) & ~int64_t(3);
     return std::max<int64_t>(cap, 4);

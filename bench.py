@@ -247,6 +247,18 @@ ENS_WORKLOAD = ("batched ensemble: 256 independent periodic universes, n^3 cells
                 "dt=0.1, field-gather Boris mover + CIC deposit of J/rho + migration, fields static")
 
 
+def universe_params(i):
+    """(n, ppc, |B|, |E|, sigma) of universe i."""
+    rng = np.random.default_rng(12345 + i)
+    n = int(rng.choice(ENS_SIZES))
+    ppc = int(rng.choice(ENS_PPC))
+    d = rng.normal(size=3)
+    B = rng.uniform(0.02, 0.2)
+    e = rng.normal(size=3)
+    E = rng.uniform(0.0, 0.02)
+    return n, ppc, B, E, rng.uniform(0.005, 0.02)
+
+
 def universe_props(i):
     from allscale_ipic3d_gb300 import abi
     rng = np.random.default_rng(12345 + i)
@@ -349,11 +361,16 @@ def run_ensemble(count, warmup, steps, local):
     sampler = ClockSampler(local)
     ms32, ps32, launches32 = timed_batch(b32, warmup, steps, sampler)
     ms64, ps64, _ = timed_batch(b64, warmup, steps)
-    rel = []
+    rel, lost = [], 0
     for i in range(count):
         c32, c64 = b32.universe(i).conserved(), b64.universe(i).conserved()
         rel.append(abs(c32["kinetic_energy"] - c64["kinetic_energy"]) / abs(c64["kinetic_energy"]))
+        lost += abs(int(c32["particles"]) - int(c64["particles"]))
     rel = np.array(rel)
+    worst = [dict(zip(("universe", "n", "ppc", "B", "E", "sigma", "ke_rel"),
+                      (int(i),) + tuple(universe_params(int(i))) + (float(rel[i]),)))
+             for i in np.argsort(rel)[::-1][:4]]
+    st32, st64 = b32.stats(), b64.stats()
     msp64, psp64 = timed_plain(b64, count, steps)
     msp32, psp32 = timed_plain(b32, count, steps)
     v32, v64 = ps32 / (ms32 * 1e-3), ps64 / (ms64 * 1e-3)
@@ -368,8 +385,147 @@ def run_ensemble(count, warmup, steps, local):
             "fp32_plain": {"value": vp32, "ms_per_step": msp32 / steps},
             "fp32_batched_over_fp64_plain": v32 / vp64, "fp32_batched_over_fp64_batched": v32 / v64,
             "kinetic_energy_rel_fp32_vs_fp64": {"after_steps": warmup + steps, "max": float(rel.max()),
-                                                "median": float(np.median(rel))},
+                                                "median": float(np.median(rel)), "worst": worst,
+                                                "particle_count_differences": lost},
+            "stats_fp32": st32, "stats_fp64": st64,
             "clocks": sampler.summary(), "unit": UNIT}
+
+
+# ---- the other configurations (optional rows: --only c1|c3|c5) ---------------------
+def seeded_plasma(rng, n, per_cell, species, origin=(0.0, 0.0, 0.0), drift=(0.0, 0.0, 0.0)):
+    """Particles grouped by cell: per_cell[c] particles uniform in cell c of an
+    n^3 unit-cell grid; species = [(q, qom, sigma, fraction)], Maxwellian."""
+    from allscale_ipic3d_gb300 import abi
+    nc = n ** 3
+    N = int(per_cell.sum())
+    cell = np.repeat(np.arange(nc), per_cell)
+    parts = np.zeros(N, abi.PARTICLE_DTYPE)
+    parts["position"] = np.array(origin) + np.stack([cell // (n * n), (cell // n) % n, cell % n], 1) + \
+        rng.random((N, 3))
+    frac = np.cumsum([sp[3] for sp in species])
+    which = np.searchsorted(frac, rng.random(N) * frac[-1], side="right")
+    sig = np.array([sp[2] for sp in species])[which]
+    parts["velocity"] = np.array(drift) + rng.normal(0.0, 1.0, (N, 3)) * sig[:, None]
+    parts["q"] = np.array([sp[0] for sp in species])[which]
+    parts["qom"] = np.array([sp[1] for sp in species])[which]
+    return parts, per_cell.astype(np.uint64)
+
+
+def config_c1():
+    """8^3 periodic unit cells, one species (q=-1, m=1), 64 ppc, sigma 0.01,
+    B=(0,0,0.1), E=(0,0.01,0): E x B drift, dt=0.1, 100 steps, FP64."""
+    from allscale_ipic3d_gb300 import abi
+    rng = np.random.default_rng(12345)
+    n = 8
+    props = abi.Props.make(size=(n, n, n), dt=0.1)
+    parts, counts = seeded_plasma(rng, n, np.full(n ** 3, 64), [(-1.0 / 64, -1.0, 0.01, 1.0)])
+    f = np.zeros(abi.field_shape(props))
+    f[..., 1] = 0.01
+    f[..., 5] = 0.1
+    bc = np.zeros(abi.bcfield_shape(props))
+    bc[..., 2] = 0.1
+    kw = dict(mover=abi.MOVER_FIELD, solver=abi.SOLVER_STATIC, projector=abi.PROJECT_CIC, bc=abi.BC_PERIODIC,
+              flags=abi.F_USE_GRAPH)
+    return ("C1 E x B drift: 8^3 periodic cells x 64 ppc (32,768), B=(0,0,0.1), E=(0,0.01,0), sigma 0.01, dt 0.1",
+            props, parts, counts, (f, bc), kw, 100)
+
+
+def config_c3():
+    """64^3 cells, 134,217,728 particles: half uniform, half in a Gaussian blob
+    (sigma 6 cells) centred at (40, 36, 32) cells; electrons (q/m -1,
+    sigma 0.02) and ions (q/m 0.01, sigma 0.002); B=(0.05,0,0.1),
+    self-consistent E (leapfrog), dt=0.05, 50 steps."""
+    from allscale_ipic3d_gb300 import abi
+    rng = np.random.default_rng(12345)
+    n = 64
+    N = 134217728
+    uni = np.full(n ** 3, (N // 2) // n ** 3, np.int64)
+    blob = rng.normal((40.0, 36.0, 32.0), 6.0, (N // 2, 3)).astype(np.int64) % n
+    blob_cells = np.bincount((blob[:, 0] * n + blob[:, 1]) * n + blob[:, 2], minlength=n ** 3)
+    del blob
+    per = uni + blob_cells
+    q = 1e-3 / 256  # macro-particle charge: plasma frequency ~0.03 in the uniform part
+    parts, counts = seeded_plasma(rng, n, per, [(-q, -1.0, 0.02, 0.5), (q, 0.01, 0.002, 0.5)])
+    props = abi.Props.make(size=(n, n, n), dt=0.05)
+    f = np.zeros(abi.field_shape(props))
+    f[..., 3] = 0.05
+    f[..., 5] = 0.1
+    bc = np.zeros(abi.bcfield_shape(props))
+    bc[..., 0] = 0.05
+    bc[..., 2] = 0.1
+    kw = dict(mover=abi.MOVER_FIELD, solver=abi.SOLVER_LEAPFROG, projector=abi.PROJECT_CIC, bc=abi.BC_PERIODIC,
+              flags=abi.F_USE_GRAPH | abi.F_REFRESH_NODE_B)
+    return ("C3 uneven load: 64^3 periodic cells, 134,217,728 particles (half uniform, half a Gaussian blob "
+            "sigma 6 cells at (40,36,32)), e-/ion (q/m -1 / 0.01, sigma 0.02 / 0.002), B=(0.05,0,0.1), "
+            "self-consistent E (leapfrog), dt 0.05; per-cell counts %d..%d" % (per.min(), per.max()),
+            props, parts, counts, (f, bc), kw, 50)
+
+
+def config_c5():
+    """128^3 cells x 128 ppc (268,435,456), electrons and ions (mass ratio
+    100, sigma 0.02 / 0.002), static dipole (|B| = 0.5 at 4 cells, core r < 2
+    masked) and a solar wind vx = 0.02 injected at -x, dt=0.05, 50 steps."""
+    from allscale_ipic3d_gb300 import abi
+    rng = np.random.default_rng(12345)
+    n = 128
+    q = 1e-3 / 64
+    parts, counts = seeded_plasma(rng, n, np.full(n ** 3, 128), [(-q, -1.0, 0.02, 0.5), (q, 0.01, 0.002, 0.5)],
+                                  origin=(-n / 2,) * 3, drift=DRIFT)
+    props = abi.Props.make(size=(n, n, n), dt=DT, planet_radius=2.0, origin=(-n / 2,) * 3,
+                           external_b=(0.0, 0.0, 4.0))
+    kw = dict(mover=abi.MOVER_DIPOLE, solver=abi.SOLVER_STATIC, projector=abi.PROJECT_CIC,
+              bc_low=[abi.BC_OPEN, abi.BC_PERIODIC, abi.BC_PERIODIC],
+              bc_high=[abi.BC_OPEN, abi.BC_PERIODIC, abi.BC_PERIODIC],
+              flags=abi.F_USE_GRAPH | abi.F_INJECT_LOW_X, inject_per_cell=64 * DRIFT[0] * DT, inject_q=-q,
+              inject_qom=-1.0, inject_drift=DRIFT, inject_vth=(0.02, 0.02, 0.02), seed=12345)
+    return ("C5 large dipole: 128^3 cells x 128 ppc (268,435,456), e-/ion mass ratio 100 (sigma 0.02 / 0.002), "
+            "static dipole |B|=0.5 at r=4 cells (core r<2 masked), solar wind vx=0.02 injected at -x, "
+            "outflow +x, dt 0.05", props, parts, counts, None, kw, 50)
+
+
+def run_config(name, warmup, local):
+    """FP32 and FP64 on the same inputs: particle-steps/s, the FP32 push's
+    live roofline, the FP32 energy error against FP64 after the run."""
+    import allscale_ipic3d_gb300 as g
+    from allscale_ipic3d_gb300 import abi
+    t0 = time.perf_counter()
+    desc, props, parts, counts, fields, kw, steps = {"c1": config_c1, "c3": config_c3, "c5": config_c5}[name]()
+    res = {"workload": desc, "cells": props.ncells, "particles": int(len(parts)), "steps": steps,
+           "warmup": warmup}
+    species = sorted({(float(a), float(b)) for a, b in zip(parts["q"][:1000], parts["qom"][:1000])})
+    cons = {}
+    for pname, prec in (("fp32", abi.FP32), ("fp64", abi.FP64)):
+        sim = g.Simulation(props, abi.Config.make(precision=prec, **kw))
+        if fields is not None:
+            sim.upload_fields(fields[0], fields[1], None)
+        # register the species with a few particles, so that the large upload
+        # takes the device path (one copy, classification on the GPU)
+        first = np.unique(parts[["q", "qom"]][:100000], return_index=True)[1]
+        c0 = np.zeros(props.ncells, np.uint64)
+        c0[0] = len(first)
+        sim.upload_particles(parts[first], c0)
+        sim.upload_particles(parts, counts)
+        sampler = ClockSampler(local)
+        ms, ps, launches, n0 = run_timed(sim, warmup, steps, sampler if pname == "fp32" else None)
+        res[pname] = {"value": ps / (ms * 1e-3), "ms_per_step": ms / steps, "gpu_launches": int(launches),
+                      "stats": sim.stats()}
+        if pname == "fp32":
+            res["clocks"] = sampler.summary()
+        cons[pname] = sim.conserved()
+        res[pname]["roofline"] = push_roofline(sim, pname, 5, props.ncells)
+        sim.close()
+    tot = lambda c: c["kinetic_energy"] + c["e_energy"] + c["b_energy"]
+    res["error_fp32_vs_fp64"] = {"steps": warmup + steps + 5,
+                                 "total_energy_rel": abs(tot(cons["fp32"]) - tot(cons["fp64"])) / abs(tot(cons["fp64"])),
+                                 "kinetic_energy_rel": abs(cons["fp32"]["kinetic_energy"] -
+                                                           cons["fp64"]["kinetic_energy"]) /
+                                 abs(cons["fp64"]["kinetic_energy"]),
+                                 "particles_fp32": cons["fp32"]["particles"],
+                                 "particles_fp64": cons["fp64"]["particles"]}
+    res["fp32_over_fp64"] = res["fp32"]["value"] / res["fp64"]["value"]
+    res["species"] = species
+    res["setup_and_run_s"] = round(time.perf_counter() - t0, 1)
+    return res
 
 
 def main():
@@ -381,9 +537,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", default="all", choices=["all", "fp32", "ensemble"],
+    ap.add_argument("--only", default="all", choices=["all", "fp32", "ensemble", "c1", "c3", "c5"],
                     help="fp32: only the FP32 timed run and its roofline (small profiling runs); "
-                         "ensemble: only the batched ensemble")
+                         "ensemble: only the batched ensemble; c1/c3/c5: that configuration alone")
     ap.add_argument("--universes", type=int, default=256, help="universes of the batched ensemble")
     ap.add_argument("--ensemble-steps", type=int, default=100)
     ap.add_argument("--no-ensemble", action="store_true")
@@ -418,6 +574,12 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     import allscale_ipic3d_gb300 as g
     from allscale_ipic3d_gb300 import abi
+
+    if args.only in ("c1", "c3", "c5"):
+        res = run_config(args.only, args.warmup, local)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "unit": UNIT, args.only: res}))
+        return 0
 
     if args.only == "ensemble":
         ens = run_ensemble(args.universes, args.warmup, args.ensemble_steps, local)

@@ -115,6 +115,8 @@ def test_adapter_standin_matches_c_abi(tmp_path, policy, fp32):
     a, b = sorted_by_cell(out, out_counts), sorted_by_cell(p2, c2)
     if policy == 0:  # no floating-point atomics on the particles' data path
         assert a.tobytes() == b.tobytes()
-    else:  # the fields evolve from FP64 atomic sums (order free)
+    else:  # the fields evolve from atomic sums (order free): FP64 rounding,
+        # or FP32 rounding where the FP32 deposit sums a warp's particles first
+        rtol, atol = (1e-5, 1e-7) if fp32 else (1e-9, 1e-12)
         for k in ("position", "velocity"):
-            np.testing.assert_allclose(a[k], b[k], rtol=1e-9, atol=1e-12)
+            np.testing.assert_allclose(a[k], b[k], rtol=rtol, atol=atol)
