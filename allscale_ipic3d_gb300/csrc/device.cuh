@@ -130,6 +130,18 @@ struct InstJob {
     double coef_scale;      // 1 / vol with the gather normalisation, else 1
 };
 
+// Copies a batch job record into shared memory (all threads of the block
+// call it; followed by a barrier), so the kernel body reads its fields from
+// shared memory instead of global memory.
+template <typename Job>
+__device__ __forceinline__ void load_job(Job& dst, const Job* src) {
+    static_assert(sizeof(Job) % 4 == 0, "job records are word-sized");
+    const int* s = reinterpret_cast<const int*>(src);
+    int* d = reinterpret_cast<int*>(&dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(Job) / 4); i += blockDim.x) d[i] = s[i];
+    __syncthreads();
+}
+
 // Per-job counters as read back after a batched step.
 struct JobStatus {
     StepCounters c;

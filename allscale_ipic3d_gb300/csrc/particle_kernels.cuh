@@ -358,6 +358,37 @@ __device__ __forceinline__ void deposit_one(const Geom& g, int c, const PState<T
     }
 }
 
+// Deposit of the warp's leavers into their destination cells, one leaver at
+// a time: lane l adds value l (corner l & 7, component l >> 3) of the leaver's
+// cloud-in-cell contribution, the same values deposit_one adds one by one, so
+// a leaver costs one 32-lane atomic instead of 32 serial ones. Every lane of
+// the warp must call it.
+template <typename T>
+__device__ __forceinline__ void warp_deposit_leavers(const Geom& g, bool leave, int dest, const PState<T>& p,
+                                                     double q) {
+    unsigned m = __ballot_sync(0xffffffffu, leave);
+    const int lane = threadIdx.x & 31, corner = lane & 7, comp = lane >> 3;
+    while (m) {
+        const int src = __ffs(m) - 1;
+        m &= m - 1;
+        const int c = __shfl_sync(0xffffffffu, dest, src);
+        PState<T> s;
+        s.x = __shfl_sync(0xffffffffu, p.x, src);
+        s.y = __shfl_sync(0xffffffffu, p.y, src);
+        s.z = __shfl_sync(0xffffffffu, p.z, src);
+        s.u = __shfl_sync(0xffffffffu, p.u, src);
+        s.v = __shfl_sync(0xffffffffu, p.v, src);
+        s.w = __shfl_sync(0xffffffffu, p.w, src);
+        int cx, cy, cz;
+        cell_coords(g, c, cx, cy, cz);
+        T rx, ry, rz;
+        frac_in_cell(g, cx, cy, cz, s, rx, ry, rz);
+        const double fac = (double)cic_weight<T>(corner, rx, ry, rz);
+        const double Q = comp == 0 ? (double)s.u : (comp == 1 ? (double)s.v : (double)s.w);
+        node_atomic_add(g, cx, cy, cz, corner * 4 + comp, comp < 3 ? (q * Q) * fac : q * fac);
+    }
+}
+
 // Warp transpose-reduction: every lane holds 32 values; afterwards lane l
 // holds the warp-wide sum of value l (31 exchanges in total).
 template <typename T>
@@ -532,7 +563,6 @@ __device__ __forceinline__ void push_body(const Geom& g, const Pop<T>& P, int64_
             } else {
                 atomicAdd(&P.ctr->lost, 1u);
             }
-            if (deposit) deposit_one<T>(g, dst[j], ps[j], q);
             ++nmig;
         }
         if (outc[j] == kMove || outc[j] == kDrop) {
@@ -540,6 +570,10 @@ __device__ __forceinline__ void push_body(const Geom& g, const Pop<T>& P, int64_
             P.hole_list[s_start[lc] + k] = (int32_t)(s0 + j);
             if (outc[j] == kDrop) ++nrem;
         }
+    }
+    if (deposit) {
+#pragma unroll
+        for (int j = 0; j < kVec; ++j) warp_deposit_leavers<T>(g, outc[j] == kMove, dst[j], ps[j], q);
     }
     nmig = __reduce_add_sync(0xffffffffu, nmig);
     nrem = __reduce_add_sync(0xffffffffu, nrem);

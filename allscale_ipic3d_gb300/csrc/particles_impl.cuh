@@ -78,9 +78,10 @@ int launch_pending_count(const Pop<T>& P, int32_t* per_cell, cudaStream_t st) {
 template <typename T>
 __global__ void __launch_bounds__(kPushThreads) k_push_batch(const PopJob<T>* __restrict__ jobs,
                                                              const int2* __restrict__ cta_job, int mode) {
+    __shared__ PopJob<T> job;
     const int2 cj = __ldg(cta_job + blockIdx.x);
-    const PopJob<T>& J = jobs[cj.x];
-    push_body<T>(J.g, J.P, cj.y, mode);
+    load_job(job, jobs + cj.x);
+    push_body<T>(job.g, job.P, cj.y, mode);
 }
 
 template <typename T>
@@ -91,9 +92,10 @@ __global__ void k_push_pending_batch(const PopJob<T>* __restrict__ jobs) {
 
 template <typename T>
 __global__ void k_place_batch(const PopJob<T>* __restrict__ jobs, const int2* __restrict__ blk_job) {
+    __shared__ PopJob<T> job;
     const int2 bj = __ldg(blk_job + blockIdx.x);
-    const PopJob<T>& J = jobs[bj.x];
-    place_body<T>(J.g, J.P, J.sort_tmp, bj.y + (int)(threadIdx.x >> 5));
+    load_job(job, jobs + bj.x);
+    place_body<T>(job.g, job.P, job.sort_tmp, bj.y + (int)(threadIdx.x >> 5));
 }
 
 template <typename T>

@@ -13,7 +13,8 @@
 //   * deposit (cell.h:810-816 in scatter form): per thread the monomial
 //     moments sum_p Q m(r_p), Q in {u, v, w, 1}, m in {1, x, y, z, xy, xz,
 //     yz, xyz}; one butterfly per axis turns them into the 8 corner weights
-//     (1-t, t), then a warp transpose-reduction and one FP64 atomic per lane.
+//     (1-t, t); each warp sums them per cell in shared memory and issues
+//     one FP64 atomic per cell, corner and component.
 #pragma once
 
 #include "particle_kernels.cuh"
@@ -132,33 +133,6 @@ __device__ __forceinline__ int step32(const Geom& g, const Push32Const& pc, cons
     return kMove;
 }
 
-// Lane l ends with the sum over the lanes with `mine` of value l (masked
-// transpose-reduction; the first exchange applies the mask, so acc stays).
-__device__ __forceinline__ float warp_transpose_masked(const float (&acc)[32], bool mine) {
-    const int lane = threadIdx.x & 31;
-    float v[16];
-    {
-        const bool upper = (lane & 16) != 0;
-#pragma unroll
-        for (int i = 0; i < 16; ++i) {
-            const float send = mine ? (upper ? acc[i] : acc[i + 16]) : 0.f;
-            const float keep = mine ? (upper ? acc[i + 16] : acc[i]) : 0.f;
-            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-        }
-    }
-#pragma unroll
-    for (int off = 8; off >= 1; off >>= 1) {
-        const bool upper = (lane & off) != 0;
-#pragma unroll
-        for (int i = 0; i < off; ++i) {
-            const float send = upper ? v[i] : v[i + off];
-            const float keep = upper ? v[i + off] : v[i];
-            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
-        }
-    }
-    return v[0];
-}
-
 // The body of the FP32 push for CTA `blk` of population P (shared by the
 // single-universe kernel and the batched one, which loads g / P / pc from
 // its job table).
@@ -166,6 +140,10 @@ __device__ __forceinline__ void push32_body(const Geom& g, const Pop<float>& P, 
                                             int mode) {
     __shared__ int64_t s_start[kMaxCellsPerCta + 1];
     __shared__ int s_count[kMaxCellsPerCta];
+    // deposit staging, one tile per warp: value l of lane t at [l * 33 + t]
+    // (the odd stride puts a lane's 32 values, and a value's 32 lanes, in 32
+    // different banks)
+    __shared__ float s_acc[kPushThreads / 32][32 * 33];
     const int64_t base = blk * kSlotsPerCta;
     const int2 cc = __ldg(P.cta_cells + blk);
     const int c0 = cc.x, nc = cc.y;
@@ -276,7 +254,6 @@ __device__ __forceinline__ void push32_body(const Geom& g, const Pop<float>& P, 
             } else {
                 atomicAdd(&P.ctr->lost, 1u);
             }
-            if (deposit) deposit_one<float>(g, dst[j], ps[j], P.q);
             ++nmig;
         }
         if (outc[j] == kMove || outc[j] == kDrop) {
@@ -284,6 +261,10 @@ __device__ __forceinline__ void push32_body(const Geom& g, const Pop<float>& P, 
             P.hole_list[s_start[lc] + k] = (int32_t)(s0 + j);
             if (outc[j] == kDrop) ++nrem;
         }
+    }
+    if (deposit) {
+#pragma unroll
+        for (int j = 0; j < kVec; ++j) warp_deposit_leavers<float>(g, outc[j] == kMove, dst[j], ps[j], P.q);
     }
     nmig = __reduce_add_sync(0xffffffffu, nmig);
     nrem = __reduce_add_sync(0xffffffffu, nrem);
@@ -322,20 +303,37 @@ __device__ __forceinline__ void push32_body(const Geom& g, const Pop<float>& P, 
             m[4] = c100 - c101; m[5] = c101;  // (1,0,0), (1,0,1)
             m[6] = c110 - c111; m[7] = c111;  // (1,1,0), (1,1,1)
         }
-        // value index of lane l in the transpose: l = q * 8 + corner; the
-        // node_atomic_add index is corner * 4 + comp with comp = q
-        unsigned todo = __ballot_sync(0xffffffffu, has_acc);
-        while (todo) {
-            const int leader = __ffs(todo) - 1;
-            const int gcell = __shfl_sync(0xffffffffu, cell, leader);
-            const bool mine = has_acc && cell == gcell;
-            const unsigned grp = __ballot_sync(0xffffffffu, mine);
-            const float tot = warp_transpose_masked(acc, mine);
+        // per cell of the warp and value l = q * 8 + corner: lane l sums value
+        // l over the cell's lanes (a contiguous run: slots are grouped by
+        // cell), then one FP64 atomic per lane and cell (node_atomic_add index
+        // corner * 4 + comp with comp = q). Warp-local: no CTA barrier.
+        float* tile = s_acc[threadIdx.x >> 5];
+#pragma unroll
+        for (int l = 0; l < 32; ++l) tile[l * 33 + lane] = acc[l];
+        const unsigned todo = __ballot_sync(0xffffffffu, has_acc);
+        // first lane of every run of lanes with the same cell
+        const int prev_cell = __shfl_up_sync(0xffffffffu, cell, 1);
+        unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev_cell != cell);
+        __syncwarp();
+        const float* row = tile + lane * 33;
+        while (heads) {
+            const int a = __ffs(heads) - 1;
+            heads &= heads - 1;
+            const int b = heads ? __ffs(heads) - 1 : 32;  // run [a, b)
+            if (!(todo & (((b < 32 ? (1u << b) : 0u) - 1u) & ~((1u << a) - 1u)))) continue;
+            float sum = 0.f;
+            for (int t = a; t < b; ++t) sum += row[t];
+            const int gcell = __shfl_sync(0xffffffffu, cell, a);
             int gx, gy, gz;
-            cell_coords(g, gcell, gx, gy, gz);
-            const int q = lane >> 3, corner = lane & 7;
-            node_atomic_add(g, gx, gy, gz, corner * 4 + q, (double)tot * P.q);
-            todo &= ~grp;
+            if (g.ncells < (1 << 24) && g.sy < 4096 && g.sz < 4096) {
+                const int u = fast_div(gcell, g.sz, pc.inv_sz);
+                gz = gcell - u * g.sz;
+                gx = fast_div(u, g.sy, pc.inv_sy);
+                gy = u - gx * g.sy;
+            } else {
+                cell_coords(g, gcell, gx, gy, gz);
+            }
+            node_atomic_add(g, gx, gy, gz, (lane & 7) * 4 + (lane >> 3), (double)sum * P.q);
         }
     }
 }
@@ -418,9 +416,10 @@ __global__ void k_cell_coef(const double* __restrict__ field, int sx, int sy, in
 template <int kMinBlocks>
 __global__ void __launch_bounds__(kPushThreads, kMinBlocks)
     k_push32_batch(const PopJob<float>* __restrict__ jobs, const int2* __restrict__ cta_job, int mode) {
+    __shared__ PopJob<float> job;
     const int2 cj = __ldg(cta_job + blockIdx.x);
-    const PopJob<float>& J = jobs[cj.x];
-    push32_body(J.g, J.P, J.pc, cj.y, mode);
+    load_job(job, jobs + cj.x);
+    push32_body(job.g, job.P, job.pc, cj.y, mode);
 }
 
 __global__ void k_push_pending32_batch(const PopJob<float>* __restrict__ jobs) {

@@ -643,10 +643,19 @@ def main():
     e2e.cell_counts()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    phase = {"upload": 0.0, "step": 0.0, "counts": 0.0}
     for _ in range(args.e2e_steps):
+        ta = time.perf_counter()
         e2e.upload_particles(host, counts)
+        tb = time.perf_counter()
         e2e.step(1)
+        e2e.synchronize()
+        tc = time.perf_counter()
         res = e2e.cell_counts()
+        td = time.perf_counter()
+        phase["upload"] += tb - ta
+        phase["step"] += tc - tb
+        phase["counts"] += td - tc
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_value = len(parts) * args.e2e_steps / e2e_s
@@ -683,6 +692,7 @@ def main():
         "cpu_baseline": cpu,
         "ensemble": ens,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(parts.nbytes + counts.nbytes),
+                "ms_per_phase": {k: round(1e3 * v / args.e2e_steps, 3) for k, v in phase.items()},
                 "d2h_bytes_per_step": int(res.nbytes)},
         "clocks": sampler.summary(),
         "gpu_launches": int(launches32),
