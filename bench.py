@@ -143,7 +143,7 @@ def measured_peak():
 
 def profiled_traffic(precision):
     """DRAM bytes per push launch from the committed ncu summary, if any."""
-    name = os.path.join(ROOT, "profiles", "k_push_%s_dipole32.md" % precision)
+    name = os.path.join(ROOT, "profiles", "k_push32_dipole32.md" if precision == "fp32" else "k_push64_dipole32.md")
     if not os.path.exists(name):
         return None
     for line in open(name):
@@ -186,29 +186,35 @@ class _Null:
         pass
 
 
-def push_roofline(sim, precision, nsteps, ncells):
-    """Live per-phase CUDA-event times of eager steps; the push kernel's
-    algorithmic bytes per launch over its duration."""
+def push_roofline(sim, precision, nsteps, props, pops):
+    """Live CUDA-event times of the push phase over `nsteps` eager steps (the
+    phase runs one launch per species population, `pops` launches of equal
+    size); the push kernel's algorithmic bytes per launch over its average
+    launch duration. Algorithmic bytes per launch: the particles' state read
+    and written once (12 x 4 B FP32, 12 x 8 B FP64), the per-cell field
+    coefficients read once (FP32: 48 floats per cell) or the node E, B read
+    once (FP64: 48 B per node), and the 4 FP64 node moments written once
+    (32 B per node)."""
     sim.profile(True)
     sim.step(nsteps)
     prof = sim.profile_read(reset=True)
     sim.profile(False)
     push = prof["push"]
-    ms_per = push["ms"] / max(push["launches"], 1)
-    parts = push["particles"] / max(push["launches"], 1)
+    ms_per = push["ms"] / max(push["launches"], 1) / pops
+    parts = push["particles"] / max(push["launches"], 1) / pops
     elem = 4 if precision == "fp32" else 8
-    # read + write of the 6 state components per particle, plus per cell the
-    # node fields read (E,B: 32 B FP32 / 48 B FP64) and the 4 FP64 moments
-    # accumulated (32 B)
-    per_cell = (32 if precision == "fp32" else 48) + 32
-    bytes_per = parts * 12 * elem + ncells * per_cell
+    nodes = (props.size[0] + 1) * (props.size[1] + 1) * (props.size[2] + 1)
+    if precision == "fp32":
+        bytes_per = parts * 12 * elem + props.ncells * 48 * 4 + nodes * 32
+    else:
+        bytes_per = parts * 12 * elem + nodes * (48 + 32)
     peak, src = measured_peak()
     achieved = bytes_per / (ms_per * 1e-3) / 1e9
     phases = {k: round(v["ms"] / max(v["launches"], 1), 5) for k, v in prof.items() if v["launches"]}
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": profiled_traffic(precision), "kernel": "ipg::k_push<%s>" % ("float" if elem == 4 else "double"),
-            "bytes_per_launch": bytes_per, "ms_per_launch": ms_per, "peak_source": src,
-            "phase_ms_per_step": phases}
+            "traffic": profiled_traffic(precision), "kernel": "ipg::k_push32<3>" if elem == 4 else "ipg::k_push<double>",
+            "bytes_per_launch": bytes_per, "ms_per_launch": ms_per, "launches_per_step": pops,
+            "peak_source": src + ", burst copy", "phase_ms_per_step": phases}
 
 
 def cpu_port_run(props, parts, counts, warmup, steps, budget_s):
@@ -512,7 +518,7 @@ def run_config(name, warmup, local):
         if pname == "fp32":
             res["clocks"] = sampler.summary()
         cons[pname] = sim.conserved()
-        res[pname]["roofline"] = push_roofline(sim, pname, 5, props.ncells)
+        res[pname]["roofline"] = push_roofline(sim, pname, 5, props, len(species))
         sim.close()
     tot = lambda c: c["kinetic_energy"] + c["e_energy"] + c["b_energy"]
     res["error_fp32_vs_fp64"] = {"steps": warmup + steps + 5,
@@ -608,7 +614,7 @@ def main():
     stats32 = sim32.stats()
 
     if args.only == "fp32":
-        roof = push_roofline(sim32, "fp32", 20, ncells)
+        roof = push_roofline(sim32, "fp32", 20, props, 2)
         out = {"metric": METRIC, "value": value32, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "ms_per_step": ms32 / args.steps, "roofline": roof, "stats": stats32, "gpu_launches": int(launches32)}
         if rank == 0:
@@ -630,8 +636,8 @@ def main():
     value64 = psteps64 / (ms64 * 1e-3)
     stats64 = sim64.stats()
     # ---- live roofline of the push kernels (eager steps, CUDA events) ----
-    roof = push_roofline(sim32, "fp32", 20, ncells)
-    roof64 = push_roofline(sim64, "fp64", 10, ncells)
+    roof = push_roofline(sim32, "fp32", 20, props, 2)
+    roof64 = push_roofline(sim64, "fp64", 10, props, 2)
     sim64.close()
 
     # ---- end to end through the public API, host buffers ----
