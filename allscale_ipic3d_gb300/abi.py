@@ -18,6 +18,7 @@ E_CUDA = -3
 E_CAPACITY = -4
 E_NODEVICE = -5
 E_STATE = -6
+E_TIMEOUT = -7
 
 # ---- enums -----------------------------------------------------------------
 FP64, FP32 = 0, 1

@@ -7,9 +7,8 @@
 //   * one or more particle populations (one per distinct (q, qom) pair),
 //     each a structure-of-arrays grouped by cell: cell c owns the slot range
 //     [start[c], start[c+1]); its first count[c] slots hold particles, the
-//     rest is slack for arrivals. start[] is a multiple of 4 so that four
-//     consecutive slots always belong to one cell (one 128-bit vector load
-//     per array and thread).
+//     rest is slack for arrivals. start[] is a multiple of 8 so that a
+//     thread's 4 or 8 consecutive slots always belong to one cell.
 //   * FP64 populations store absolute positions (Particle::position,
 //     particle.h:11); FP32 populations store the position relative to the
 //     cell origin in units of the cell width, in [0, 1] when inside.
@@ -23,7 +22,8 @@ namespace ipg {
 constexpr int kVec = 4;                 // particles per thread (one float4 / 2x double2)
 constexpr int kPushThreads = 256;       // threads per CTA of the push kernel
 constexpr int kSlotsPerCta = kVec * kPushThreads;
-constexpr int kMaxCellsPerCta = kSlotsPerCta / 4 + 2;  // caps are >= 4 slots
+constexpr int kSlotAlign = 8;          // start[] and every cell's capacity are multiples of 8
+constexpr int kMaxCellsPerCta = kSlotsPerCta / kSlotAlign + 2;
 
 // Geometry and physics of one universe (UniverseProperties plus the policy).
 struct Geom {
@@ -66,7 +66,7 @@ struct StepCounters {
     uint32_t migrated;      // particles that changed cell
     uint32_t injected;
     uint32_t lost;          // pending list overflow (must stay 0)
-    uint32_t pad;
+    uint32_t timeouts;      // CTAs that gave up a bounded wait (must stay 0)
 };
 
 template <typename T>
@@ -89,7 +89,12 @@ struct Pop {
     StepCounters* ctr;
     int64_t capacity;       // total slots
     double q, qom;
+    int32_t shape;          // launch shape of the FP32 push (kPushShape*)
+    int32_t pad;
 };
+
+// Launch shapes of the pipelined FP32 push (shared-memory stages per CTA).
+enum : int32_t { kPushStages3 = 0, kPushStages2 = 1, kPushShapeCount = 2 };
 
 // Every constant of the step in FP32, computed on the host: the kernel runs
 // no FP64 instruction per particle (GB300's FP64 rate is a small fraction of

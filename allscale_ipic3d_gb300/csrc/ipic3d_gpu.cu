@@ -72,6 +72,7 @@ struct PopStore {
     Mover<T>*outbox = nullptr, *pending_in = nullptr, *pending_out = nullptr;
     uint32_t* pending_in_count = nullptr;
     StepCounters* ctr = nullptr;
+    int32_t shape = 0;             // launch shape of the FP32 push
     std::vector<int64_t> h_start;  // host copy of start[]
 
     void release() {
@@ -103,6 +104,8 @@ struct PopStore {
         P.capacity = capacity;
         P.q = q;
         P.qom = qom;
+        P.shape = shape;
+        P.pad = 0;
         return P;
     }
 };
@@ -188,7 +191,7 @@ void release_pops(ipic3d_ctx* ctx) {
 }
 
 // Slots reserved for a cell holding n particles: n plus the slack, rounded up
-// to a multiple of 4 (one vector group), at least 4. The slack is the largest
+// to a multiple of kSlotAlign (a push thread's slots), at least kSlotAlign. The slack is the largest
 // of slack_min, slack * n and 2 sqrt(n): a thermal plasma that starts with
 // equal counts per cell relaxes to Poisson counts (standard deviation
 // sqrt(n)), and two deviations keep all but a few percent of the cells
@@ -199,8 +202,8 @@ int64_t cell_capacity(const ipic3d_config& cfg, uint64_t n) {
     int64_t extra = std::max<int64_t>(smin, (int64_t)std::ceil(slack * (double)n));
     extra = std::max<int64_t>(extra, (int64_t)std::ceil(2.0 * std::sqrt((double)n)));
     int64_t cap = (int64_t)n + extra;
-    cap = (cap + 3) & ~int64_t(3);
-    return std::max<int64_t>(cap, 4);
+    cap = (cap + kSlotAlign - 1) & ~int64_t(kSlotAlign - 1);
+    return std::max<int64_t>(cap, kSlotAlign);
 }
 
 template <typename T>
@@ -209,6 +212,7 @@ int alloc_pop(ipic3d_ctx* ctx, PopStore<T>& P, const std::vector<uint64_t>& coun
     P.h_start.assign(nc + 1, 0);
     for (int64_t c = 0; c < nc; ++c) P.h_start[c + 1] = P.h_start[c] + cell_capacity(ctx->cfg, counts[c]);
     P.capacity = P.h_start[nc];
+    P.shape = ctx->cfg.block_size == 3 ? kPushStages3 : kPushStages2;
     // every particle can wait at most once per step: capacity entries suffice
     P.pending_cap = (uint32_t)std::min<int64_t>(std::max<int64_t>(1 << 12, P.capacity), 0x7fffffff);
     int64_t inject_cap = 0;
@@ -225,8 +229,12 @@ int alloc_pop(ipic3d_ctx* ctx, PopStore<T>& P, const std::vector<uint64_t>& coun
     CU(cudaMalloc(&P.v, cap * sizeof(T)));
     CU(cudaMalloc(&P.w, cap * sizeof(T)));
     if (ctx->cfg.flags & IPIC3D_F_TRACK_IDS) CU(cudaMalloc(&P.id, cap * sizeof(uint32_t)));
-    CU(cudaMalloc(&P.start, (nc + 1) * sizeof(int64_t)));
-    CU(cudaMalloc(&P.count, nc * sizeof(int32_t)));
+    // padded: the FP32 push bulk-copies aligned slices of start[] / count[]
+    // that may reach up to 3 entries past the last cell
+    CU(cudaMalloc(&P.start, (nc + 4) * sizeof(int64_t)));
+    CU(cudaMalloc(&P.count, (nc + 4) * sizeof(int32_t)));
+    CU(cudaMemsetAsync(P.start, 0, (nc + 4) * sizeof(int64_t), ctx->stream));
+    CU(cudaMemsetAsync(P.count, 0, (nc + 4) * sizeof(int32_t), ctx->stream));
     CU(cudaMalloc(&P.hole_cnt, nc * sizeof(int32_t)));
     CU(cudaMalloc(&P.arr_cnt, nc * sizeof(int32_t)));
     CU(cudaMalloc(&P.hole_list, cap * sizeof(int32_t)));
@@ -786,6 +794,7 @@ int after_steps(ipic3d_ctx* ctx, bool force_relayout = false) {
         total.migrated += c.migrated;
         total.injected += c.injected;
         total.lost += c.lost;
+        total.timeouts += c.timeouts;
         total.pending_out += c.pending_out;
         pending += pin;
     };
@@ -806,6 +815,8 @@ int after_steps(ipic3d_ctx* ctx, bool force_relayout = false) {
     ctx->last = total;
     ctx->pending_last = pending;
     if (total.lost) return fail(IPIC3D_E_CAPACITY, "%u particles lost: pending list full", total.lost);
+    if (total.timeouts)
+        return fail(IPIC3D_E_TIMEOUT, "%u thread blocks gave up waiting for a bulk copy", total.timeouts);
     // waiting particles are pushed and placed again every step (a cheap
     // path); re-lay out once they exceed 0.5% of the particles (or `force`)
     if (pending > std::max<uint64_t>(64, ctx->particles_hint / 200) || (pending && force_relayout))
@@ -884,6 +895,10 @@ int create_impl(const ipic3d_props* props, const ipic3d_config* cfg, cudaStream_
     if (!(prop.major == 10 && prop.minor == 3))
         return fail(IPIC3D_E_NODEVICE, "device %d is sm_%d%d; this library is built for sm_103a only", dev,
                     prop.major, prop.minor);
+    {
+        const cudaError_t e = init_push32(dev);
+        if (e != cudaSuccess) return fail(IPIC3D_E_CUDA, "push kernel set-up: %s", cudaGetErrorString(e));
+    }
     auto* ctx = new (std::nothrow) ipic3d_ctx();
     if (!ctx) return fail(IPIC3D_E_NOMEM, "host allocation");
     ctx->props = *props;

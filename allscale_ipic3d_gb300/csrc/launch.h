@@ -44,6 +44,7 @@ template <typename T>
 int launch_batch_status(const PopJob<T>* jobs, int njobs, JobStatus* out, cudaStream_t st);
 int launch_cell_coef_batch(const InstJob* inst, int ninst, int64_t max_cells, cudaStream_t st);  // particles_fp32.cu
 Push32Const push32_const(const Geom& g, const Pop<float>& P);                                    // particles_fp32.cu
+cudaError_t init_push32(int dev);  // once per device, before any capture (particles_fp32.cu)
 int launch_ghost_batch(const InstJob* jobs, int ninst, int max_s, cudaStream_t st);              // fields.cu
 int launch_leapfrog_batch(const InstJob* jobs, int ninst, int max_s, bool refresh_node_b, cudaStream_t st);
 int launch_forward_batch(const InstJob* jobs, int ninst, int max_s, cudaStream_t st);

@@ -1,9 +1,80 @@
 // FP32 particle kernels: positions relative to the cell origin, FP32 push
 // with fused multiply-adds, FP64 node accumulation of the deposit.
+#include <mutex>
+
 #include "particles_impl.cuh"
 #include "push32.cuh"
+#include "push32_pipe.cuh"
 
 namespace ipg {
+
+namespace {
+constexpr int kMaxDevices = 64;
+constexpr int kPipeStages = 2;  // shared-memory stages per CTA (2 CTAs per SM)
+std::mutex g_pipe_mu;
+bool g_pipe_ready[kMaxDevices] = {};
+int g_pipe_grid[kMaxDevices] = {};  // persistent CTAs of the pipelined push
+
+using PipeFn = void (*)(Geom, Pop<float>, Push32Const, int);
+
+// The compile-time policies that are instantiated (kPipe* bit sets): the
+// step with the dipole mover, the field-gather mover with or without the
+// dipole term, each with or without the deposit; and the deposit alone.
+constexpr int kPipeVariants[] = {
+    kPipeStep | kPipeDipole,
+    kPipeStep | kPipeDipole | kPipeDeposit,
+    kPipeStep | kPipeGather,
+    kPipeStep | kPipeGather | kPipeDeposit,
+    kPipeStep | kPipeGather | kPipeDipole,
+    kPipeStep | kPipeGather | kPipeDipole | kPipeDeposit,
+    kPipeDeposit,
+};
+
+template <int kF>
+constexpr PipeFn pipe_fn() {
+    return k_push32_pipe<kPipeStages, 2, kF>;
+}
+
+PipeFn pipe_kernel(int f) {
+    switch (f) {
+        case kPipeStep | kPipeDipole: return pipe_fn<kPipeStep | kPipeDipole>();
+        case kPipeStep | kPipeDipole | kPipeDeposit: return pipe_fn<kPipeStep | kPipeDipole | kPipeDeposit>();
+        case kPipeStep | kPipeGather: return pipe_fn<kPipeStep | kPipeGather>();
+        case kPipeStep | kPipeGather | kPipeDeposit: return pipe_fn<kPipeStep | kPipeGather | kPipeDeposit>();
+        case kPipeStep | kPipeGather | kPipeDipole: return pipe_fn<kPipeStep | kPipeGather | kPipeDipole>();
+        case kPipeStep | kPipeGather | kPipeDipole | kPipeDeposit:
+            return pipe_fn<kPipeStep | kPipeGather | kPipeDipole | kPipeDeposit>();
+        case kPipeDeposit: return pipe_fn<kPipeDeposit>();
+        default: return nullptr;
+    }
+}
+}  // namespace
+
+// Once per device (the device current): shared-memory opt-in and persistent
+// grid size of the pipelined push kernels. Called when a context is created,
+// before any stream capture.
+cudaError_t init_push32(int dev) {
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_pipe_mu);
+    if (g_pipe_ready[dev]) return cudaSuccess;
+    const int bytes = (int)pipe_smem_bytes<kPipeStages>();
+    int min_per_sm = 1 << 30;
+    for (int f : kPipeVariants) {
+        PipeFn fn = pipe_kernel(f);
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) return e;
+        int per_sm = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kPipeThreads, bytes);
+        if (e != cudaSuccess) return e;
+        if (per_sm < min_per_sm) min_per_sm = per_sm;
+    }
+    int sms = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    g_pipe_grid[dev] = (min_per_sm > 0 ? min_per_sm : 1) * sms;
+    g_pipe_ready[dev] = true;
+    return cudaSuccess;
+}
 
 Push32Const push32_const(const Geom& g, const Pop<float>& P) {
     Push32Const pc;
@@ -23,12 +94,28 @@ Push32Const push32_const(const Geom& g, const Pop<float>& P) {
     return pc;
 }
 
-// the FP32 step uses the lean kernels of push32.cuh
+// the FP32 step: the pipelined persistent push (push32_pipe.cuh), the
+// instance of the step's policies
 template <>
 int launch_push<float>(const Geom& g, const Pop<float>& P, int mode, cudaStream_t st) {
     if (P.capacity <= 0) return 0;
-    const int64_t blocks = (P.capacity + kSlotsPerCta - 1) / kSlotsPerCta;
-    k_push32<3><<<(unsigned)blocks, kPushThreads, 0, st>>>(g, P, push32_const(g, P), mode);
+    int f = g.deposit ? kPipeDeposit : 0;
+    if (mode == 0) {
+        f |= kPipeStep;
+        if (g.mover == 1) f |= kPipeGather;
+        if (g.mover != 1 || (g.flags & 4u)) f |= kPipeDipole;
+    } else if (!g.deposit) {
+        return 0;  // nothing to deposit
+    }
+    PipeFn fn = pipe_kernel(f);
+    if (!fn) return 0;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int64_t tiles = (P.capacity + kTileSlots - 1) / kTileSlots;
+    int grid = g_pipe_grid[dev];
+    if (grid <= 0) grid = 1;  // init_push32 did not run on this device: the launch fails (no shared-memory opt-in)
+    if (grid > tiles) grid = (int)tiles;
+    fn<<<grid, kPipeThreads, pipe_smem_bytes<kPipeStages>(), st>>>(g, P, push32_const(g, P), (int)tiles);
     return 1;
 }
 

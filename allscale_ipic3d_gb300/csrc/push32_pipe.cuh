@@ -1,0 +1,755 @@
+// The FP32 push as a persistent, warp-specialised, TMA-pipelined kernel.
+//
+// Each CTA has one producer warp and eight compute warps. The producer's
+// elected lane streams 1024-slot tiles of a population through a ring of
+// shared-memory stages with bulk copies (cp.async.bulk, completion counted
+// on the stage's `full` mbarrier): x y z u v w of the tile's slots and the
+// tile's slice of the cell tables start[] / count[]. The compute warps push
+// the particles of a stage in shared memory and release it on its `empty`
+// mbarrier; the producer then writes the stage back in place with bulk
+// stores and refills it with the tile after next. No compute thread loads or
+// stores particle state in global memory and no CTA-wide barrier separates
+// the warps: a warp waits only for the data it works on.
+//
+// Work inside a tile. A tile whose cells are large (at most 32 cells) is cut
+// into items: the occupied slots of one cell, at most 128 at a time. Warps
+// take items from a per-stage counter; lane l pushes the item's particles
+// l, l + 32, ... and adds their cloud-in-cell moments to its accumulators,
+// so a warp sums one cell and flushes it once (transpose-reduction across
+// the lanes). A tile of many small cells goes thread-per-4-slots instead:
+// warp w pushes slots [128 w, 128 w + 128) and flushes its per-cell runs of
+// lanes through a shared-memory tile.
+//
+// Per particle the physics is step32's (push32.cuh): field gather from the
+// cell's trilinear polynomial and/or the analytic dipole, the reference's
+// sub-cycled Boris mover (particle.h:31-49, cell.h:896-964) and the export
+// classification (cell.h:1093-1146), with the wall logic skipped for cells
+// that touch no reflecting or open face.
+//
+// Deposit of the stayers (cell.h:787-824 in scatter form): the monomial
+// moments of the particles about the cell centre, Q m(r - 1/2) for Q in
+// {u, v, w, 1} and m in {1, x, y, xy, z, xz, yz, xyz} (moment index = bits
+// x|y<<1|z<<2), are summed per cell; lane v then owns value v = 8 Q + m and
+// three butterflies (one per axis: (a, b) -> (a/2 - b, a/2 + b)) turn the
+// moments into the sums of the cloud-in-cell weights (1 - r, r) per corner:
+// one FP64 atomic per lane adds corner m's component Q to its node. Centred
+// moments keep the FP32 sums small, so the butterflies' cancellation loses
+// no more than the sums' own rounding.
+//
+// Every wait on an mbarrier is bounded (kWaitCycles): on expiry the CTA
+// records a timeout in the population's counters, drains its own copies and
+// returns; the host turns the count into IPIC3D_E_TIMEOUT.
+#pragma once
+
+#include <cstddef>
+
+#include "push32.cuh"
+
+namespace ipg {
+
+// ---- bulk copy / mbarrier primitives (sm_90+ PTX) ---------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ uint32_t mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok;
+}
+// ~1 s at the GB300's 2.07 GHz: far beyond any copy's latency
+constexpr long long kWaitCycles = 2000000000LL;
+// Waits for the phase of `bar` with parity `parity`; false after kWaitCycles
+// (or 2^26 polls), or as soon as *abort is set.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const volatile int* abort) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    for (uint32_t it = 0; it < (1u << 26); ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (*abort || clock64() - t0 > kWaitCycles) break;
+    }
+    return false;
+}
+// global -> shared, `bytes` (multiple of 16, both addresses 16-byte aligned)
+__device__ __forceinline__ void bulk_load(void* smem_dst, const void* gsrc, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(smem_dst)),
+                 "l"(gsrc), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+// shared -> global, same rules
+__device__ __forceinline__ void bulk_store(void* gdst, const void* smem_src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst), "r"(smem_u32(smem_src)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// the shared-memory sources of all committed bulk stores have been read
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// all committed bulk stores are complete
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// orders this thread's generic-proxy shared-memory accesses before later
+// async-proxy (bulk copy) accesses
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// ---- shared-memory layout ------------------------------------------------------
+constexpr int kTileSlots = kSlotsPerCta;  // 1024 slots per tile (the cta_cells table's unit)
+constexpr int kComputeWarps = 8;
+constexpr int kComputeThreads = kComputeWarps * 32;
+constexpr int kPipeThreads = kComputeThreads + 32;  // + the producer warp
+constexpr int kItemSlots = 256;                     // particles per item (8 per lane)
+static_assert(kTileSlots == 4 * kComputeThreads, "slot mode: 4 slots per compute thread");
+
+constexpr int kItemMaxCells = 32;  // tiles of at most this many cells run in item mode
+
+// Every member is a bulk-copy destination: 16-byte aligned offsets.
+struct __align__(16) PipeStage {
+    alignas(16) float s[6][kTileSlots];              // x y z u v w of the tile's slots
+    alignas(16) float coef[kItemMaxCells * 48];      // item mode + field gather: cellcoef of the tile's cells
+    alignas(16) int64_t start[kMaxCellsPerCta + 4];  // start[(c0 & ~1) ...]
+    alignas(16) int32_t count[kMaxCellsPerCta + 8];  // count[(c0 & ~3) ...]
+};
+static_assert(offsetof(PipeStage, coef) % 16 == 0 && offsetof(PipeStage, start) % 16 == 0 &&
+                  offsetof(PipeStage, count) % 16 == 0 && sizeof(PipeStage) % 16 == 0,
+              "bulk copies need 16-byte aligned shared-memory destinations");
+
+template <int kStages>
+struct PipeSmem {
+    PipeStage stage[kStages];
+    alignas(16) float flush[kComputeWarps][32 * 36];  // per-warp deposit tile (warp_column_sum)
+    uint64_t full[kStages];               // the stage's copies landed
+    uint64_t empty[kStages];              // the compute warps are done with the stage
+    int2 desc[kStages];                   // (first cell, number of cells) of the stage's tile
+    int next_item[kStages];               // item counter of the stage's tile
+    int abort;                            // a wait expired: every warp stops
+};
+
+static_assert(offsetof(PipeSmem<2>, stage) == 0 && offsetof(PipeSmem<3>, stage) == 0, "stages first");
+
+template <int kStages>
+constexpr size_t pipe_smem_bytes() {
+    return sizeof(PipeSmem<kStages>);
+}
+
+// Bulk-copy sizes of one tile (all multiples of 16 bytes; every source
+// 16-byte aligned: slot bases are multiples of 1024, the cell tables are
+// read from an even / multiple-of-4 index and allocated with padding).
+struct TileCopy {
+    int64_t base;
+    uint32_t slot_bytes;   // per array
+    int64_t s_first;       // first start[] entry copied
+    uint32_t s_bytes;
+    int64_t c_first;       // first count[] entry copied
+    uint32_t c_bytes;
+};
+
+__device__ __forceinline__ TileCopy tile_copy(const Pop<float>& P, int tile, int2 desc) {
+    TileCopy t;
+    t.base = (int64_t)tile * kTileSlots;
+    const int64_t n = P.capacity - t.base < kTileSlots ? P.capacity - t.base : kTileSlots;
+    t.slot_bytes = (uint32_t)(n * 4);
+    t.s_first = desc.x & ~1;
+    const int64_t ns = ((int64_t)desc.x + desc.y + 1 - t.s_first + 1) & ~int64_t(1);
+    t.s_bytes = (uint32_t)(ns * 8);
+    t.c_first = desc.x & ~3;
+    const int64_t ncnt = ((int64_t)desc.x + desc.y - t.c_first + 3) & ~int64_t(3);
+    t.c_bytes = (uint32_t)(ncnt * 4);
+    return t;
+}
+
+// Issued by the producer: the tile's copies into `st`, counted on `bar`;
+// with `coef` (item mode, field gather) also the cells' field coefficients
+// (48 floats = 192 bytes per cell, contiguous from cell c0).
+__device__ __forceinline__ void issue_tile(const Pop<float>& P, const float* coef, int tile, int2 desc,
+                                           PipeStage& st, uint64_t* bar) {
+    const TileCopy t = tile_copy(P, tile, desc);
+    const bool with_coef = coef != nullptr && desc.y <= kItemMaxCells;
+    const uint32_t coef_bytes = with_coef ? (uint32_t)desc.y * 192u : 0u;
+    mbar_arrive_expect_tx(bar, 6u * t.slot_bytes + t.s_bytes + t.c_bytes + coef_bytes);
+    float* const arr[6] = {P.x, P.y, P.z, P.u, P.v, P.w};
+#pragma unroll
+    for (int a = 0; a < 6; ++a) bulk_load(st.s[a], arr[a] + t.base, t.slot_bytes, bar);
+    bulk_load(st.start, P.start + t.s_first, t.s_bytes, bar);
+    bulk_load(st.count, P.count + t.c_first, t.c_bytes, bar);
+    if (coef_bytes) bulk_load(st.coef, coef + (size_t)desc.x * 48, coef_bytes, bar);
+}
+
+// 16-byte load from shared memory (p is a generic address of shared memory).
+__device__ __forceinline__ float4 ld_shared_f4(const float* p) {
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(smem_u32(p)));
+    return v;
+}
+
+// eval_fields (push32.cuh) with the coefficients in shared memory.
+__device__ __forceinline__ void eval_fields_smem(const float* coef, float x, float y, float z, float (&f)[6]) {
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        const float4 lo = ld_shared_f4(coef + 8 * q), hi = ld_shared_f4(coef + 8 * q + 4);
+        const float a = fmaf(y, hi.w, hi.y);
+        float b = fmaf(y, hi.x, lo.y);
+        b = fmaf(z, a, b);
+        const float gz = fmaf(z, hi.z, lo.z);
+        float r = fmaf(y, gz, lo.x);
+        r = fmaf(z, lo.w, r);
+        f[q] = fmaf(x, b, r);
+    }
+}
+
+// Compile-time policy of one pipelined push launch (template bit set).
+enum : int {
+    kPipeStep = 1,     // mover + export (else: deposit of the particles as they are)
+    kPipeGather = 2,   // field-gather mover: E, B from the cell's polynomial
+    kPipeDipole = 4,   // analytic dipole B added
+    kPipeDeposit = 8,  // cloud-in-cell deposit of J and rho
+};
+
+struct CellInfo {
+    int cx, cy, cz;
+    float ox, oy, oz;
+    bool edge;  // a face of this cell lies on a reflecting or open domain face
+};
+
+__device__ __forceinline__ CellInfo cell_info(const Geom& g, const Push32Const& pc, int cell) {
+    CellInfo c;
+    if (g.ncells < (1 << 24) && g.sy < 4096 && g.sz < 4096) {
+        const int t = fast_div(cell, g.sz, pc.inv_sz);
+        c.cz = cell - t * g.sz;
+        c.cx = fast_div(t, g.sy, pc.inv_sy);
+        c.cy = t - c.cx * g.sy;
+    } else {
+        cell_coords(g, cell, c.cx, c.cy, c.cz);
+    }
+    c.ox = fmaf((float)c.cx, pc.w[0], pc.origin[0]);
+    c.oy = fmaf((float)c.cy, pc.w[1], pc.origin[1]);
+    c.oz = fmaf((float)c.cz, pc.w[2], pc.origin[2]);
+    c.edge = (c.cx == 0 && g.bc_lo[0] != 1) || (c.cx == g.sx - 1 && g.bc_hi[0] != 1) ||
+             (c.cy == 0 && g.bc_lo[1] != 1) || (c.cy == g.sy - 1 && g.bc_hi[1] != 1) ||
+             (c.cz == 0 && g.bc_lo[2] != 1) || (c.cz == g.sz - 1 && g.bc_hi[2] != 1);
+    return c;
+}
+
+// Mover + export of one particle (FP32, cell-relative), the physics of
+// step32 (push32.cuh) specialised at compile time: kGather / kDipole select
+// the field terms, kSmemCoef says where the coefficients are. The wall logic
+// runs only for cells on a reflecting or open face; the rotation factor
+// 2 / (1 + |t|^2) comes from the hardware reciprocal plus one Newton-Raphson
+// step (r + r (1 - d r)). A leaver's move is returned in `dir` as
+// (dx + 1) | (dy + 1) << 2 | (dz + 1) << 4.
+template <bool kSmemCoef, bool kGather, bool kDipole>
+__device__ __forceinline__ int step32f(const Geom& g, const Push32Const& pc, const float* __restrict__ coef,
+                                       const CellInfo& ci, PState<float>& p, int& dir) {
+    float E[6];
+    if (kGather) {
+        if (kSmemCoef)
+            eval_fields_smem(coef, p.x, p.y, p.z, E);
+        else
+            eval_fields(coef, p.x, p.y, p.z, E);
+    } else {
+#pragma unroll
+        for (int q = 0; q < 6; ++q) E[q] = 0.f;
+    }
+    if (kDipole) {
+        const float X = fmaf(p.x, pc.w[0], ci.ox), Y = fmaf(p.y, pc.w[1], ci.oy), Z = fmaf(p.z, pc.w[2], ci.oz);
+        const float r2 = fmaf(X, X, fmaf(Y, Y, Z * Z));
+        const float ir = rsqrtf(r2), ir2 = ir * ir;
+        const float fac1 = pc.mft * (ir2 * ir2 * ir);
+        E[3] = fmaf(3.f * X * Z, fac1, E[3]);
+        E[4] = fmaf(3.f * Y * Z, fac1, E[4]);
+        E[5] = fmaf(fmaf(2.f * Z, Z, -fmaf(X, X, Y * Y)), fac1, E[5]);
+    }
+    const float bmag = fmaf(E[3], E[3], fmaf(E[4], E[4], E[5] * E[5]));
+    const float ratio = pc.k_sub * bmag;  // >= 0 or NaN
+    // cell.h:947-952; a quotient beyond the int range (or NaN) leaves the
+    // particle unmoved, as the reference's x86 conversion does
+    int ns = 0;
+    if (ratio < 2147483647.f) {
+        ns = (int)ratio + 1;
+        ns = ns < 100 ? ns : 100;
+    }
+    if (ns > 0) {
+        const float dts = ns == 1 ? pc.dt : __fdividef(pc.dt, (float)ns);
+        const float k = pc.qom * 0.5f * dts;
+        const float tx = k * E[3], ty = k * E[4], tz = k * E[5];
+        const float den = fmaf(tx, tx, fmaf(ty, ty, fmaf(tz, tz, 1.f)));
+        float inv = __fdividef(1.f, den);
+        inv = fmaf(inv, fmaf(-den, inv, 1.f), inv);
+        const float inv2 = 2.f * inv;
+        const float sx = tx * inv2, sy = ty * inv2, sz = tz * inv2;
+        const float kex = k * E[0], key = k * E[1], kez = k * E[2];
+        const float ax = dts * pc.inv_w[0], ay = dts * pc.inv_w[1], az = dts * pc.inv_w[2];
+        int s = 0;
+        do {
+            const float mx = p.u + kex, my = p.v + key, mz = p.w + kez;
+            const float px = mx + (my * tz - mz * ty);
+            const float py = my + (mz * tx - mx * tz);
+            const float pz = mz + (mx * ty - my * tx);
+            p.u = mx + (py * sz - pz * sy) + kex;
+            p.v = my + (pz * sx - px * sz) + key;
+            p.w = mz + (px * sy - py * sx) + kez;
+            p.x = fmaf(p.u, ax, p.x);
+            p.y = fmaf(p.v, ay, p.y);
+            p.z = fmaf(p.w, az, p.z);
+        } while (++s < ns);
+    }
+    float R[3] = {p.x, p.y, p.z};
+    if (ci.edge) {
+        const int pos[3] = {ci.cx, ci.cy, ci.cz};
+        const int size[3] = {g.sx, g.sy, g.sz};
+        bool invert = false, drop = false;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            if (pos[a] == 0 && R[a] < 0.f) {
+                if (g.bc_lo[a] == 0) { invert = true; R[a] += 0.5f; }
+                else if (g.bc_lo[a] == 2) drop = true;
+            } else if (pos[a] == size[a] - 1 && R[a] > 1.f) {
+                if (g.bc_hi[a] == 0) { invert = true; R[a] -= 0.5f; }
+                else if (g.bc_hi[a] == 2) drop = true;
+            }
+        }
+        if (invert) { p.u = -p.u; p.v = -p.v; p.w = -p.w; }
+        if (drop) return kDrop;
+    }
+    {
+        const float dx = fmaf(R[0], pc.w[0], ci.ox - pc.center[0]);
+        const float dy = fmaf(R[1], pc.w[1], ci.oy - pc.center[1]);
+        const float dz = fmaf(R[2], pc.w[2], ci.oz - pc.center[2]);
+        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= pc.planet_r2) return kDrop;  // cell.h:1123-1128
+    }
+    const float fx = R[0] < 0.f ? -1.f : (R[0] > 1.f ? 1.f : 0.f);
+    const float fy = R[1] < 0.f ? -1.f : (R[1] > 1.f ? 1.f : 0.f);
+    const float fz = R[2] < 0.f ? -1.f : (R[2] > 1.f ? 1.f : 0.f);
+    p.x = R[0] - fx;
+    p.y = R[1] - fy;
+    p.z = R[2] - fz;
+    if (fx == 0.f && fy == 0.f && fz == 0.f) return kStay;
+    dir = ((int)fx + 1) | (((int)fy + 1) << 2) | (((int)fz + 1) << 4);
+    return kMove;
+}
+
+// FP64 atomic of corner m (bits x|y<<1|z<<2) and component q (0-2 J, 3 rho)
+// of the cell at (cx, cy, cz).
+__device__ __forceinline__ void corner_atomic_add(const Geom& g, int cx, int cy, int cz, int m, int q, double val) {
+    const int64_t n = node_index(g, cx + (m & 1), cy + ((m >> 1) & 1), cz + (m >> 2));
+    if (q < 3)
+        atomicAdd(g.J + 3 * n + q, val);
+    else
+        atomicAdd(g.rho + n, val);
+}
+
+// Cloud-in-cell deposit of the warp's leavers (ballot `lb`) into their
+// destination cells, one leaver at a time: lane l adds component l >> 3 at
+// corner l & 7 -- one 32-lane atomic per leaver.
+__device__ __forceinline__ void deposit_leavers32(const Geom& g, unsigned lb, int nx, int ny, int nz,
+                                                  const PState<float>& p, double q) {
+    const int lane = threadIdx.x & 31, m = lane & 7, comp = lane >> 3;
+    while (lb) {
+        const int src = __ffs(lb) - 1;
+        lb &= lb - 1;
+        const int cx = __shfl_sync(0xffffffffu, nx, src), cy = __shfl_sync(0xffffffffu, ny, src),
+                  cz = __shfl_sync(0xffffffffu, nz, src);
+        const float x = __shfl_sync(0xffffffffu, p.x, src), y = __shfl_sync(0xffffffffu, p.y, src),
+                    z = __shfl_sync(0xffffffffu, p.z, src);
+        const float u = __shfl_sync(0xffffffffu, p.u, src), v = __shfl_sync(0xffffffffu, p.v, src),
+                    w = __shfl_sync(0xffffffffu, p.w, src);
+        const float wt = ((m & 1) ? x : 1.f - x) * ((m & 2) ? y : 1.f - y) * ((m & 4) ? z : 1.f - z);
+        const float Q = comp == 0 ? u : (comp == 1 ? v : (comp == 2 ? w : 1.f));
+        const double val = (double)(Q * wt) * q;
+        if (val != 0.0) corner_atomic_add(g, cx, cy, cz, m, comp, val);
+    }
+}
+
+// Adds the centred cloud-in-cell moments of a stayer to acc (index 8 Q + m).
+__device__ __forceinline__ void add_moments(float (&acc)[32], const PState<float>& p) {
+    const float x = p.x - 0.5f, y = p.y - 0.5f, z = p.z - 0.5f;
+    const float xy = x * y, xz = x * z, yz = y * z, xyz = xy * z;
+    const float Q[3] = {p.u, p.v, p.w};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        acc[q * 8 + 0] += Q[q];
+        acc[q * 8 + 1] = fmaf(Q[q], x, acc[q * 8 + 1]);
+        acc[q * 8 + 2] = fmaf(Q[q], y, acc[q * 8 + 2]);
+        acc[q * 8 + 3] = fmaf(Q[q], xy, acc[q * 8 + 3]);
+        acc[q * 8 + 4] = fmaf(Q[q], z, acc[q * 8 + 4]);
+        acc[q * 8 + 5] = fmaf(Q[q], xz, acc[q * 8 + 5]);
+        acc[q * 8 + 6] = fmaf(Q[q], yz, acc[q * 8 + 6]);
+        acc[q * 8 + 7] = fmaf(Q[q], xyz, acc[q * 8 + 7]);
+    }
+    acc[24] += 1.f;
+    acc[25] += x;
+    acc[26] += y;
+    acc[27] += xy;
+    acc[28] += z;
+    acc[29] += xz;
+    acc[30] += yz;
+    acc[31] += xyz;
+}
+
+// Lane v holds the summed moment v = 8 Q + m of one cell: the three axis
+// butterflies give the cloud-in-cell corner sum of corner m, component Q;
+// one FP64 atomic adds it (times the charge) to the node.
+__device__ __forceinline__ void emit_corner_sums(const Geom& g, float s, int cx, int cy, int cz, double q) {
+    const int lane = threadIdx.x & 31, m = lane & 7;
+#pragma unroll
+    for (int bit = 1; bit < 8; bit <<= 1) {
+        const float o = __shfl_xor_sync(0xffffffffu, s, bit);
+        s = (m & bit) ? fmaf(0.5f, o, s) : fmaf(0.5f, s, -o);
+    }
+    if (s != 0.f) corner_atomic_add(g, cx, cy, cz, m, lane >> 3, (double)s * q);
+}
+
+// Leaver bookkeeping of one warp step: outbox (one warp-aggregated append),
+// arrival list of the destination, cooperative deposit; the old slot is
+// filed as a hole of its cell (leavers and drops). `dir` is step32f's move.
+__device__ __forceinline__ void leave_and_hole(const Geom& g, const Pop<float>& P, int outcome, int dir,
+                                               const CellInfo& ci, const PState<float>& p, int slot, int cell,
+                                               int cstart, bool deposit, uint32_t& nmig, uint32_t& nrem) {
+    const int lane = threadIdx.x & 31;
+    const bool leave = outcome == kMove;
+    const unsigned lb = __ballot_sync(0xffffffffu, leave);
+    if (lb) {
+        // destination cell (periodic wrap of the index, as the outbox expects)
+        int nx = ci.cx + (dir & 3) - 1, ny = ci.cy + ((dir >> 2) & 3) - 1, nz = ci.cz + ((dir >> 4) & 3) - 1;
+        nx = nx < 0 ? nx + g.sx : (nx >= g.sx ? nx - g.sx : nx);
+        ny = ny < 0 ? ny + g.sy : (ny >= g.sy ? ny - g.sy : ny);
+        nz = nz < 0 ? nz + g.sz : (nz >= g.sz ? nz - g.sz : nz);
+        const int leader = __ffs(lb) - 1;
+        uint32_t o = 0;
+        if (lane == leader) o = atomicAdd(&P.ctr->outbox, (uint32_t)__popc(lb));
+        o = __shfl_sync(0xffffffffu, o, leader) + __popc(lb & ((1u << lane) - 1u));
+        if (leave) {
+            Mover<float> m;
+            m.cell = cell_id(g, nx, ny, nz);
+            m.id = P.id ? P.id[slot] : 0u;
+            m.x = p.x; m.y = p.y; m.z = p.z;
+            m.u = p.u; m.v = p.v; m.w = p.w;
+            if (o < P.outbox_cap) {
+                P.outbox[o] = m;
+                register_arrival(P, o, m);
+            } else {
+                atomicAdd(&P.ctr->lost, 1u);
+            }
+            ++nmig;
+        }
+        if (deposit) deposit_leavers32(g, lb, nx, ny, nz, p, P.q);
+    }
+    if (outcome == kMove || outcome == kDrop) {
+        const int k = atomicAdd(P.hole_cnt + cell, 1);
+        P.hole_list[cstart + k] = slot;
+        if (outcome == kDrop) ++nrem;
+    }
+}
+
+// Sum over the warp's lanes of acc[v] into lane v, through the warp's
+// shared-memory tile: row t (lane t's 32 values) at [36 t], written with
+// 128-bit stores; lane v reads column v (36 = 4 mod 32: no bank conflicts
+// either way).
+constexpr int kFlushStride = 36;
+__device__ __forceinline__ float warp_column_sum(const float (&acc)[32], float* flush_tile) {
+    const int lane = threadIdx.x & 31;
+    float4* row = reinterpret_cast<float4*>(flush_tile + lane * kFlushStride);
+#pragma unroll
+    for (int v = 0; v < 8; ++v) row[v] = make_float4(acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
+    __syncwarp();
+    float s = 0.f;
+#pragma unroll
+    for (int t = 0; t < 32; ++t) s += flush_tile[t * kFlushStride + lane];
+    __syncwarp();
+    return s;
+}
+
+// Item mode: the warp pushes particles [a, b) (tile-local slots, b - a <=
+// kItemSlots) of cell `cell`, lane l taking a + l, a + l + 32, ...; stayers
+// go back to HBM with coalesced stores, the cell's moments are flushed once.
+// `coef` points at the cell's 48 field coefficients (shared memory).
+template <int kF>
+__device__ __forceinline__ void push_item(const Geom& g, const Pop<float>& P, const Push32Const& pc,
+                                          const PipeStage& st, const float* coef, int base, int cell, int cstart,
+                                          int a, int b, float* flush_tile, uint32_t& nmig, uint32_t& nrem) {
+    constexpr bool kStep = (kF & kPipeStep) != 0, kDep = (kF & kPipeDeposit) != 0;
+    const int lane = threadIdx.x & 31;
+    const CellInfo ci = cell_info(g, pc, cell);
+    float acc[32];
+#pragma unroll
+    for (int l = 0; l < 32; ++l) acc[l] = 0.f;
+#pragma unroll 1
+    for (int s0 = a; s0 < b; s0 += 32) {
+        const int sl = s0 + lane;
+        PState<float> p;
+        int outcome = -1, dir = 0;
+        if (sl < b) {
+            p.x = st.s[0][sl]; p.y = st.s[1][sl]; p.z = st.s[2][sl];
+            p.u = st.s[3][sl]; p.v = st.s[4][sl]; p.w = st.s[5][sl];
+            outcome = kStep ? step32f<true, (kF & kPipeGather) != 0, (kF & kPipeDipole) != 0>(g, pc, coef, ci, p, dir)
+                            : kStay;
+            if (outcome == kStay) {
+                if (kStep) {
+                    const int gs = base + sl;
+                    P.x[gs] = p.x; P.y[gs] = p.y; P.z[gs] = p.z;
+                    P.u[gs] = p.u; P.v[gs] = p.v; P.w[gs] = p.w;
+                }
+                if (kDep) add_moments(acc, p);
+            }
+        }
+        if (kStep) leave_and_hole(g, P, outcome, dir, ci, p, base + sl, cell, cstart, kDep, nmig, nrem);
+    }
+    if (kDep) emit_corner_sums(g, warp_column_sum(acc, flush_tile), ci.cx, ci.cy, ci.cz, P.q);
+}
+
+// Slot mode: warp w pushes slots [128 w, 128 w + 128) of the tile, thread t
+// the 4 slots from 4 t (one cell: capacities are multiples of 8), and flushes
+// per run of lanes of one cell.
+template <int kF>
+__device__ __forceinline__ void push_slots(const Geom& g, const Pop<float>& P, const Push32Const& pc,
+                                           PipeStage& st, int base, int2 desc, float* flush_tile, uint32_t& nmig,
+                                           uint32_t& nrem) {
+    constexpr bool kStep = (kF & kPipeStep) != 0, kDep = (kF & kPipeDeposit) != 0;
+    constexpr int kPer = 4;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int c0 = desc.x, nc = desc.y;
+    const int64_t* S = st.start + (c0 & 1);  // S[i] = start[c0 + i]
+    const int32_t* N = st.count + (c0 & 3);  // N[i] = count[c0 + i]
+    const int s0 = base + tid * kPer;
+    int lc = 0;
+    {
+        int lo = 0, hi = nc - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (S[mid] <= s0) lo = mid; else hi = mid - 1;
+        }
+        lc = lo;
+    }
+    const int cell = c0 + lc;
+    const int cstart = (int)S[lc];
+    int nv = 0;
+    if (s0 < P.capacity) {
+        const int e = cstart + N[lc] - s0;
+        nv = e <= 0 ? 0 : (e >= kPer ? kPer : e);
+    }
+    const CellInfo ci = cell_info(g, pc, cell);
+    const float* coef = g.cellcoef + (size_t)cell * 48;
+    float acc[32];
+#pragma unroll
+    for (int l = 0; l < 32; ++l) acc[l] = 0.f;
+    bool has_acc = false;
+    // lane groups start at different slots of their run of 4: the words a
+    // warp reads in one step fall in 32 different banks
+    const int rot = lane >> 3;
+    const int sl0 = tid * kPer;
+#pragma unroll 1
+    for (int jj = 0; jj < kPer; ++jj) {
+        const int j = (jj + rot) & (kPer - 1);
+        const int sl = sl0 + j;
+        PState<float> p;
+        int outcome = -1, dir = 0;
+        if (j < nv) {
+            p.x = st.s[0][sl]; p.y = st.s[1][sl]; p.z = st.s[2][sl];
+            p.u = st.s[3][sl]; p.v = st.s[4][sl]; p.w = st.s[5][sl];
+            outcome = kStep ? step32f<false, (kF & kPipeGather) != 0, (kF & kPipeDipole) != 0>(g, pc, coef, ci, p, dir)
+                            : kStay;
+            if (outcome == kStay) {
+                if (kStep) {
+                    st.s[0][sl] = p.x; st.s[1][sl] = p.y; st.s[2][sl] = p.z;
+                    st.s[3][sl] = p.u; st.s[4][sl] = p.v; st.s[5][sl] = p.w;
+                }
+                if (kDep) {
+                    add_moments(acc, p);
+                    has_acc = true;
+                }
+            }
+        }
+        if (kStep) leave_and_hole(g, P, outcome, dir, ci, p, base + sl, cell, cstart, kDep, nmig, nrem);
+    }
+    if (!kDep) return;
+    float4* row = reinterpret_cast<float4*>(flush_tile + lane * kFlushStride);
+#pragma unroll
+    for (int v = 0; v < 8; ++v) row[v] = make_float4(acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
+    const unsigned todo = __ballot_sync(0xffffffffu, has_acc);
+    const int prev_cell = __shfl_up_sync(0xffffffffu, cell, 1);
+    unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev_cell != cell);
+    __syncwarp();
+    while (heads) {
+        const int a = __ffs(heads) - 1;
+        heads &= heads - 1;
+        const int b = heads ? __ffs(heads) - 1 : 32;  // run [a, b)
+        const unsigned run = (b < 32 ? (1u << b) : 0u) - (1u << a);
+        if (!(todo & run)) continue;
+        float s = 0.f;
+#pragma unroll 4
+        for (int t = a; t < b; ++t) s += flush_tile[t * kFlushStride + lane];
+        const int gx = __shfl_sync(0xffffffffu, ci.cx, a), gy = __shfl_sync(0xffffffffu, ci.cy, a),
+                  gz = __shfl_sync(0xffffffffu, ci.cz, a);
+        emit_corner_sums(g, s, gx, gy, gz, P.q);
+    }
+    __syncwarp();
+}
+
+// One compute warp's share of the tile in `st`.
+template <int kF>
+__device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& P, const Push32Const& pc, int tile,
+                                               int2 desc, PipeStage& st, int* next_item, float* flush_tile,
+                                               uint32_t& nmig, uint32_t& nrem) {
+    const int lane = threadIdx.x & 31;
+    const int base = tile * kTileSlots;
+    const int c0 = desc.x, nc = desc.y;
+    if (nc > kItemMaxCells) {
+        push_slots<kF>(g, P, pc, st, base, desc, flush_tile, nmig, nrem);
+        return;
+    }
+    // item mode: lane i describes cell c0 + i: its occupied slots [lo, hi)
+    // within the tile, its items and their exclusive prefix
+    const int64_t* S = st.start + (c0 & 1);
+    const int32_t* N = st.count + (c0 & 3);
+    int lo = 0, hi = 0, cst = 0;
+    if (lane < nc) {
+        cst = (int)S[lane];
+        const int l = cst - base, h = cst + N[lane] - base;
+        lo = l < 0 ? 0 : l;
+        hi = h > kTileSlots ? kTileSlots : h;
+    }
+    const int items = hi > lo ? (hi - lo + kItemSlots - 1) / kItemSlots : 0;
+    int incl = items;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int n = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += n;
+    }
+    const int excl = incl - items;
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    for (;;) {
+        int j = 0;
+        if (lane == 0) j = atomicAdd(next_item, 1);
+        j = __shfl_sync(0xffffffffu, j, 0);
+        if (j >= total) break;
+        const unsigned owners = __ballot_sync(0xffffffffu, items > 0 && excl <= j);
+        const int src = 31 - __clz(owners);
+        const int clo = __shfl_sync(0xffffffffu, lo, src), chi = __shfl_sync(0xffffffffu, hi, src);
+        const int cex = __shfl_sync(0xffffffffu, excl, src);
+        const int cstart = __shfl_sync(0xffffffffu, cst, src);
+        const int a = clo + (j - cex) * kItemSlots;
+        const int b = a + kItemSlots < chi ? a + kItemSlots : chi;
+        push_item<kF>(g, P, pc, st, st.coef + src * 48, base, c0 + src, cstart, a, b, flush_tile, nmig, nrem);
+    }
+}
+
+// The persistent kernel: CTA b pushes tiles b, b + G, b + 2G, ... of one
+// population (G = gridDim.x) through kStages stages.
+template <int kStages, int kMinBlocks, int kF>
+__global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
+    k_push32_pipe(Geom g, Pop<float> P, Push32Const pc, int ntiles) {
+    constexpr bool kStep = (kF & kPipeStep) != 0;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    PipeSmem<kStages>& sm = *reinterpret_cast<PipeSmem<kStages>*>(smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int G = gridDim.x;
+    if (tid == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&sm.full[s], 1);
+            mbar_init(&sm.empty[s], kComputeWarps);
+        }
+        sm.abort = 0;
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const volatile int* abort = &sm.abort;
+
+    if (warp == kComputeWarps) {
+        // ---- producer ----
+        if (lane != 0) return;
+        const float* coef = (kF & kPipeGather) ? g.cellcoef : nullptr;
+        int issued = 0;  // tiles of this CTA whose copies were issued
+        for (int s = 0; s < kStages; ++s) {
+            const int t = blockIdx.x + s * G;
+            if (t >= ntiles) break;
+            const int2 d = __ldg(P.cta_cells + t);
+            sm.desc[s] = d;
+            sm.next_item[s] = 0;
+            issue_tile(P, coef, t, d, sm.stage[s], &sm.full[s]);
+            ++issued;
+        }
+        int2 next_desc = make_int2(0, 0);
+        if (blockIdx.x + kStages * G < ntiles) next_desc = __ldg(P.cta_cells + blockIdx.x + kStages * G);
+        bool failed = false;
+        int k = 0;
+        for (int t = blockIdx.x; t < ntiles; t += G, ++k) {
+            const int s = k % kStages;
+            if (!mbar_wait(&sm.empty[s], (uint32_t)(k / kStages) & 1u, abort)) {
+                failed = true;
+                break;
+            }
+            // slot mode writes the tile back from the stage; item mode's warps
+            // stored their stayers themselves
+            const bool store = kStep && sm.desc[s].y > kItemMaxCells;
+            if (store) {
+                const TileCopy c = tile_copy(P, t, sm.desc[s]);
+                float* const arr[6] = {P.x, P.y, P.z, P.u, P.v, P.w};
+#pragma unroll
+                for (int a = 0; a < 6; ++a) bulk_store(arr[a] + c.base, sm.stage[s].s[a], c.slot_bytes);
+                bulk_commit();
+            }
+            const int tn = t + kStages * G;
+            if (tn < ntiles) {
+                if (store) bulk_wait_read_all();  // the stores have read the stage
+                const int2 d = next_desc;
+                if (tn + G < ntiles) next_desc = __ldg(P.cta_cells + tn + G);
+                sm.desc[s] = d;
+                sm.next_item[s] = 0;
+                issue_tile(P, coef, tn, d, sm.stage[s], &sm.full[s]);
+                ++issued;
+            }
+        }
+        if (failed) {
+            if (atomicExch(&sm.abort, 1) == 0) atomicAdd(&P.ctr->timeouts, 1u);
+            // copies still in flight land before the CTA leaves
+            const int never = 0;
+            for (int kk = k; kk < issued; ++kk)
+                mbar_wait(&sm.full[kk % kStages], (uint32_t)(kk / kStages) & 1u, &never);
+        }
+        bulk_wait_all();
+        return;
+    }
+
+    // ---- compute warps ----
+    float* flush_tile = sm.flush[warp];
+    uint32_t nmig = 0, nrem = 0;
+    int k = 0;
+    for (int t = blockIdx.x; t < ntiles; t += G, ++k) {
+        const int s = k % kStages;
+        // warp-uniform: every lane polls the same barrier
+        if (!__all_sync(0xffffffffu, mbar_wait(&sm.full[s], (uint32_t)(k / kStages) & 1u, abort))) {
+            if (lane == 0 && atomicExch(&sm.abort, 1) == 0) atomicAdd(&P.ctr->timeouts, 1u);
+            break;
+        }
+        push_tile_warp<kF>(g, P, pc, t, sm.desc[s], sm.stage[s], &sm.next_item[s], flush_tile, nmig, nrem);
+        fence_proxy_async_smem();  // this warp's writes to the stage, before the bulk stores read it
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.empty[s]);
+    }
+    nmig = __reduce_add_sync(0xffffffffu, nmig);
+    nrem = __reduce_add_sync(0xffffffffu, nrem);
+    if (lane == 0) {
+        if (nmig) atomicAdd(&P.ctr->migrated, nmig);
+        if (nrem) atomicAdd(&P.ctr->removed, nrem);
+    }
+}
+
+}  // namespace ipg

@@ -43,6 +43,7 @@ extern "C" {
 #define IPIC3D_E_CAPACITY -4    /* particle storage full (grow and retry)  */
 #define IPIC3D_E_NODEVICE -5    /* no usable sm_103 device                 */
 #define IPIC3D_E_STATE -6       /* call out of order (e.g. no particles)   */
+#define IPIC3D_E_TIMEOUT -7     /* a kernel gave up a bounded device wait  */
 
 /* ---- step configuration (the simulateSteps template arguments) ---------- */
 enum ipic3d_precision {
