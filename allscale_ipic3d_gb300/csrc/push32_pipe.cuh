@@ -111,11 +111,13 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
 
 // ---- shared-memory layout ------------------------------------------------------
 constexpr int kTileSlots = kSlotsPerCta;  // 1024 slots per tile (the cta_cells table's unit)
-constexpr int kComputeWarps = 8;
+// 7 compute warps + the producer: 2 CTAs = 16 warps per SM, 4 per scheduler,
+// which leaves each thread 128 registers
+constexpr int kComputeWarps = 7;
 constexpr int kComputeThreads = kComputeWarps * 32;
 constexpr int kPipeThreads = kComputeThreads + 32;  // + the producer warp
+constexpr int kSlotWarps = kTileSlots / 128;        // slot mode: 128-slot slices of a tile
 constexpr int kItemSlots = 256;                     // particles per item (8 per lane)
-static_assert(kTileSlots == 4 * kComputeThreads, "slot mode: 4 slots per compute thread");
 
 constexpr int kItemMaxCells = 32;  // tiles of at most this many cells run in item mode
 
@@ -515,16 +517,16 @@ __device__ __forceinline__ void push_item(const Geom& g, const Pop<float>& P, co
     if (kDep) emit_corner_sums(g, warp_column_sum(acc, flush_tile), ci.cx, ci.cy, ci.cz, P.q);
 }
 
-// Slot mode: warp w pushes slots [128 w, 128 w + 128) of the tile, thread t
-// the 4 slots from 4 t (one cell: capacities are multiples of 8), and flushes
-// per run of lanes of one cell.
+// Slot mode: slice w of the tile (slots [128 w, 128 w + 128)) is pushed by
+// one warp, thread t of the slice the 4 slots from 4 t (one cell:
+// capacities are multiples of 8), and flushed per run of lanes of one cell.
 template <int kF>
 __device__ __forceinline__ void push_slots(const Geom& g, const Pop<float>& P, const Push32Const& pc,
-                                           PipeStage& st, int base, int2 desc, float* flush_tile, uint32_t& nmig,
-                                           uint32_t& nrem) {
+                                           PipeStage& st, int base, int2 desc, int slice, float* flush_tile,
+                                           uint32_t& nmig, uint32_t& nrem) {
     constexpr bool kStep = (kF & kPipeStep) != 0, kDep = (kF & kPipeDeposit) != 0;
     constexpr int kPer = 4;
-    const int tid = threadIdx.x, lane = tid & 31;
+    const int lane = threadIdx.x & 31, tid = slice * 32 + lane;
     const int c0 = desc.x, nc = desc.y;
     const int64_t* S = st.start + (c0 & 1);  // S[i] = start[c0 + i]
     const int32_t* N = st.count + (c0 & 3);  // N[i] = count[c0 + i]
@@ -612,7 +614,8 @@ __device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& 
     const int base = tile * kTileSlots;
     const int c0 = desc.x, nc = desc.y;
     if (nc > kItemMaxCells) {
-        push_slots<kF>(g, P, pc, st, base, desc, flush_tile, nmig, nrem);
+        for (int w = threadIdx.x >> 5; w < kSlotWarps; w += kComputeWarps)
+            push_slots<kF>(g, P, pc, st, base, desc, w, flush_tile, nmig, nrem);
         return;
     }
     // item mode: lane i describes cell c0 + i: its occupied slots [lo, hi)
