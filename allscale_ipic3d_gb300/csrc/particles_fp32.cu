@@ -10,7 +10,7 @@ namespace ipg {
 
 namespace {
 constexpr int kMaxDevices = 64;
-constexpr int kPipeStages = 2;  // shared-memory stages per CTA (2 CTAs per SM)
+constexpr int kPipeStages = 3;  // shared-memory stages per CTA (2 CTAs per SM)
 std::mutex g_pipe_mu;
 bool g_pipe_ready[kMaxDevices] = {};
 int g_pipe_grid[kMaxDevices] = {};  // persistent CTAs of the pipelined push

@@ -36,7 +36,7 @@
 // moments keep the FP32 sums small, so the butterflies' cancellation loses
 // no more than the sums' own rounding.
 //
-// Every wait on an mbarrier is bounded (kWaitCycles): on expiry the CTA
+// Every wait on an mbarrier is bounded (kMaxPolls): on expiry the CTA
 // records a timeout in the population's counters, drains its own copies and
 // returns; the host turns the count into IPIC3D_E_TIMEOUT.
 #pragma once
@@ -61,27 +61,27 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                  : "memory");
 }
+// One poll of the phase with parity `parity`; the thread sleeps in the
+// barrier until the phase completes or about kPollNs nanoseconds pass.
+constexpr uint32_t kPollNs = 20000;
 __device__ __forceinline__ uint32_t mbar_try_wait(uint64_t* bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
+        : "r"(smem_u32(bar)), "r"(parity), "n"(kPollNs)
         : "memory");
     return ok;
 }
-// ~1 s at the GB300's 2.07 GHz: far beyond any copy's latency
-constexpr long long kWaitCycles = 2000000000LL;
-// Waits for the phase of `bar` with parity `parity`; false after kWaitCycles
-// (or 2^26 polls), or as soon as *abort is set.
+// Polls until the phase completes: false after kMaxPolls polls (about 1 s)
+// or as soon as *abort is set.
+constexpr uint32_t kMaxPolls = 1000000000u / kPollNs;
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const volatile int* abort) {
-    if (mbar_try_wait(bar, parity)) return true;
-    const long long t0 = clock64();
-    for (uint32_t it = 0; it < (1u << 26); ++it) {
+    for (uint32_t it = 0; it < kMaxPolls; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if (*abort || clock64() - t0 > kWaitCycles) break;
+        if (*abort) break;
     }
     return false;
 }
@@ -135,7 +135,6 @@ static_assert(offsetof(PipeStage, coef) % 16 == 0 && offsetof(PipeStage, start) 
 template <int kStages>
 struct PipeSmem {
     PipeStage stage[kStages];
-    alignas(16) float flush[kComputeWarps][32 * 36];  // per-warp deposit tile (warp_column_sum)
     uint64_t full[kStages];               // the stage's copies landed
     uint64_t empty[kStages];              // the compute warps are done with the stage
     int2 desc[kStages];                   // (first cell, number of cells) of the stage's tile
@@ -143,7 +142,7 @@ struct PipeSmem {
     int abort;                            // a wait expired: every warp stops
 };
 
-static_assert(offsetof(PipeSmem<2>, stage) == 0 && offsetof(PipeSmem<3>, stage) == 0, "stages first");
+static_assert(offsetof(PipeSmem<3>, stage) == 0, "stages first");
 
 template <int kStages>
 constexpr size_t pipe_smem_bytes() {
@@ -461,24 +460,6 @@ __device__ __forceinline__ void leave_and_hole(const Geom& g, const Pop<float>& 
     }
 }
 
-// Sum over the warp's lanes of acc[v] into lane v, through the warp's
-// shared-memory tile: row t (lane t's 32 values) at [36 t], written with
-// 128-bit stores; lane v reads column v (36 = 4 mod 32: no bank conflicts
-// either way).
-constexpr int kFlushStride = 36;
-__device__ __forceinline__ float warp_column_sum(const float (&acc)[32], float* flush_tile) {
-    const int lane = threadIdx.x & 31;
-    float4* row = reinterpret_cast<float4*>(flush_tile + lane * kFlushStride);
-#pragma unroll
-    for (int v = 0; v < 8; ++v) row[v] = make_float4(acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
-    __syncwarp();
-    float s = 0.f;
-#pragma unroll
-    for (int t = 0; t < 32; ++t) s += flush_tile[t * kFlushStride + lane];
-    __syncwarp();
-    return s;
-}
-
 // Item mode: the warp pushes particles [a, b) (tile-local slots, b - a <=
 // kItemSlots) of cell `cell`, lane l taking a + l, a + l + 32, ...; stayers
 // go back to HBM with coalesced stores, the cell's moments are flushed once.
@@ -486,7 +467,7 @@ __device__ __forceinline__ float warp_column_sum(const float (&acc)[32], float* 
 template <int kF>
 __device__ __forceinline__ void push_item(const Geom& g, const Pop<float>& P, const Push32Const& pc,
                                           const PipeStage& st, const float* coef, int base, int cell, int cstart,
-                                          int a, int b, float* flush_tile, uint32_t& nmig, uint32_t& nrem) {
+                                          int a, int b, uint32_t& nmig, uint32_t& nrem) {
     constexpr bool kStep = (kF & kPipeStep) != 0, kDep = (kF & kPipeDeposit) != 0;
     const int lane = threadIdx.x & 31;
     const CellInfo ci = cell_info(g, pc, cell);
@@ -514,7 +495,32 @@ __device__ __forceinline__ void push_item(const Geom& g, const Pop<float>& P, co
         }
         if (kStep) leave_and_hole(g, P, outcome, dir, ci, p, base + sl, cell, cstart, kDep, nmig, nrem);
     }
-    if (kDep) emit_corner_sums(g, warp_column_sum(acc, flush_tile), ci.cx, ci.cy, ci.cz, P.q);
+    if (kDep) emit_corner_sums(g, warp_transpose_sum<float>(acc), ci.cx, ci.cy, ci.cz, P.q);
+}
+
+// warp_transpose_sum of acc over the lanes with `mine` set (the others add
+// zero), without a masked copy of acc: the first exchange applies the mask.
+__device__ __forceinline__ float run_transpose_sum(const float (&acc)[32], bool mine) {
+    const int lane = threadIdx.x & 31;
+    const bool upper = (lane & 16) != 0;
+    float v[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const float send = mine ? (upper ? acc[i] : acc[i + 16]) : 0.f;
+        const float keep = mine ? (upper ? acc[i + 16] : acc[i]) : 0.f;
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+#pragma unroll
+    for (int off = 8; off >= 1; off >>= 1) {
+        const bool up = (lane & off) != 0;
+#pragma unroll
+        for (int i = 0; i < off; ++i) {
+            const float send = up ? v[i] : v[i + off];
+            const float keep = up ? v[i + off] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+        }
+    }
+    return v[0];
 }
 
 // Slot mode: slice w of the tile (slots [128 w, 128 w + 128)) is pushed by
@@ -522,8 +528,8 @@ __device__ __forceinline__ void push_item(const Geom& g, const Pop<float>& P, co
 // capacities are multiples of 8), and flushed per run of lanes of one cell.
 template <int kF>
 __device__ __forceinline__ void push_slots(const Geom& g, const Pop<float>& P, const Push32Const& pc,
-                                           PipeStage& st, int base, int2 desc, int slice, float* flush_tile,
-                                           uint32_t& nmig, uint32_t& nrem) {
+                                           PipeStage& st, int base, int2 desc, int slice, uint32_t& nmig,
+                                           uint32_t& nrem) {
     constexpr bool kStep = (kF & kPipeStep) != 0, kDep = (kF & kPipeDeposit) != 0;
     constexpr int kPer = 4;
     const int lane = threadIdx.x & 31, tid = slice * 32 + lane;
@@ -582,40 +588,33 @@ __device__ __forceinline__ void push_slots(const Geom& g, const Pop<float>& P, c
         if (kStep) leave_and_hole(g, P, outcome, dir, ci, p, base + sl, cell, cstart, kDep, nmig, nrem);
     }
     if (!kDep) return;
-    float4* row = reinterpret_cast<float4*>(flush_tile + lane * kFlushStride);
-#pragma unroll
-    for (int v = 0; v < 8; ++v) row[v] = make_float4(acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
     const unsigned todo = __ballot_sync(0xffffffffu, has_acc);
     const int prev_cell = __shfl_up_sync(0xffffffffu, cell, 1);
     unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev_cell != cell);
-    __syncwarp();
     while (heads) {
         const int a = __ffs(heads) - 1;
         heads &= heads - 1;
         const int b = heads ? __ffs(heads) - 1 : 32;  // run [a, b)
         const unsigned run = (b < 32 ? (1u << b) : 0u) - (1u << a);
         if (!(todo & run)) continue;
-        float s = 0.f;
-#pragma unroll 4
-        for (int t = a; t < b; ++t) s += flush_tile[t * kFlushStride + lane];
+        const float s = run_transpose_sum(acc, ((run >> lane) & 1u) != 0);
         const int gx = __shfl_sync(0xffffffffu, ci.cx, a), gy = __shfl_sync(0xffffffffu, ci.cy, a),
                   gz = __shfl_sync(0xffffffffu, ci.cz, a);
         emit_corner_sums(g, s, gx, gy, gz, P.q);
     }
-    __syncwarp();
 }
 
 // One compute warp's share of the tile in `st`.
 template <int kF>
 __device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& P, const Push32Const& pc, int tile,
-                                               int2 desc, PipeStage& st, int* next_item, float* flush_tile,
-                                               uint32_t& nmig, uint32_t& nrem) {
+                                               int2 desc, PipeStage& st, int* next_item, uint32_t& nmig,
+                                               uint32_t& nrem) {
     const int lane = threadIdx.x & 31;
     const int base = tile * kTileSlots;
     const int c0 = desc.x, nc = desc.y;
     if (nc > kItemMaxCells) {
         for (int w = threadIdx.x >> 5; w < kSlotWarps; w += kComputeWarps)
-            push_slots<kF>(g, P, pc, st, base, desc, w, flush_tile, nmig, nrem);
+            push_slots<kF>(g, P, pc, st, base, desc, w, nmig, nrem);
         return;
     }
     // item mode: lane i describes cell c0 + i: its occupied slots [lo, hi)
@@ -650,7 +649,7 @@ __device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& 
         const int cstart = __shfl_sync(0xffffffffu, cst, src);
         const int a = clo + (j - cex) * kItemSlots;
         const int b = a + kItemSlots < chi ? a + kItemSlots : chi;
-        push_item<kF>(g, P, pc, st, st.coef + src * 48, base, c0 + src, cstart, a, b, flush_tile, nmig, nrem);
+        push_item<kF>(g, P, pc, st, st.coef + src * 48, base, c0 + src, cstart, a, b, nmig, nrem);
     }
 }
 
@@ -732,7 +731,6 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
     }
 
     // ---- compute warps ----
-    float* flush_tile = sm.flush[warp];
     uint32_t nmig = 0, nrem = 0;
     int k = 0;
     for (int t = blockIdx.x; t < ntiles; t += G, ++k) {
@@ -742,7 +740,7 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
             if (lane == 0 && atomicExch(&sm.abort, 1) == 0) atomicAdd(&P.ctr->timeouts, 1u);
             break;
         }
-        push_tile_warp<kF>(g, P, pc, t, sm.desc[s], sm.stage[s], &sm.next_item[s], flush_tile, nmig, nrem);
+        push_tile_warp<kF>(g, P, pc, t, sm.desc[s], sm.stage[s], &sm.next_item[s], nmig, nrem);
         fence_proxy_async_smem();  // this warp's writes to the stage, before the bulk stores read it
         __syncwarp();
         if (lane == 0) mbar_arrive(&sm.empty[s]);
