@@ -22,6 +22,7 @@ namespace ipg {
 constexpr int kVec = 4;                 // particles per thread (one float4 / 2x double2)
 constexpr int kPushThreads = 256;       // threads per CTA of the push kernel
 constexpr int kSlotsPerCta = kVec * kPushThreads;
+constexpr int kSetPops = 4;             // populations per launch of the population-set kernels
 constexpr int kSlotAlign = 8;          // start[] and every cell's capacity are multiples of 8
 constexpr int kMaxCellsPerCta = kSlotsPerCta / kSlotAlign + 2;
 
@@ -65,6 +66,7 @@ struct StepCounters {
     uint32_t removed;       // particles removed (planet, open faces)
     uint32_t migrated;      // particles that changed cell
     uint32_t injected;
+    uint32_t dirty;         // cells with holes or arrivals this step (entries of dirty_list)
     uint32_t lost;          // pending list overflow (must stay 0)
     uint32_t timeouts;      // CTAs that gave up a bounded wait (must stay 0)
 };
@@ -80,6 +82,8 @@ struct Pop {
     int32_t* hole_list;     // [capacity] holes of cell c at start[c] + k
     int32_t* arr_cnt;       // [ncells]
     int32_t* arr_list;      // [capacity] arrivals of cell c at start[c] + k (outbox index)
+    int32_t* dirty_flag;    // [ncells] 1 while the cell is on this step's dirty list
+    int32_t* dirty_list;    // [ncells] cells with holes or arrivals (the placement's work list)
     Mover<T>* outbox;
     uint32_t outbox_cap;
     Mover<T>* pending_in;   // pushed this step
@@ -91,6 +95,16 @@ struct Pop {
     double q, qom;
     int32_t shape;          // launch shape of the FP32 push (kPushShape*)
     int32_t pad;
+};
+
+// Up to kSetPops populations of one universe advanced by one launch
+// (blockIdx.y = population for the placement, pending and rotation kernels).
+template <typename T>
+struct PopSet {
+    Pop<T> p[kSetPops];
+    int32_t* sort_tmp[kSetPops];    // placement scratch of each population
+    uint32_t* pend_count[kSetPops]; // = p[i].pending_in_count, writable (rotation)
+    int n;
 };
 
 // Launch shapes of the pipelined FP32 push (shared-memory stages per CTA).
@@ -109,6 +123,11 @@ struct Push32Const {
     float origin[3];  // domain origin relative to the dipole centre (0,0,0)
     float center[3];  // object centre (planet)
     float inv_sy, inv_sz;  // 1 / cells along y and z (cell index -> coordinates)
+};
+
+// The push constants of the populations of a PopSet.
+struct Push32Set {
+    Push32Const c[kSetPops];
 };
 
 // ---- batched ensemble ------------------------------------------------------
@@ -180,6 +199,38 @@ __device__ __forceinline__ int fast_div(int a, int d, float inv_d) {
     const int r = a - q * d;
     q += (r >= d) - (r < 0);
     return q;
+}
+
+// Puts cell c on the step's dirty list (once per step: the flag is cleared
+// by the placement that processes the cell).
+template <typename T>
+__device__ __forceinline__ void mark_dirty(const Pop<T>& P, int c) {
+    if (atomicExch(P.dirty_flag + c, 1) == 0) P.dirty_list[atomicAdd(&P.ctr->dirty, 1u)] = c;
+}
+
+// Files slot `slot` as a hole of cell c (its slots start at cstart).
+template <typename T>
+__device__ __forceinline__ void file_hole(const Pop<T>& P, int c, int64_t cstart, int64_t slot) {
+    const int k = atomicAdd(P.hole_cnt + c, 1);
+    P.hole_list[cstart + k] = (int32_t)slot;
+    if (k == 0) mark_dirty(P, c);
+}
+
+// t = (a * n1 + b) * n2 + c for t in [0, n0 * n1 * n2): 32-bit divisions
+// when t fits (64-bit division by a runtime divisor is a long software
+// sequence on the GPU).
+__device__ __forceinline__ void split3(int64_t t, int n1, int n2, int& a, int& b, int& c) {
+    if (t < 0x7fffffff) {
+        const unsigned u = (unsigned)t, r = u / (unsigned)n2;
+        c = (int)(u - r * (unsigned)n2);
+        a = (int)(r / (unsigned)n1);
+        b = (int)(r - (unsigned)a * (unsigned)n1);
+    } else {
+        c = (int)(t % n2);
+        const int64_t r = t / n2;
+        b = (int)(r % n1);
+        a = (int)(r / n1);
+    }
 }
 
 // Warp-aggregated atomic increment: one atomic per warp for all active

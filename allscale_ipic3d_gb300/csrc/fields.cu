@@ -15,6 +15,8 @@
 // The reference's per-node solver updates E and then Bc in one in-place pass
 // whose result depends on the visiting order; here E is updated everywhere
 // first and Bc afterwards (the order-independent two-phase reading).
+#include <cmath>
+
 #include "launch.h"
 
 namespace ipg {
@@ -29,9 +31,10 @@ __device__ __forceinline__ void ghost_body(double* g, int n, int per, int64_t t0
     const int end = n - 1;
     const int64_t m = (int64_t)(end - 1) * (end - 1);
     for (int64_t t = t0; t < m * per; t += stride) {
-        const int comp = (int)(t % per);
-        const int64_t ab = t / per;
-        const int a = 1 + (int)(ab / (end - 1)), b = 1 + (int)(ab % (end - 1));
+        int a, b, comp;
+        split3(t, end - 1, per, a, b, comp);  // t = (a' (end - 1) + b') per + comp
+        a += 1;
+        b += 1;
         g[fidx(n, 0, a, b) * per + comp] = g[fidx(n, end - 1, a, b) * per + comp];
         g[fidx(n, end, a, b) * per + comp] = g[fidx(n, 1, a, b) * per + comp];
         g[fidx(n, a, 0, b) * per + comp] = g[fidx(n, a, end - 1, b) * per + comp];
@@ -45,18 +48,30 @@ struct SolverArgs {
     int s;                // cells per axis (cubic)
     double dt, c;
     double wx, wy, wz;
+    double iwx, iwy, iwz;  // 1 / w (the multiplying solvers)
     double* field;        // (s+3)^3 x 9
     double* bc;           // (s+2)^3 x 3
     const double* J;      // (s+1)^3 x 3
 };
 
+// d / w: the reference's division (kMul false) or the product with 1 / w
+// (kMul: equal bit for bit when w is a power of two; the FP32 path's solver
+// otherwise)
+template <bool kMul>
+__device__ __forceinline__ double over(double d, double w, double iw) {
+    return kMul ? d * iw : d / w;
+}
+
 // E at pos in [1, s+2)^3 from Bc(pos), Bc(pos - e_i) and J(pos - 1).
+template <bool kMul = false>
 __device__ __forceinline__ void leapfrog_e_body(SolverArgs A, int64_t t0, int64_t stride) {
     const int n = A.s + 1;  // nodes per axis in the updated box
     const int64_t total = (int64_t)n * n * n;
     const double c2 = A.c * A.c;
     for (int64_t t = t0; t < total; t += stride) {
-        const int x = 1 + (int)(t / ((int64_t)n * n)), y = 1 + (int)((t / n) % n), z = 1 + (int)(t % n);
+        int x, y, z;
+        split3(t, n, n, x, y, z);
+        ++x; ++y; ++z;
         const int nb = A.s + 2, nf = A.s + 3, nd = A.s + 1;
         const double* B0 = A.bc + 3 * fidx(nb, x, y, z);
         const double* Bxm = A.bc + 3 * fidx(nb, x - 1, y, z);
@@ -64,27 +79,33 @@ __device__ __forceinline__ void leapfrog_e_body(SolverArgs A, int64_t t0, int64_
         const double* Bzm = A.bc + 3 * fidx(nb, x, y, z - 1);
         const double* J = A.J + 3 * fidx(nd, x - 1, y - 1, z - 1);
         double* E = A.field + 9 * fidx(nf, x, y, z);
-        E[0] = E[0] + A.dt * (c2 * ((B0[2] - Bym[2]) / A.wy - (B0[1] - Bzm[1]) / A.wz) - J[0]);
-        E[1] = E[1] + A.dt * (c2 * ((B0[0] - Bzm[0]) / A.wz - (B0[2] - Bxm[2]) / A.wx) - J[1]);
-        E[2] = E[2] + A.dt * (c2 * ((B0[1] - Bxm[1]) / A.wx - (B0[0] - Bym[0]) / A.wy) - J[2]);
+        E[0] = E[0] + A.dt * (c2 * (over<kMul>(B0[2] - Bym[2], A.wy, A.iwy) - over<kMul>(B0[1] - Bzm[1], A.wz, A.iwz)) -
+                              J[0]);
+        E[1] = E[1] + A.dt * (c2 * (over<kMul>(B0[0] - Bzm[0], A.wz, A.iwz) - over<kMul>(B0[2] - Bxm[2], A.wx, A.iwx)) -
+                              J[1]);
+        E[2] = E[2] + A.dt * (c2 * (over<kMul>(B0[1] - Bxm[1], A.wx, A.iwx) - over<kMul>(B0[0] - Bym[0], A.wy, A.iwy)) -
+                              J[2]);
     }
 }
 
 // Bc at pos in [1, s+1)^3 from the new E at pos and pos + e_i.
+template <bool kMul = false>
 __device__ __forceinline__ void leapfrog_b_body(SolverArgs A, int64_t t0, int64_t stride) {
     const int n = A.s;
     const int64_t total = (int64_t)n * n * n;
     for (int64_t t = t0; t < total; t += stride) {
-        const int x = 1 + (int)(t / ((int64_t)n * n)), y = 1 + (int)((t / n) % n), z = 1 + (int)(t % n);
+        int x, y, z;
+        split3(t, n, n, x, y, z);
+        ++x; ++y; ++z;
         const int nb = A.s + 2, nf = A.s + 3;
         const double* E0 = A.field + 9 * fidx(nf, x, y, z);
         const double* Ex = A.field + 9 * fidx(nf, x + 1, y, z);
         const double* Ey = A.field + 9 * fidx(nf, x, y + 1, z);
         const double* Ez = A.field + 9 * fidx(nf, x, y, z + 1);
         double* B = A.bc + 3 * fidx(nb, x, y, z);
-        B[0] = B[0] - A.dt * ((Ey[2] - E0[2]) / A.wy - (Ez[1] - E0[1]) / A.wz);
-        B[1] = B[1] - A.dt * ((Ez[0] - E0[0]) / A.wz - (Ex[2] - E0[2]) / A.wx);
-        B[2] = B[2] - A.dt * ((Ex[1] - E0[1]) / A.wx - (Ey[0] - E0[0]) / A.wy);
+        B[0] = B[0] - A.dt * (over<kMul>(Ey[2] - E0[2], A.wy, A.iwy) - over<kMul>(Ez[1] - E0[1], A.wz, A.iwz));
+        B[1] = B[1] - A.dt * (over<kMul>(Ez[0] - E0[0], A.wz, A.iwz) - over<kMul>(Ex[2] - E0[2], A.wx, A.iwx));
+        B[2] = B[2] - A.dt * (over<kMul>(Ex[1] - E0[1], A.wx, A.iwx) - over<kMul>(Ey[0] - E0[0], A.wy, A.iwy));
     }
 }
 
@@ -141,7 +162,9 @@ __device__ __forceinline__ void forward_e_body(SolverArgs A, int64_t t0, int64_t
     const int n = A.s + 1;
     const int64_t total = (int64_t)n * n * n;
     for (int64_t t = t0; t < total; t += stride) {
-        const int x = 1 + (int)(t / ((int64_t)n * n)), y = 1 + (int)((t / n) % n), z = 1 + (int)(t % n);
+        int x, y, z;
+        split3(t, n, n, x, y, z);
+        ++x; ++y; ++z;
         double cx, cy, cz;
         curl_b(A, x, y, z, cx, cy, cz);
         const double* J = A.J + 3 * fidx(A.s + 1, x - 1, y - 1, z - 1);
@@ -156,7 +179,9 @@ __device__ __forceinline__ void forward_b_body(SolverArgs A, int64_t t0, int64_t
     const int n = A.s;
     const int64_t total = (int64_t)n * n * n;
     for (int64_t t = t0; t < total; t += stride) {
-        const int x = 1 + (int)(t / ((int64_t)n * n)), y = 1 + (int)((t / n) % n), z = 1 + (int)(t % n);
+        int x, y, z;
+        split3(t, n, n, x, y, z);
+        ++x; ++y; ++z;
         double cx, cy, cz;
         curl_e(A, x, y, z, cx, cy, cz);
         double* B = A.bc + 3 * fidx(A.s + 2, x, y, z);
@@ -171,7 +196,9 @@ __device__ __forceinline__ void interp_c2n_body(SolverArgs A, int64_t t0, int64_
     const int n = A.s + 1;
     const int64_t total = (int64_t)n * n * n;
     for (int64_t t = t0; t < total; t += stride) {
-        const int x = 1 + (int)(t / ((int64_t)n * n)), y = 1 + (int)((t / n) % n), z = 1 + (int)(t % n);
+        int x, y, z;
+        split3(t, n, n, x, y, z);
+        ++x; ++y; ++z;
         double a0 = 0.0, a1 = 0.0, a2 = 0.0;
         for (int i = 0; i < 2; i++)
             for (int j = 0; j < 2; j++)
@@ -193,7 +220,8 @@ __device__ __forceinline__ void j_finalize_body(int sx, int sy, int sz, double* 
     const int64_t total = (int64_t)sx * sy * sz;
     const int ny = sy + 1, nz = sz + 1;
     for (int64_t t = t0; t < total; t += stride) {
-        const int x = (int)(t / ((int64_t)sy * sz)), y = (int)((t / sz) % sy), z = (int)(t % sz);
+        int x, y, z;
+        split3(t, sy, sz, x, y, z);
         const int nxs = x == 0 ? 2 : 1, nys = y == 0 ? 2 : 1, nzs = z == 0 ? 2 : 1;
         double a[4] = {0.0, 0.0, 0.0, 0.0};
         for (int i = 0; i < nxs; ++i)
@@ -234,6 +262,9 @@ __host__ __device__ inline SolverArgs solver_args(const Geom& g) {
     A.wx = g.w[0];
     A.wy = g.w[1];
     A.wz = g.w[2];
+    A.iwx = 1.0 / g.w[0];
+    A.iwy = 1.0 / g.w[1];
+    A.iwz = 1.0 / g.w[2];
     A.field = g.field;
     A.bc = g.bcfield;
     A.J = g.J;
@@ -241,14 +272,51 @@ __host__ __device__ inline SolverArgs solver_args(const Geom& g) {
 }
 
 // single-universe kernels
-__global__ void k_ghost(double* g, int n, int per) { ghost_body(g, n, per, grid_t0(), grid_stride()); }
-__global__ void k_leapfrog_e(SolverArgs A) { leapfrog_e_body(A, grid_t0(), grid_stride()); }
-__global__ void k_leapfrog_b(SolverArgs A) { leapfrog_b_body(A, grid_t0(), grid_stride()); }
+// both grids' ghost faces in one launch: threads [0, nf_items) the field,
+// the rest the Bc grid
+__global__ void k_ghost2(double* field, int nf, double* bc, int nb) {
+    const int64_t mf = (int64_t)(nf - 2) * (nf - 2) * 9;
+    const int64_t t = grid_t0();
+    if (t < mf)
+        ghost_body(field, nf, 9, t, mf);
+    else
+        ghost_body(bc, nb, 3, t - mf, (int64_t)(nb - 2) * (nb - 2) * 3);
+}
+template <bool kMul>
+__global__ void k_leapfrog_e(SolverArgs A) { leapfrog_e_body<kMul>(A, grid_t0(), grid_stride()); }
+template <bool kMul>
+__global__ void k_leapfrog_b(SolverArgs A) { leapfrog_b_body<kMul>(A, grid_t0(), grid_stride()); }
 __global__ void k_forward_e(SolverArgs A) { forward_e_body(A, grid_t0(), grid_stride()); }
 __global__ void k_forward_b(SolverArgs A) { forward_b_body(A, grid_t0(), grid_stride()); }
 __global__ void k_interp_c2n(SolverArgs A) { interp_c2n_body(A, grid_t0(), grid_stride()); }
 __global__ void k_j_finalize(int sx, int sy, int sz, double* J, double* rho, double vol, int div8) {
     j_finalize_body(sx, sy, sz, J, rho, vol, div8, grid_t0(), grid_stride());
+}
+// The same with the normalisation as one multiplication by `inv` (1 / vol
+// [/ 8]): for the FP32 path, and wherever vol is a power of two (then the
+// product equals the reference's quotients bit for bit).
+__global__ void k_j_finalize_mul(int sx, int sy, int sz, double* J, double* rho, double inv) {
+    const int64_t total = (int64_t)sx * sy * sz;
+    const int ny = sy + 1, nz = sz + 1;
+    for (int64_t t = grid_t0(); t < total; t += grid_stride()) {
+        int x, y, z;
+        split3(t, sy, sz, x, y, z);
+        const int nxs = x == 0 ? 2 : 1, nys = y == 0 ? 2 : 1, nzs = z == 0 ? 2 : 1;
+        double a[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int i = 0; i < nxs; ++i)
+            for (int j = 0; j < nys; ++j)
+                for (int k = 0; k < nzs; ++k) {
+                    const int64_t n = ((int64_t)(i ? sx : x) * ny + (j ? sy : y)) * nz + (k ? sz : z);
+                    a[0] += J[3 * n]; a[1] += J[3 * n + 1]; a[2] += J[3 * n + 2]; a[3] += rho[n];
+                }
+        for (int c = 0; c < 4; ++c) a[c] *= inv;
+        for (int i = 0; i < nxs; ++i)
+            for (int j = 0; j < nys; ++j)
+                for (int k = 0; k < nzs; ++k) {
+                    const int64_t n = ((int64_t)(i ? sx : x) * ny + (j ? sy : y)) * nz + (k ? sz : z);
+                    J[3 * n] = a[0]; J[3 * n + 1] = a[1]; J[3 * n + 2] = a[2]; rho[n] = a[3];
+                }
+    }
 }
 
 // batched kernels: blockIdx.y is the universe, blockIdx.x strides over its
@@ -361,7 +429,9 @@ __global__ void k_reduce_fields(const double* field, int s, double vol, double f
     const int n = s + 1, nf = s + 3;
     const int64_t total = (int64_t)n * n * n;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        const int x = 1 + (int)(t / ((int64_t)n * n)), y = 1 + (int)((t / n) % n), z = 1 + (int)(t % n);
+        int x, y, z;
+        split3(t, n, n, x, y, z);
+        ++x; ++y; ++z;
         const double* f = field + 9 * fidx(nf, x, y, z);
         double e = f[0] * f[0];
         e += f[1] * f[1];
@@ -403,16 +473,27 @@ inline int grid_for(int64_t n, int threads, int64_t max_blocks = 152 * 32) {
 
 int launch_ghost(const Geom& g, cudaStream_t st) {
     const int nf = g.sx + 3, nb = g.sx + 2;
-    k_ghost<<<grid_for((int64_t)(nf - 2) * (nf - 2) * 9, 256), 256, 0, st>>>(g.field, nf, 9);
-    k_ghost<<<grid_for((int64_t)(nb - 2) * (nb - 2) * 3, 256), 256, 0, st>>>(g.bcfield, nb, 3);
-    return 2;
+    const int64_t items = (int64_t)(nf - 2) * (nf - 2) * 9 + (int64_t)(nb - 2) * (nb - 2) * 3;
+    k_ghost2<<<(unsigned)((items + 255) / 256), 256, 0, st>>>(g.field, nf, g.bcfield, nb);
+    return 1;
 }
 
-int launch_leapfrog(const Geom& g, bool refresh_node_b, cudaStream_t st) {
+static bool pow2(double v) {
+    int e = 0;
+    return std::frexp(v, &e) == 0.5;
+}
+
+int launch_leapfrog(const Geom& g, bool refresh_node_b, bool exact, cudaStream_t st) {
     SolverArgs A = solver_args(g);
     const int64_t ne = (int64_t)(g.sx + 1) * (g.sx + 1) * (g.sx + 1);
-    k_leapfrog_e<<<grid_for(ne, 256), 256, 0, st>>>(A);
-    k_leapfrog_b<<<grid_for((int64_t)g.sx * g.sx * g.sx, 256), 256, 0, st>>>(A);
+    const bool mul = !exact || (pow2(g.w[0]) && pow2(g.w[1]) && pow2(g.w[2]));
+    if (mul) {
+        k_leapfrog_e<true><<<grid_for(ne, 256), 256, 0, st>>>(A);
+        k_leapfrog_b<true><<<grid_for((int64_t)g.sx * g.sx * g.sx, 256), 256, 0, st>>>(A);
+    } else {
+        k_leapfrog_e<false><<<grid_for(ne, 256), 256, 0, st>>>(A);
+        k_leapfrog_b<false><<<grid_for((int64_t)g.sx * g.sx * g.sx, 256), 256, 0, st>>>(A);
+    }
     if (refresh_node_b) {
         k_interp_c2n<<<grid_for(ne, 256), 256, 0, st>>>(A);
         return 3;
@@ -429,9 +510,15 @@ int launch_forward(const Geom& g, cudaStream_t st) {
     return 3;
 }
 
-int launch_j_finalize(const Geom& g, bool div8, cudaStream_t st) {
-    k_j_finalize<<<grid_for((int64_t)g.sx * g.sy * g.sz, 256), 256, 0, st>>>(g.sx, g.sy, g.sz, g.J, g.rho, g.vol,
-                                                                             div8 ? 1 : 0);
+int launch_j_finalize(const Geom& g, bool div8, bool exact, cudaStream_t st) {
+    if (exact && !pow2(g.vol)) {  // vol = 2^k: 1 / vol is exact
+        k_j_finalize<<<grid_for((int64_t)g.sx * g.sy * g.sz, 256), 256, 0, st>>>(g.sx, g.sy, g.sz, g.J, g.rho,
+                                                                                 g.vol, div8 ? 1 : 0);
+    } else {
+        const double inv = div8 ? 1.0 / g.vol / 8.0 : 1.0 / g.vol;
+        k_j_finalize_mul<<<grid_for((int64_t)g.sx * g.sy * g.sz, 256), 256, 0, st>>>(g.sx, g.sy, g.sz, g.J, g.rho,
+                                                                                     inv);
+    }
     return 1;
 }
 

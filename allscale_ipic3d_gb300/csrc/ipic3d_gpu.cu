@@ -69,6 +69,7 @@ struct PopStore {
     int2* cta_cells = nullptr;
     int32_t *count = nullptr, *hole_cnt = nullptr, *arr_cnt = nullptr;
     int32_t *hole_list = nullptr, *arr_list = nullptr, *sort_tmp = nullptr;
+    int32_t *dirty_flag = nullptr, *dirty_list = nullptr;
     Mover<T>*outbox = nullptr, *pending_in = nullptr, *pending_out = nullptr;
     uint32_t* pending_in_count = nullptr;
     StepCounters* ctr = nullptr;
@@ -78,7 +79,7 @@ struct PopStore {
     void release() {
         dfree(x); dfree(y); dfree(z); dfree(u); dfree(v); dfree(w); dfree(id);
         dfree(start); dfree(cta_cells); dfree(count); dfree(hole_cnt); dfree(arr_cnt);
-        dfree(hole_list); dfree(arr_list); dfree(sort_tmp);
+        dfree(hole_list); dfree(arr_list); dfree(sort_tmp); dfree(dirty_flag); dfree(dirty_list);
         dfree(outbox); dfree(pending_in); dfree(pending_out);
         dfree(pending_in_count); dfree(ctr);
         capacity = 0;
@@ -94,6 +95,8 @@ struct PopStore {
         P.hole_list = hole_list;
         P.arr_cnt = arr_cnt;
         P.arr_list = arr_list;
+        P.dirty_flag = dirty_flag;
+        P.dirty_list = dirty_list;
         P.outbox = outbox;
         P.outbox_cap = outbox_cap;
         P.pending_in = pending_in;
@@ -115,6 +118,23 @@ struct PopStore {
 
 namespace ipg {
 constexpr int kMaxPops = 16;
+
+// The populations in launch sets of up to kSetPops.
+template <typename T>
+std::vector<PopSet<T>> pop_sets(std::vector<PopStore<T>>& pops) {
+    std::vector<PopSet<T>> out;
+    for (size_t i = 0; i < pops.size(); i += kSetPops) {
+        PopSet<T> S{};
+        S.n = (int)std::min<size_t>(kSetPops, pops.size() - i);
+        for (int k = 0; k < S.n; ++k) {
+            S.p[k] = pops[i + k].view();
+            S.sort_tmp[k] = pops[i + k].sort_tmp;
+            S.pend_count[k] = pops[i + k].pending_in_count;
+        }
+        out.push_back(S);
+    }
+    return out;
+}
 // Advances the device step counter (keys the injection generator).
 __global__ void k_step_end(uint64_t* step) { *step += 1; }
 }  // namespace ipg
@@ -240,6 +260,9 @@ int alloc_pop(ipic3d_ctx* ctx, PopStore<T>& P, const std::vector<uint64_t>& coun
     CU(cudaMalloc(&P.hole_list, cap * sizeof(int32_t)));
     CU(cudaMalloc(&P.arr_list, cap * sizeof(int32_t)));
     CU(cudaMalloc(&P.sort_tmp, cap * sizeof(int32_t)));
+    CU(cudaMalloc(&P.dirty_flag, nc * sizeof(int32_t)));
+    CU(cudaMalloc(&P.dirty_list, nc * sizeof(int32_t)));
+    CU(cudaMemsetAsync(P.dirty_flag, 0, nc * sizeof(int32_t), ctx->stream));
     CU(cudaMalloc(&P.outbox, (size_t)P.outbox_cap * sizeof(Mover<T>)));
     CU(cudaMalloc(&P.pending_in, (size_t)P.pending_cap * sizeof(Mover<T>)));
     CU(cudaMalloc(&P.pending_out, (size_t)P.pending_cap * sizeof(Mover<T>)));
@@ -427,6 +450,7 @@ int scatter_pops(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, const std::vec
         cudaStream_t st = ctx->stream;
         CU(cudaMemsetAsync(P.hole_cnt, 0, nc * sizeof(int32_t), st));
         CU(cudaMemsetAsync(P.arr_cnt, 0, nc * sizeof(int32_t), st));
+        CU(cudaMemsetAsync(P.dirty_flag, 0, nc * sizeof(int32_t), st));
         CU(cudaMemsetAsync(P.pending_in_count, 0, sizeof(uint32_t), st));
         CU(cudaMemsetAsync(P.ctr, 0, sizeof(StepCounters), st));
     }
@@ -696,9 +720,9 @@ int project_impl(ipic3d_ctx* ctx) {
     Geom g = ctx->g;
     g.deposit = 1;
     int n = 0;
-    for (auto& P : ctx->p32) n += launch_push<float>(g, P.view(), 1, st);
-    for (auto& P : ctx->p64) n += launch_push<double>(g, P.view(), 1, st);
-    n += launch_j_finalize(g, (ctx->cfg.flags & IPIC3D_F_J_DIV8) != 0, st);
+    for (auto& S : pop_sets(ctx->p32)) n += launch_push<float>(g, S, 1, st);
+    for (auto& S : pop_sets(ctx->p64)) n += launch_push<double>(g, S, 1, st);
+    n += launch_j_finalize(g, (ctx->cfg.flags & IPIC3D_F_J_DIV8) != 0, !ctx->fp32, st);
     ctx->j_valid = true;
     return check_launch(ctx, n);
 }
@@ -708,7 +732,7 @@ int solve_impl(ipic3d_ctx* ctx) {
     int n = 0;
     ph_begin(ctx, IPIC3D_PHASE_FIELDS);
     if (ctx->cfg.solver == IPIC3D_SOLVER_LEAPFROG)
-        n += launch_leapfrog(ctx->g, (ctx->cfg.flags & IPIC3D_F_REFRESH_NODE_B) != 0, st);
+        n += launch_leapfrog(ctx->g, (ctx->cfg.flags & IPIC3D_F_REFRESH_NODE_B) != 0, !ctx->fp32, st);
     else if (ctx->cfg.solver == IPIC3D_SOLVER_FORWARD)
         n += launch_forward(ctx->g, st);
     if (ctx->fp32 && ctx->cfg.mover == IPIC3D_MOVER_FIELD && ctx->cfg.solver != IPIC3D_SOLVER_STATIC)
@@ -731,14 +755,16 @@ int move_impl(ipic3d_ctx* ctx, bool deposit) {
         CU(cudaMemsetAsync(ctx->J, 0, ctx->nnode() * 3 * sizeof(double), st));
         CU(cudaMemsetAsync(ctx->rho, 0, ctx->nnode() * sizeof(double), st));
     }
+    const auto s32 = pop_sets(ctx->p32);
+    const auto s64 = pop_sets(ctx->p64);
     ph_begin(ctx, IPIC3D_PHASE_PUSH);
-    for (auto& P : ctx->p32) n += launch_push<float>(g, P.view(), 0, st);
-    for (auto& P : ctx->p64) n += launch_push<double>(g, P.view(), 0, st);
+    for (auto& S : s32) n += launch_push<float>(g, S, 0, st);
+    for (auto& S : s64) n += launch_push<double>(g, S, 0, st);
     ph_end(ctx, IPIC3D_PHASE_PUSH);
     ctx->push_particles = ctx->particles_hint;
     ph_begin(ctx, IPIC3D_PHASE_PENDING);
-    for (auto& P : ctx->p32) n += launch_push_pending<float>(g, P.view(), st);
-    for (auto& P : ctx->p64) n += launch_push_pending<double>(g, P.view(), st);
+    for (auto& S : s32) n += launch_push_pending<float>(g, S, st);
+    for (auto& S : s64) n += launch_push_pending<double>(g, S, st);
     ph_end(ctx, IPIC3D_PHASE_PENDING);
     const bool inject = (ctx->cfg.flags & IPIC3D_F_INJECT_LOW_X) && ctx->cfg.bc_low[0] == IPIC3D_BC_OPEN &&
                         ctx->cfg.inject_per_cell > 0;
@@ -753,17 +779,20 @@ int move_impl(ipic3d_ctx* ctx, bool deposit) {
         ph_end(ctx, IPIC3D_PHASE_INJECT);
     }
     ph_begin(ctx, IPIC3D_PHASE_PLACE);
-    for (auto& P : ctx->p32) {
-        n += launch_place<float>(g, P.view(), P.sort_tmp, st);
-        n += launch_pending_rotate<float>(P.view(), P.pending_in_count, st);
-    }
-    for (auto& P : ctx->p64) {
-        n += launch_place<double>(g, P.view(), P.sort_tmp, st);
-        n += launch_pending_rotate<double>(P.view(), P.pending_in_count, st);
+    for (auto& S : s32) n += launch_place<float>(g, S, st);
+    for (auto& S : s64) n += launch_place<double>(g, S, st);
+    // the last rotation also advances the device step counter
+    for (size_t i = 0; i < s32.size(); ++i)
+        n += launch_pending_rotate<float>(s32[i], s64.empty() && i + 1 == s32.size() ? ctx->d_step : nullptr, st);
+    for (size_t i = 0; i < s64.size(); ++i)
+        n += launch_pending_rotate<double>(s64[i], i + 1 == s64.size() ? ctx->d_step : nullptr, st);
+    if (s32.empty() && s64.empty()) {
+        k_step_end<<<1, 1, 0, st>>>(ctx->d_step);
+        ++n;
     }
     ph_end(ctx, IPIC3D_PHASE_PLACE);
     if (deposit) {
-        n += launch_j_finalize(g, (ctx->cfg.flags & IPIC3D_F_J_DIV8) != 0, st);
+        n += launch_j_finalize(g, (ctx->cfg.flags & IPIC3D_F_J_DIV8) != 0, !ctx->fp32, st);
         ph_end(ctx, IPIC3D_PHASE_MOMENTS);
     }
     return check_launch(ctx, n);
@@ -778,9 +807,7 @@ int enqueue_step(ipic3d_ctx* ctx) {
         if ((rc = check_launch(ctx, n))) return rc;
         if ((rc = solve_impl(ctx))) return rc;
     }
-    if ((rc = move_impl(ctx, project))) return rc;
-    k_step_end<<<1, 1, 0, ctx->stream>>>(ctx->d_step);
-    return check_launch(ctx, 1);
+    return move_impl(ctx, project);  // advances the device step counter
 }
 
 // Reads the step counters back; rebuilds the layout when particles wait for
@@ -1194,8 +1221,6 @@ int ipic3d_gpu_move(ipic3d_ctx* ctx) {
     if (rc) return rc;
     if ((rc = move_impl(ctx, false))) return rc;
     ctx->j_valid = false;
-    k_step_end<<<1, 1, 0, ctx->stream>>>(ctx->d_step);
-    if ((rc = check_launch(ctx, 1))) return rc;
     return after_steps(ctx);
 }
 

@@ -8,18 +8,20 @@
 
 namespace ipg {
 
-// particles (particles_fp64.cu / particles_fp32.cu)
+// particles (particles_fp64.cu / particles_fp32.cu); the PopSet launchers
+// advance all populations of a set with one launch
 template <typename T>
-int launch_push(const Geom& g, const Pop<T>& P, int mode, cudaStream_t st);
+int launch_push(const Geom& g, const PopSet<T>& S, int mode, cudaStream_t st);
 template <typename T>
-int launch_push_pending(const Geom& g, const Pop<T>& P, cudaStream_t st);
+int launch_push_pending(const Geom& g, const PopSet<T>& S, cudaStream_t st);
 template <typename T>
 int launch_inject(const Geom& g, const Pop<T>& P, double per_cell, const double drift[3], const double vth[3],
                   uint64_t seed, const uint64_t* d_step, cudaStream_t st);
 template <typename T>
-int launch_place(const Geom& g, const Pop<T>& P, int32_t* sort_tmp, cudaStream_t st);
+int launch_place(const Geom& g, const PopSet<T>& S, cudaStream_t st);
+// `step` (may be null): the device step counter, advanced by the launch
 template <typename T>
-int launch_pending_rotate(const Pop<T>& P, uint32_t* pending_in_count, cudaStream_t st);
+int launch_pending_rotate(const PopSet<T>& S, uint64_t* step, cudaStream_t st);
 template <typename T>
 int launch_relayout(const Pop<T>& from, const Pop<T>& to, int ncells, int32_t* pend_per_cell_scratch,
                     cudaStream_t st);
@@ -52,9 +54,10 @@ int launch_j_finalize_batch(const InstJob* jobs, int ninst, int64_t max_cells, c
 
 // fields (fields.cu)
 int launch_ghost(const Geom& g, cudaStream_t st);
-int launch_leapfrog(const Geom& g, bool refresh_node_b, cudaStream_t st);
+int launch_leapfrog(const Geom& g, bool refresh_node_b, bool exact, cudaStream_t st);
 int launch_forward(const Geom& g, cudaStream_t st);
-int launch_j_finalize(const Geom& g, bool div8, cudaStream_t st);
+// exact: the reference's divisions (FP64 parity); else one multiplication
+int launch_j_finalize(const Geom& g, bool div8, bool exact, cudaStream_t st);
 int launch_node32(const Geom& g, float4* node32, cudaStream_t st);
 int launch_cell_coef(const Geom& g, float* coef, cudaStream_t st);  // particles_fp32.cu
 int reduce_blocks();

@@ -427,6 +427,7 @@ __device__ __forceinline__ void move_slot(const Pop<T>& P, int64_t from, int64_t
 template <typename T>
 __device__ __forceinline__ void register_arrival(const Pop<T>& P, uint32_t o, const Mover<T>& m) {
     int k = atomicAdd(P.arr_cnt + m.cell, 1);
+    if (k == 0) mark_dirty(P, m.cell);
     int64_t s = P.start[m.cell];
     if (k < (int)(P.start[m.cell + 1] - s)) {
         P.arr_list[s + k] = (int32_t)o;
@@ -566,8 +567,7 @@ __device__ __forceinline__ void push_body(const Geom& g, const Pop<T>& P, int64_
             ++nmig;
         }
         if (outc[j] == kMove || outc[j] == kDrop) {
-            int k = atomicAdd(P.hole_cnt + cell, 1);
-            P.hole_list[s_start[lc] + k] = (int32_t)(s0 + j);
+            file_hole(P, cell, s_start[lc], s0 + j);
             if (outc[j] == kDrop) ++nrem;
         }
     }
@@ -661,8 +661,8 @@ __device__ __forceinline__ void push_pending_body(const Geom& g, const Pop<T>& P
 }
 
 template <typename T>
-__global__ void k_push_pending(Geom g, Pop<T> P) {
-    push_pending_body<T>(g, P, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+__global__ void k_push_pending(Geom g, const __grid_constant__ PopSet<T> S) {
+    push_pending_body<T>(g, S.p[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 // ---- injection at the x = 0 face (not in the reference) ---------------------
@@ -691,41 +691,64 @@ struct InjectParams {
 
 template <typename T>
 __global__ void k_inject(Geom g, Pop<T> P, InjectParams ip) {
+    // one thread per face cell; the warp takes its cells' particles one round
+    // at a time (warp-aggregated outbox appends, cooperative deposit)
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= g.sy * g.sz) return;
-    const int j = f / g.sz, k = f % g.sz;
-    const int c = cell_id(g, 0, j, k);
+    const int lane = threadIdx.x & 31;
+    int j = 0, k = 0, c = 0, n = 0;
     const uint64_t step = *ip.step;
-    const int n = (int)floor(ip.per_cell + u01(inj_key(ip.seed, step, (uint64_t)c, 0)));
-    for (int m = 0; m < n; ++m) {
-        const uint64_t d = 1 + 8 * (uint64_t)m;
-        double u[7];
-#pragma unroll
-        for (int t = 0; t < 7; ++t) u[t] = u01(inj_key(ip.seed, step, (uint64_t)c, d + t));
-        const double g1 = sqrt(-2.0 * log(1.0 - u[3])), th1 = 2.0 * 3.14159265358979323846 * u[4];
-        const double g2 = sqrt(-2.0 * log(1.0 - u[5])), th2 = 2.0 * 3.14159265358979323846 * u[6];
-        PState<T> p;
-        if constexpr (std::is_same<T, double>::value) {
-            p.x = g.origin[0] + u[0] * g.w[0];
-            p.y = g.origin[1] + ((double)j + u[1]) * g.w[1];
-            p.z = g.origin[2] + ((double)k + u[2]) * g.w[2];
-        } else {
-            p.x = (float)u[0]; p.y = (float)u[1]; p.z = (float)u[2];
-        }
-        p.u = (T)(ip.drift[0] + ip.vth[0] * (g1 * cos(th1)));
-        p.v = (T)(ip.drift[1] + ip.vth[1] * (g1 * sin(th1)));
-        p.w = (T)(ip.drift[2] + ip.vth[2] * (g2 * cos(th2)));
-        Mover<T> mv = {c, 0xffffffffu, p.x, p.y, p.z, p.u, p.v, p.w};
-        uint32_t o = atomicAdd(&P.ctr->outbox, 1u);
-        if (o < P.outbox_cap) {
-            P.outbox[o] = mv;
-            register_arrival(P, o, mv);
-        } else {
-            atomicAdd(&P.ctr->lost, 1u);
-        }
-        if (g.deposit) deposit_one<T>(g, c, p, P.q);
+    if (f < g.sy * g.sz) {
+        j = f / g.sz;
+        k = f - j * g.sz;
+        c = cell_id(g, 0, j, k);
+        n = (int)floor(ip.per_cell + u01(inj_key(ip.seed, step, (uint64_t)c, 0)));
     }
-    if (n) atomicAdd(&P.ctr->injected, (uint32_t)n);
+    const int nmax = __reduce_max_sync(0xffffffffu, n);
+    for (int m = 0; m < nmax; ++m) {
+        const bool has = m < n;
+        PState<T> p = {};
+        Mover<T> mv = {};
+        if (has) {
+            const uint64_t d = 1 + 8 * (uint64_t)m;
+            double u[7];
+#pragma unroll
+            for (int t = 0; t < 7; ++t) u[t] = u01(inj_key(ip.seed, step, (uint64_t)c, d + t));
+            if constexpr (std::is_same<T, double>::value) {
+                const double g1 = sqrt(-2.0 * log(1.0 - u[3])), th1 = 2.0 * 3.14159265358979323846 * u[4];
+                const double g2 = sqrt(-2.0 * log(1.0 - u[5])), th2 = 2.0 * 3.14159265358979323846 * u[6];
+                p.x = g.origin[0] + u[0] * g.w[0];
+                p.y = g.origin[1] + ((double)j + u[1]) * g.w[1];
+                p.z = g.origin[2] + ((double)k + u[2]) * g.w[2];
+                p.u = ip.drift[0] + ip.vth[0] * (g1 * cos(th1));
+                p.v = ip.drift[1] + ip.vth[1] * (g1 * sin(th1));
+                p.w = ip.drift[2] + ip.vth[2] * (g2 * cos(th2));
+            } else {
+                // the same draws, Box-Muller in FP32 (GB300's FP64
+                // transcendentals would dominate this kernel)
+                const float g1 = sqrtf(-2.f * logf(1.f - (float)u[3])), g2 = sqrtf(-2.f * logf(1.f - (float)u[5]));
+                float s1, c1, s2, c2;
+                sincospif(2.f * (float)u[4], &s1, &c1);
+                sincospif(2.f * (float)u[6], &s2, &c2);
+                p.x = (float)u[0]; p.y = (float)u[1]; p.z = (float)u[2];
+                p.u = (float)ip.drift[0] + (float)ip.vth[0] * (g1 * c1);
+                p.v = (float)ip.drift[1] + (float)ip.vth[1] * (g1 * s1);
+                p.w = (float)ip.drift[2] + (float)ip.vth[2] * (g2 * c2);
+            }
+            mv = {c, 0xffffffffu, p.x, p.y, p.z, p.u, p.v, p.w};
+        }
+        const uint32_t o = warp_append(&P.ctr->outbox, has);
+        if (has) {
+            if (o < P.outbox_cap) {
+                P.outbox[o] = mv;
+                register_arrival(P, o, mv);
+            } else {
+                atomicAdd(&P.ctr->lost, 1u);
+            }
+        }
+        if (g.deposit) warp_deposit_leavers<T>(g, has, c, p, P.q);
+    }
+    const int tot = __reduce_add_sync(0xffffffffu, n);
+    if (lane == 0 && tot) atomicAdd(&P.ctr->injected, (uint32_t)tot);
 }
 
 // ---- import: one warp per cell ------------------------------------------------
@@ -752,15 +775,18 @@ __device__ __forceinline__ void place_body(const Geom& g, const Pop<T>& P, int32
         if (pi < P.pending_cap) P.pending_out[pi] = m;
         else atomicAdd(&P.ctr->lost, 1u);
     }
-    // holes in ascending order (rank sort; hole counts are small)
-    for (int i = lane; i < nh; i += 32) {
-        const int32_t h = P.hole_list[s0 + i];
-        int r = 0;
-        for (int j = 0; j < nh; ++j) r += P.hole_list[s0 + j] < h;
-        sort_tmp[s0 + r] = h;
+    // holes in ascending order (rank sort; hole counts are small; one hole
+    // is sorted already)
+    if (nh > 1) {
+        for (int i = lane; i < nh; i += 32) {
+            const int32_t h = P.hole_list[s0 + i];
+            int r = 0;
+            for (int j = 0; j < nh; ++j) r += P.hole_list[s0 + j] < h;
+            sort_tmp[s0 + r] = h;
+        }
+        __syncwarp();
     }
-    __syncwarp();
-    const int32_t* H = sort_tmp + s0;
+    const int32_t* H = (nh > 1 ? sort_tmp : P.hole_list) + s0;
     const int m = nh < np ? nh : np;
     for (int i = lane; i < m; i += 32) write_slot(P, H[i], P.outbox[P.arr_list[s0 + i]]);
     for (int i = nh + lane; i < np; i += 32) write_slot(P, s0 + cnt + (i - nh), P.outbox[P.arr_list[s0 + i]]);
@@ -796,12 +822,20 @@ __device__ __forceinline__ void place_body(const Geom& g, const Pop<T>& P, int32
         P.count[c] = newcount;
         P.hole_cnt[c] = 0;
         P.arr_cnt[c] = 0;
+        P.dirty_flag[c] = 0;
     }
 }
 
+// The cells of the step's dirty lists (the only ones with holes or
+// arrivals), one warp per cell, warps striding over the list of population
+// blockIdx.y.
 template <typename T>
-__global__ void k_place(Geom g, Pop<T> P, int32_t* sort_tmp) {
-    place_body<T>(g, P, sort_tmp, (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5));
+__global__ void k_place(Geom g, const __grid_constant__ PopSet<T> S) {
+    const Pop<T>& P = S.p[blockIdx.y];
+    int32_t* sort_tmp = S.sort_tmp[blockIdx.y];
+    const uint32_t n = P.ctr->dirty;
+    const uint32_t w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i = w0; i < n; i += nw) place_body<T>(g, P, sort_tmp, P.dirty_list[i]);
 }
 
 // Moves this step's pending list to the next step's input (thread t0 = 0
@@ -815,9 +849,13 @@ __device__ __forceinline__ void pending_rotate_body(const Pop<T>& P, uint32_t* p
     if (t0 == 0) *pending_in_count = n;
 }
 
+// Population blockIdx.y; thread 0 of population 0 also advances the device
+// step counter (`step`, may be null), which keys the injection generator.
 template <typename T>
-__global__ void k_pending_rotate(Pop<T> P, uint32_t* pending_in_count) {
-    pending_rotate_body<T>(P, pending_in_count, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+__global__ void k_pending_rotate(const __grid_constant__ PopSet<T> S, uint64_t* step) {
+    pending_rotate_body<T>(S.p[blockIdx.y], S.pend_count[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x,
+                           gridDim.x * blockDim.x);
+    if (step && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *step += 1;
 }
 
 // ---- re-layout (cells ran out of slack) ---------------------------------------

@@ -15,7 +15,7 @@ std::mutex g_pipe_mu;
 bool g_pipe_ready[kMaxDevices] = {};
 int g_pipe_grid[kMaxDevices] = {};  // persistent CTAs of the pipelined push
 
-using PipeFn = void (*)(Geom, Pop<float>, Push32Const, int);
+using PipeFn = void (*)(Geom, PopSet<float>, Push32Set, TileMap);
 
 // The compile-time policies that are instantiated (kPipe* bit sets): the
 // step with the dipole mover, the field-gather mover with or without the
@@ -95,10 +95,9 @@ Push32Const push32_const(const Geom& g, const Pop<float>& P) {
 }
 
 // the FP32 step: the pipelined persistent push (push32_pipe.cuh), the
-// instance of the step's policies
+// instance of the step's policies, one launch for all populations of S
 template <>
-int launch_push<float>(const Geom& g, const Pop<float>& P, int mode, cudaStream_t st) {
-    if (P.capacity <= 0) return 0;
+int launch_push<float>(const Geom& g, const PopSet<float>& S, int mode, cudaStream_t st) {
     int f = g.deposit ? kPipeDeposit : 0;
     if (mode == 0) {
         f |= kPipeStep;
@@ -108,25 +107,36 @@ int launch_push<float>(const Geom& g, const Pop<float>& P, int mode, cudaStream_
         return 0;  // nothing to deposit
     }
     PipeFn fn = pipe_kernel(f);
-    if (!fn) return 0;
+    if (!fn || S.n <= 0) return 0;
+    TileMap tm{};
+    tm.n = S.n;
+    Push32Set pcs{};
+    for (int i = 0; i < S.n; ++i) {
+        tm.first[i + 1] = tm.first[i] + (int)((S.p[i].capacity + kTileSlots - 1) / kTileSlots);
+        pcs.c[i] = push32_const(g, S.p[i]);
+    }
+    const int tiles = tm.first[S.n];
+    if (tiles <= 0) return 0;
     int dev = 0;
     cudaGetDevice(&dev);
-    const int64_t tiles = (P.capacity + kTileSlots - 1) / kTileSlots;
     int grid = g_pipe_grid[dev];
     if (grid <= 0) grid = 1;  // init_push32 did not run on this device: the launch fails (no shared-memory opt-in)
-    if (grid > tiles) grid = (int)tiles;
-    fn<<<grid, kPipeThreads, pipe_smem_bytes<kPipeStages>(), st>>>(g, P, push32_const(g, P), (int)tiles);
+    if (grid > tiles) grid = tiles;
+    fn<<<grid, kPipeThreads, pipe_smem_bytes<kPipeStages>(), st>>>(g, S, pcs, tm);
     return 1;
 }
 
 template <>
-int launch_push_pending<float>(const Geom& g, const Pop<float>& P, cudaStream_t st) {
-    k_push_pending32<<<152, 128, 0, st>>>(g, P, push32_const(g, P));
+int launch_push_pending<float>(const Geom& g, const PopSet<float>& S, cudaStream_t st) {
+    if (S.n <= 0) return 0;
+    Push32Set pcs{};
+    for (int i = 0; i < S.n; ++i) pcs.c[i] = push32_const(g, S.p[i]);
+    k_push_pending32<<<dim3(152, S.n), 128, 0, st>>>(g, S, pcs);
     return 1;
 }
 
 int launch_cell_coef(const Geom& g, float* coef, cudaStream_t st) {
-    const int64_t n = (int64_t)g.sx * g.sy * g.sz;
+    const int64_t n = (int64_t)g.sx * g.sy * g.sz * 6;
     int64_t blocks = (n + 127) / 128;
     if (blocks > 152 * 16) blocks = 152 * 16;
     const double scale = (g.flags & 2u) ? 1.0 / g.vol : 1.0;
@@ -149,7 +159,7 @@ int launch_push_pending_batch<float>(const PopJob<float>* jobs, int njobs, cudaS
 }
 
 int launch_cell_coef_batch(const InstJob* inst, int ninst, int64_t max_cells, cudaStream_t st) {
-    int64_t blocks = (max_cells + 127) / 128;
+    int64_t blocks = (max_cells * 6 + 127) / 128;
     if (blocks > 64) blocks = 64;
     k_cell_coef_batch<<<dim3((unsigned)blocks, ninst), 128, 0, st>>>(inst);
     return 1;
@@ -163,8 +173,8 @@ template int launch_batch_end<float>(const PopJob<float>*, const InstJob*, int, 
 template int launch_batch_status<float>(const PopJob<float>*, int, JobStatus*, cudaStream_t);
 template int launch_inject<float>(const Geom&, const Pop<float>&, double, const double*, const double*, uint64_t,
                                   const uint64_t*, cudaStream_t);
-template int launch_place<float>(const Geom&, const Pop<float>&, int32_t*, cudaStream_t);
-template int launch_pending_rotate<float>(const Pop<float>&, uint32_t*, cudaStream_t);
+template int launch_place<float>(const Geom&, const PopSet<float>&, cudaStream_t);
+template int launch_pending_rotate<float>(const PopSet<float>&, uint64_t*, cudaStream_t);
 template int launch_relayout<float>(const Pop<float>&, const Pop<float>&, int, int32_t*, cudaStream_t);
 template int launch_pending_count<float>(const Pop<float>&, int32_t*, cudaStream_t);
 }  // namespace ipg

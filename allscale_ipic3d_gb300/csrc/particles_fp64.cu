@@ -5,17 +5,17 @@
 
 namespace ipg {
 template <>
-int launch_push<double>(const Geom& g, const Pop<double>& P, int mode, cudaStream_t st) {
-    return launch_push_generic<double>(g, P, mode, st);
+int launch_push<double>(const Geom& g, const PopSet<double>& S, int mode, cudaStream_t st) {
+    return launch_push_generic<double>(g, S, mode, st);
 }
 template <>
-int launch_push_pending<double>(const Geom& g, const Pop<double>& P, cudaStream_t st) {
-    return launch_push_pending_generic<double>(g, P, st);
+int launch_push_pending<double>(const Geom& g, const PopSet<double>& S, cudaStream_t st) {
+    return launch_push_pending_generic<double>(g, S, st);
 }
 template int launch_inject<double>(const Geom&, const Pop<double>&, double, const double*, const double*, uint64_t,
                                    const uint64_t*, cudaStream_t);
-template int launch_place<double>(const Geom&, const Pop<double>&, int32_t*, cudaStream_t);
-template int launch_pending_rotate<double>(const Pop<double>&, uint32_t*, cudaStream_t);
+template int launch_place<double>(const Geom&, const PopSet<double>&, cudaStream_t);
+template int launch_pending_rotate<double>(const PopSet<double>&, uint64_t*, cudaStream_t);
 template int launch_relayout<double>(const Pop<double>&, const Pop<double>&, int, int32_t*, cudaStream_t);
 template int launch_pending_count<double>(const Pop<double>&, int32_t*, cudaStream_t);
 

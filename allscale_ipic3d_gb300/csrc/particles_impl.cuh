@@ -8,22 +8,28 @@
 namespace ipg {
 
 template <typename T>
-int launch_push(const Geom& g, const Pop<T>& P, int mode, cudaStream_t st);
+int launch_push(const Geom& g, const PopSet<T>& S, int mode, cudaStream_t st);
 template <typename T>
-int launch_push_pending(const Geom& g, const Pop<T>& P, cudaStream_t st);
+int launch_push_pending(const Geom& g, const PopSet<T>& S, cudaStream_t st);
 
 // generic versions (the FP64 path); particles_fp32.cu specialises both
 template <typename T>
-int launch_push_generic(const Geom& g, const Pop<T>& P, int mode, cudaStream_t st) {
-    if (P.capacity <= 0) return 0;
-    const int64_t blocks = (P.capacity + kSlotsPerCta - 1) / kSlotsPerCta;
-    k_push<T><<<(unsigned)blocks, kPushThreads, 0, st>>>(g, P, mode);
-    return 1;
+int launch_push_generic(const Geom& g, const PopSet<T>& S, int mode, cudaStream_t st) {
+    int n = 0;
+    for (int i = 0; i < S.n; ++i) {
+        const Pop<T>& P = S.p[i];
+        if (P.capacity <= 0) continue;
+        const int64_t blocks = (P.capacity + kSlotsPerCta - 1) / kSlotsPerCta;
+        k_push<T><<<(unsigned)blocks, kPushThreads, 0, st>>>(g, P, mode);
+        ++n;
+    }
+    return n;
 }
 
 template <typename T>
-int launch_push_pending_generic(const Geom& g, const Pop<T>& P, cudaStream_t st) {
-    k_push_pending<T><<<152, 128, 0, st>>>(g, P);
+int launch_push_pending_generic(const Geom& g, const PopSet<T>& S, cudaStream_t st) {
+    if (S.n <= 0) return 0;
+    k_push_pending<T><<<dim3(152, S.n), 128, 0, st>>>(g, S);
     return 1;
 }
 
@@ -44,15 +50,19 @@ int launch_inject(const Geom& g, const Pop<T>& P, double per_cell, const double 
 }
 
 template <typename T>
-int launch_place(const Geom& g, const Pop<T>& P, int32_t* sort_tmp, cudaStream_t st) {
-    const int64_t threads = (int64_t)g.ncells * 32;
-    k_place<T><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(g, P, sort_tmp);
+int launch_place(const Geom& g, const PopSet<T>& S, cudaStream_t st) {
+    if (S.n <= 0) return 0;
+    // a warp per dirty cell, at most one per cell; 8 warps per block
+    int64_t blocks = ((int64_t)g.ncells + 7) / 8;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    k_place<T><<<dim3((unsigned)blocks, S.n), 256, 0, st>>>(g, S);
     return 1;
 }
 
 template <typename T>
-int launch_pending_rotate(const Pop<T>& P, uint32_t* pending_in_count, cudaStream_t st) {
-    k_pending_rotate<T><<<152, 256, 0, st>>>(P, pending_in_count);
+int launch_pending_rotate(const PopSet<T>& S, uint64_t* step, cudaStream_t st) {
+    if (S.n <= 0) return 0;
+    k_pending_rotate<T><<<dim3(152, S.n), 256, 0, st>>>(S, step);
     return 1;
 }
 
@@ -115,7 +125,7 @@ __global__ void k_batch_begin(const PopJob<T>* __restrict__ jobs, int njobs, con
         for (int64_t j = t0; j < njobs; j += stride) {
             StepCounters* c = jobs[j].P.ctr;
             c->outbox = 0; c->pending_out = 0; c->deferred = 0;
-            c->removed = 0; c->migrated = 0; c->injected = 0;
+            c->removed = 0; c->migrated = 0; c->injected = 0; c->dirty = 0;
         }
         if (t0 == 0) *flagged = 0;
         return;

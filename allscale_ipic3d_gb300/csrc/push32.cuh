@@ -257,8 +257,7 @@ __device__ __forceinline__ void push32_body(const Geom& g, const Pop<float>& P, 
             ++nmig;
         }
         if (outc[j] == kMove || outc[j] == kDrop) {
-            const int k = atomicAdd(P.hole_cnt + cell, 1);
-            P.hole_list[s_start[lc] + k] = (int32_t)(s0 + j);
+            file_hole(P, cell, s_start[lc], s0 + j);
             if (outc[j] == kDrop) ++nrem;
         }
     }
@@ -376,34 +375,54 @@ __device__ __forceinline__ void push_pending32_body(const Geom& g, const Pop<flo
     }
 }
 
-__global__ void k_push_pending32(Geom g, Pop<float> P, Push32Const pc) {
-    push_pending32_body(g, P, pc, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+// population blockIdx.y of the set, pc.c[blockIdx.y] its push constants
+__global__ void k_push_pending32(Geom g, const __grid_constant__ PopSet<float> S,
+                                 const __grid_constant__ Push32Set pc) {
+    push_pending32_body(g, S.p[blockIdx.y], pc.c[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x,
+                        gridDim.x * blockDim.x);
 }
 
-// Cell coefficients of the trilinear field polynomial (FP64 sums, stored
-// FP32): coefficient m of component q (Ex, Ey, Ez, Bx, By, Bz) of cell c at
-// coef[c * 48 + q * 8 + m]; monomials m = 1, x, y, z, xy, xz, yz, xyz.
+// Cell coefficients of the trilinear field polynomial, stored FP32:
+// coefficient m of component q (Ex, Ey, Ez, Bx, By, Bz) of cell c at
+// coef[c * 48 + q * 8 + m]; monomials m = 1, x, y, z, xy, xz, yz, xyz. One
+// thread per (cell, component): the seven corner differences from corner
+// (0,0,0) are taken in FP64 and rounded once, the mixed terms are then FP32
+// sums of those differences (a few FP64 operations per coefficient instead
+// of an FP64 polynomial: GB300's FP64 rate is a small fraction of FP32's).
 __device__ __forceinline__ void cell_coef_body(const double* __restrict__ field, int sx, int sy, int sz, double scale,
                                                float* coef, int64_t t0, int64_t stride) {
-    const int64_t total = (int64_t)sx * sy * sz;
-    for (int64_t c = t0; c < total; c += stride) {
-        const int z = (int)(c % sz), y = (int)((c / sz) % sy), x = (int)(c / ((int64_t)sy * sz));
-        for (int q = 0; q < 6; ++q) {
-            double f[2][2][2];
-            for (int i = 0; i < 2; ++i)
-                for (int j = 0; j < 2; ++j)
-                    for (int k = 0; k < 2; ++k)
-                        f[i][j][k] = field[9 * (((int64_t)(x + i + 1) * (sy + 3) + (y + j + 1)) * (sz + 3) + (z + k + 1)) + q];
-            const double m0 = f[0][0][0];
-            const double mx = f[1][0][0] - f[0][0][0], my = f[0][1][0] - f[0][0][0], mz = f[0][0][1] - f[0][0][0];
-            const double mxy = f[1][1][0] - f[1][0][0] - f[0][1][0] + f[0][0][0];
-            const double mxz = f[1][0][1] - f[1][0][0] - f[0][0][1] + f[0][0][0];
-            const double myz = f[0][1][1] - f[0][1][0] - f[0][0][1] + f[0][0][0];
-            const double mxyz = f[1][1][1] - f[1][1][0] - f[1][0][1] - f[0][1][1] + f[1][0][0] + f[0][1][0] +
-                                f[0][0][1] - f[0][0][0];
-            const double m[8] = {m0, mx, my, mz, mxy, mxz, myz, mxyz};
-            for (int k = 0; k < 8; ++k) coef[c * 48 + q * 8 + k] = (float)(m[k] * scale);
+    const int64_t total = (int64_t)sx * sy * sz * 6;
+    const float fs = (float)scale;
+    for (int64_t t = t0; t < total; t += stride) {
+        const int q = (int)(t % 6);
+        const int64_t c = t / 6;
+        int x, y, z;
+        split3(c, sy, sz, x, y, z);
+        const int64_t sy3 = sy + 3, sz3 = sz + 3;
+        const double* f0 = field + 9 * (((int64_t)(x + 1) * sy3 + (y + 1)) * sz3 + (z + 1)) + q;
+        const int64_t dx = 9 * sy3 * sz3, dy = 9 * sz3, dz = 9;
+        const double f000 = __ldg(f0);
+        const float d100 = (float)(__ldg(f0 + dx) - f000), d010 = (float)(__ldg(f0 + dy) - f000);
+        const float d001 = (float)(__ldg(f0 + dz) - f000), d110 = (float)(__ldg(f0 + dx + dy) - f000);
+        const float d101 = (float)(__ldg(f0 + dx + dz) - f000), d011 = (float)(__ldg(f0 + dy + dz) - f000);
+        const float d111 = (float)(__ldg(f0 + dx + dy + dz) - f000);
+        float m[8];
+        m[0] = (float)f000;
+        m[1] = d100;
+        m[2] = d010;
+        m[3] = d001;
+        m[4] = d110 - d100 - d010;
+        m[5] = d101 - d100 - d001;
+        m[6] = d011 - d010 - d001;
+        m[7] = ((d111 - d110) - (d101 + d011)) + (d100 + d010 + d001);
+        if (scale != 1.0) {
+            m[0] = (float)(f000 * scale);
+#pragma unroll
+            for (int k = 1; k < 8; ++k) m[k] *= fs;
         }
+        float4* out = reinterpret_cast<float4*>(coef + c * 48 + q * 8);
+        out[0] = make_float4(m[0], m[1], m[2], m[3]);
+        out[1] = make_float4(m[4], m[5], m[6], m[7]);
     }
 }
 

@@ -138,6 +138,7 @@ struct PipeSmem {
     uint64_t full[kStages];               // the stage's copies landed
     uint64_t empty[kStages];              // the compute warps are done with the stage
     int2 desc[kStages];                   // (first cell, number of cells) of the stage's tile
+    int pop[kStages];                     // population of the stage's tile
     int next_item[kStages];               // item counter of the stage's tile
     int abort;                            // a wait expired: every warp stops
 };
@@ -454,8 +455,7 @@ __device__ __forceinline__ void leave_and_hole(const Geom& g, const Pop<float>& 
         if (deposit) deposit_leavers32(g, lb, nx, ny, nz, p, P.q);
     }
     if (outcome == kMove || outcome == kDrop) {
-        const int k = atomicAdd(P.hole_cnt + cell, 1);
-        P.hole_list[cstart + k] = slot;
+        file_hole(P, cell, cstart, slot);
         if (outcome == kDrop) ++nrem;
     }
 }
@@ -653,16 +653,42 @@ __device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& 
     }
 }
 
-// The persistent kernel: CTA b pushes tiles b, b + G, b + 2G, ... of one
-// population (G = gridDim.x) through kStages stages.
+// Tile t of a launch over several populations: population i holds tiles
+// [first[i], first[i + 1]).
+struct TileMap {
+    int first[kSetPops + 1];
+    int n;  // populations
+};
+
+__device__ __forceinline__ int tile_pop(const TileMap& tm, int t) {
+    int i = 0;
+    while (i + 1 < tm.n && t >= tm.first[i + 1]) ++i;
+    return i;
+}
+
+// Adds a compute warp's migration / removal counts to population counters.
+__device__ __forceinline__ void flush_counts(StepCounters* ctr, uint32_t& nmig, uint32_t& nrem) {
+    const uint32_t m = __reduce_add_sync(0xffffffffu, nmig), r = __reduce_add_sync(0xffffffffu, nrem);
+    if ((threadIdx.x & 31) == 0) {
+        if (m) atomicAdd(&ctr->migrated, m);
+        if (r) atomicAdd(&ctr->removed, r);
+    }
+    nmig = nrem = 0;
+}
+
+// The persistent kernel: CTA b pushes tiles b, b + G, b + 2G, ... (G =
+// gridDim.x) of the populations of S, numbered through tm, with kStages
+// shared-memory stages in flight.
 template <int kStages, int kMinBlocks, int kF>
 __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
-    k_push32_pipe(Geom g, Pop<float> P, Push32Const pc, int ntiles) {
+    k_push32_pipe(Geom g, const __grid_constant__ PopSet<float> S, const __grid_constant__ Push32Set pcs,
+                  const __grid_constant__ TileMap tm) {
     constexpr bool kStep = (kF & kPipeStep) != 0;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     PipeSmem<kStages>& sm = *reinterpret_cast<PipeSmem<kStages>*>(smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int G = gridDim.x;
+    const int ntiles = tm.first[tm.n];
     if (tid == 0) {
         for (int s = 0; s < kStages; ++s) {
             mbar_init(&sm.full[s], 1);
@@ -678,18 +704,26 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
         // ---- producer ----
         if (lane != 0) return;
         const float* coef = (kF & kPipeGather) ? g.cellcoef : nullptr;
+        auto load_desc = [&](int t) {
+            const int pi = tile_pop(tm, t);
+            return __ldg(S.p[pi].cta_cells + (t - tm.first[pi]));
+        };
+        auto issue = [&](int t, int s, int2 d) {
+            const int pi = tile_pop(tm, t);
+            sm.desc[s] = d;
+            sm.pop[s] = pi;
+            sm.next_item[s] = 0;
+            issue_tile(S.p[pi], coef, t - tm.first[pi], d, sm.stage[s], &sm.full[s]);
+        };
         int issued = 0;  // tiles of this CTA whose copies were issued
         for (int s = 0; s < kStages; ++s) {
             const int t = blockIdx.x + s * G;
             if (t >= ntiles) break;
-            const int2 d = __ldg(P.cta_cells + t);
-            sm.desc[s] = d;
-            sm.next_item[s] = 0;
-            issue_tile(P, coef, t, d, sm.stage[s], &sm.full[s]);
+            issue(t, s, load_desc(t));
             ++issued;
         }
         int2 next_desc = make_int2(0, 0);
-        if (blockIdx.x + kStages * G < ntiles) next_desc = __ldg(P.cta_cells + blockIdx.x + kStages * G);
+        if (blockIdx.x + kStages * G < ntiles) next_desc = load_desc(blockIdx.x + kStages * G);
         bool failed = false;
         int k = 0;
         for (int t = blockIdx.x; t < ntiles; t += G, ++k) {
@@ -702,7 +736,8 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
             // stored their stayers themselves
             const bool store = kStep && sm.desc[s].y > kItemMaxCells;
             if (store) {
-                const TileCopy c = tile_copy(P, t, sm.desc[s]);
+                const Pop<float>& P = S.p[sm.pop[s]];
+                const TileCopy c = tile_copy(P, t - tm.first[sm.pop[s]], sm.desc[s]);
                 float* const arr[6] = {P.x, P.y, P.z, P.u, P.v, P.w};
 #pragma unroll
                 for (int a = 0; a < 6; ++a) bulk_store(arr[a] + c.base, sm.stage[s].s[a], c.slot_bytes);
@@ -712,15 +747,13 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
             if (tn < ntiles) {
                 if (store) bulk_wait_read_all();  // the stores have read the stage
                 const int2 d = next_desc;
-                if (tn + G < ntiles) next_desc = __ldg(P.cta_cells + tn + G);
-                sm.desc[s] = d;
-                sm.next_item[s] = 0;
-                issue_tile(P, coef, tn, d, sm.stage[s], &sm.full[s]);
+                if (tn + G < ntiles) next_desc = load_desc(tn + G);
+                issue(tn, s, d);
                 ++issued;
             }
         }
         if (failed) {
-            if (atomicExch(&sm.abort, 1) == 0) atomicAdd(&P.ctr->timeouts, 1u);
+            if (atomicExch(&sm.abort, 1) == 0) atomicAdd(&S.p[0].ctr->timeouts, 1u);
             // copies still in flight land before the CTA leaves
             const int never = 0;
             for (int kk = k; kk < issued; ++kk)
@@ -732,25 +765,27 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
 
     // ---- compute warps ----
     uint32_t nmig = 0, nrem = 0;
+    int cur = -1;  // population of the counts held
     int k = 0;
     for (int t = blockIdx.x; t < ntiles; t += G, ++k) {
         const int s = k % kStages;
         // warp-uniform: every lane polls the same barrier
         if (!__all_sync(0xffffffffu, mbar_wait(&sm.full[s], (uint32_t)(k / kStages) & 1u, abort))) {
-            if (lane == 0 && atomicExch(&sm.abort, 1) == 0) atomicAdd(&P.ctr->timeouts, 1u);
+            if (lane == 0 && atomicExch(&sm.abort, 1) == 0) atomicAdd(&S.p[0].ctr->timeouts, 1u);
             break;
         }
-        push_tile_warp<kF>(g, P, pc, t, sm.desc[s], sm.stage[s], &sm.next_item[s], nmig, nrem);
+        const int pi = sm.pop[s];
+        if (pi != cur) {
+            if (cur >= 0) flush_counts(S.p[cur].ctr, nmig, nrem);
+            cur = pi;
+        }
+        push_tile_warp<kF>(g, S.p[pi], pcs.c[pi], t - tm.first[pi], sm.desc[s], sm.stage[s], &sm.next_item[s],
+                           nmig, nrem);
         fence_proxy_async_smem();  // this warp's writes to the stage, before the bulk stores read it
         __syncwarp();
         if (lane == 0) mbar_arrive(&sm.empty[s]);
     }
-    nmig = __reduce_add_sync(0xffffffffu, nmig);
-    nrem = __reduce_add_sync(0xffffffffu, nrem);
-    if (lane == 0) {
-        if (nmig) atomicAdd(&P.ctr->migrated, nmig);
-        if (nrem) atomicAdd(&P.ctr->removed, nrem);
-    }
+    if (cur >= 0) flush_counts(S.p[cur].ctr, nmig, nrem);
 }
 
 }  // namespace ipg
