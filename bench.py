@@ -143,7 +143,7 @@ def measured_peak():
 
 def profiled_traffic(precision):
     """DRAM bytes per push launch from the committed ncu summary, if any."""
-    name = os.path.join(ROOT, "profiles", "k_push32_dipole32.md" if precision == "fp32" else "k_push64_dipole32.md")
+    name = os.path.join(ROOT, "profiles", "k_push32_pipe_dipole32.md" if precision == "fp32" else "k_push64_dipole32.md")
     if not os.path.exists(name):
         return None
     for line in open(name):
@@ -187,10 +187,11 @@ class _Null:
 
 
 def push_roofline(sim, precision, nsteps, props, pops):
-    """Live CUDA-event times of the push phase over `nsteps` eager steps (the
-    phase runs one launch per species population, `pops` launches of equal
-    size); the push kernel's algorithmic bytes per launch over its average
-    launch duration. Algorithmic bytes per launch: the particles' state read
+    """Live CUDA-event times of the push phase over `nsteps` eager steps; the
+    push kernel's algorithmic bytes per launch over its average launch
+    duration. The FP32 push is one launch per step for all `pops` species
+    populations; the FP64 push one launch per population (`pops` launches of
+    equal size). Algorithmic bytes per population: the particles' state read
     and written once (12 x 4 B FP32, 12 x 8 B FP64), the per-cell field
     coefficients read once (FP32: 48 floats per cell) or the node E, B read
     once (FP64: 48 B per node), and the 4 FP64 node moments written once
@@ -200,20 +201,23 @@ def push_roofline(sim, precision, nsteps, props, pops):
     prof = sim.profile_read(reset=True)
     sim.profile(False)
     push = prof["push"]
-    ms_per = push["ms"] / max(push["launches"], 1) / pops
-    parts = push["particles"] / max(push["launches"], 1) / pops
+    per_launch_pops = pops if precision == "fp32" else 1
+    launches_per_step = 1 if precision == "fp32" else pops
+    ms_per = push["ms"] / max(push["launches"], 1) / launches_per_step
+    parts = push["particles"] / max(push["launches"], 1) / launches_per_step
     elem = 4 if precision == "fp32" else 8
     nodes = (props.size[0] + 1) * (props.size[1] + 1) * (props.size[2] + 1)
     if precision == "fp32":
-        bytes_per = parts * 12 * elem + props.ncells * 48 * 4 + nodes * 32
+        bytes_per = parts * 12 * elem + per_launch_pops * (props.ncells * 48 * 4 + nodes * 32)
     else:
         bytes_per = parts * 12 * elem + nodes * (48 + 32)
     peak, src = measured_peak()
     achieved = bytes_per / (ms_per * 1e-3) / 1e9
     phases = {k: round(v["ms"] / max(v["launches"], 1), 5) for k, v in prof.items() if v["launches"]}
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": profiled_traffic(precision), "kernel": "ipg::k_push32<3>" if elem == 4 else "ipg::k_push<double>",
-            "bytes_per_launch": bytes_per, "ms_per_launch": ms_per, "launches_per_step": pops,
+            "traffic": profiled_traffic(precision),
+            "kernel": "ipg::k_push32_pipe<3, 2, 15>" if elem == 4 else "ipg::k_push<double>",
+            "bytes_per_launch": bytes_per, "ms_per_launch": ms_per, "launches_per_step": launches_per_step,
             "peak_source": src + ", burst copy", "phase_ms_per_step": phases}
 
 
