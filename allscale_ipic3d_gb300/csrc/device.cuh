@@ -46,7 +46,7 @@ struct Geom {
     double* bcfield;        // (s+2)^3 x 3
     double* J;              // (s+1)^3 x 3 raw sums during the deposit
     double* rho;            // (s+1)^3
-    const float4* node32;   // (s+3)^3 x 2 float4: {Ex,Ey,Ez,0},{Bx,By,Bz,0} (FP32 gather)
+    float4* node32;         // (s+3)^3 x 2 float4: {Ex,Ey,Ez,0},{Bx,By,Bz,0} (FP32 path, else null)
     const float* cellcoef;  // s^3 x 48: trilinear polynomial of E, B per cell (FP32 push)
 };
 

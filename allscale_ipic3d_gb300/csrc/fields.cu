@@ -49,6 +49,7 @@ struct SolverArgs {
     double dt, c;
     double wx, wy, wz;
     double iwx, iwy, iwz;  // 1 / w (the multiplying solvers)
+    float4* n32;          // FP32 node copy {Ex,Ey,Ez,0},{Bx,By,Bz,0} kept current (FP32 path), or null
     double* field;        // (s+3)^3 x 9
     double* bc;           // (s+2)^3 x 3
     const double* J;      // (s+1)^3 x 3
@@ -85,6 +86,7 @@ __device__ __forceinline__ void leapfrog_e_body(SolverArgs A, int64_t t0, int64_
                               J[1]);
         E[2] = E[2] + A.dt * (c2 * (over<kMul>(B0[1] - Bxm[1], A.wx, A.iwx) - over<kMul>(B0[0] - Bym[0], A.wy, A.iwy)) -
                               J[2]);
+        if (A.n32) A.n32[2 * fidx(nf, x, y, z)] = make_float4((float)E[0], (float)E[1], (float)E[2], 0.f);
     }
 }
 
@@ -172,6 +174,7 @@ __device__ __forceinline__ void forward_e_body(SolverArgs A, int64_t t0, int64_t
         E[0] += (A.c * cx - J[0]) * A.dt;
         E[1] += (A.c * cy - J[1]) * A.dt;
         E[2] += (A.c * cz - J[2]) * A.dt;
+        if (A.n32) A.n32[2 * fidx(A.s + 3, x, y, z)] = make_float4((float)E[0], (float)E[1], (float)E[2], 0.f);
     }
 }
 
@@ -208,6 +211,7 @@ __device__ __forceinline__ void interp_c2n_body(SolverArgs A, int64_t t0, int64_
                 }
         double* B = A.field + 9 * fidx(A.s + 3, x, y, z) + 3;
         B[0] = .125 * a0; B[1] = .125 * a1; B[2] = .125 * a2;
+        if (A.n32) A.n32[2 * fidx(A.s + 3, x, y, z) + 1] = make_float4((float)B[0], (float)B[1], (float)B[2], 0.f);
     }
 }
 
@@ -268,6 +272,7 @@ __host__ __device__ inline SolverArgs solver_args(const Geom& g) {
     A.field = g.field;
     A.bc = g.bcfield;
     A.J = g.J;
+    A.n32 = g.node32;
     return A;
 }
 

@@ -675,7 +675,7 @@ void refresh_geom(ipic3d_ctx* ctx) {
     g.bcfield = ctx->bcfield;
     g.J = ctx->J;
     g.rho = ctx->rho;
-    g.node32 = ctx->node32;
+    g.node32 = ctx->fp32 ? ctx->node32 : nullptr;  // the FP32 gather's node copy
     g.cellcoef = ctx->cellcoef;
 }
 
@@ -1104,7 +1104,8 @@ int ipic3d_gpu_upload_fields(ipic3d_ctx* ctx, const double* field, const double*
         // a supplied J is used as it is while the projector is off
     }
     if (field && ctx->fp32) {
-        int n = launch_cell_coef(ctx->g, ctx->cellcoef, st);
+        int n = launch_node32(ctx->g, ctx->node32, st);
+        n += launch_cell_coef(ctx->g, ctx->cellcoef, st);
         if ((rc = check_launch(ctx, n))) return rc;
     }
     CU(cudaStreamSynchronize(st));

@@ -136,11 +136,18 @@ int launch_push_pending<float>(const Geom& g, const PopSet<float>& S, cudaStream
 }
 
 int launch_cell_coef(const Geom& g, float* coef, cudaStream_t st) {
+    const float scale = (g.flags & 2u) ? (float)(1.0 / g.vol) : 1.0f;
+    if (g.node32) {
+        const int64_t n = (int64_t)g.sx * g.sy * g.sz;
+        int64_t blocks = (n + 127) / 128;
+        if (blocks > 152 * 16) blocks = 152 * 16;
+        k_cell_coef32<<<(unsigned)blocks, 128, 0, st>>>(g.node32, g.sx, g.sy, g.sz, scale, coef);
+        return 1;
+    }
     const int64_t n = (int64_t)g.sx * g.sy * g.sz * 6;
     int64_t blocks = (n + 127) / 128;
     if (blocks > 152 * 16) blocks = 152 * 16;
-    const double scale = (g.flags & 2u) ? 1.0 / g.vol : 1.0;
-    k_cell_coef<<<(unsigned)blocks, 128, 0, st>>>(g.field, g.sx, g.sy, g.sz, scale, coef);
+    k_cell_coef<<<(unsigned)blocks, 128, 0, st>>>(g.field, g.sx, g.sy, g.sz, (g.flags & 2u) ? 1.0 / g.vol : 1.0, coef);
     return 1;
 }
 

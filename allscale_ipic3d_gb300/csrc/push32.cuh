@@ -431,6 +431,41 @@ __global__ void k_cell_coef(const double* __restrict__ field, int sx, int sy, in
                    (int64_t)gridDim.x * blockDim.x);
 }
 
+// The same coefficients from the FP32 node copy (n32: {Ex,Ey,Ez,0},
+// {Bx,By,Bz,0} per node of the (s+3)^3 field grid), one thread per cell:
+// sixteen 16-byte loads and FP32 corner differences.
+__global__ void k_cell_coef32(const float4* __restrict__ n32, int sx, int sy, int sz, float scale, float* coef) {
+    const int64_t total = (int64_t)sx * sy * sz;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < total;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        int x, y, z;
+        split3(c, sy, sz, x, y, z);
+        const int64_t sy3 = sy + 3, sz3 = sz + 3;
+        const int64_t n0 = ((int64_t)(x + 1) * sy3 + (y + 1)) * sz3 + (z + 1);
+        const int64_t dx = sy3 * sz3, dy = sz3;
+        float f[8][6];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int64_t n = n0 + ((k & 1) ? dx : 0) + ((k & 2) ? dy : 0) + ((k & 4) ? 1 : 0);
+            const float4 e = __ldg(n32 + 2 * n), b = __ldg(n32 + 2 * n + 1);
+            f[k][0] = e.x; f[k][1] = e.y; f[k][2] = e.z;
+            f[k][3] = b.x; f[k][4] = b.y; f[k][5] = b.z;
+        }
+        float4* out = reinterpret_cast<float4*>(coef + c * 48);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            // corner k = i + 2 j + 4 l at (x + i, y + j, z + l)
+            const float f000 = f[0][q], d100 = f[1][q] - f000, d010 = f[2][q] - f000, d001 = f[4][q] - f000;
+            const float d110 = f[3][q] - f000, d101 = f[5][q] - f000, d011 = f[6][q] - f000, d111 = f[7][q] - f000;
+            const float m1 = d100, m2 = d010, m3 = d001;
+            const float m4 = d110 - d100 - d010, m5 = d101 - d100 - d001, m6 = d011 - d010 - d001;
+            const float m7 = ((d111 - d110) - (d101 + d011)) + (d100 + d010 + d001);
+            out[2 * q] = make_float4(f000 * scale, m1 * scale, m2 * scale, m3 * scale);
+            out[2 * q + 1] = make_float4(m4 * scale, m5 * scale, m6 * scale, m7 * scale);
+        }
+    }
+}
+
 // ---- batched ensemble (tables as in particles_impl.cuh) ---------------------
 template <int kMinBlocks>
 __global__ void __launch_bounds__(kPushThreads, kMinBlocks)
