@@ -12,11 +12,11 @@
 // the warps: a warp waits only for the data it works on.
 //
 // Work inside a tile. A tile whose cells are large (at most 32 cells) is cut
-// into items: the occupied slots of one cell, at most 128 at a time. Warps
+// into items: the occupied slots of one cell, at most 256 at a time. Warps
 // take items from a per-stage counter; lane l pushes the item's particles
-// l, l + 32, ... and adds their cloud-in-cell moments to its accumulators,
-// so a warp sums one cell and flushes it once (transpose-reduction across
-// the lanes). A tile of many small cells goes thread-per-4-slots instead:
+// l, l + 32, ..., then a second pass over the stayers adds their cloud-in-
+// cell moments to the lane's accumulators, so a warp sums one cell and
+// flushes it once (transpose-reduction across the lanes). A tile of many small cells goes thread-per-4-slots instead:
 // warp w pushes slots [128 w, 128 w + 128) and flushes its per-cell runs of
 // lanes through a shared-memory tile.
 //
@@ -111,9 +111,9 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
 
 // ---- shared-memory layout ------------------------------------------------------
 constexpr int kTileSlots = kSlotsPerCta;  // 1024 slots per tile (the cta_cells table's unit)
-// 7 compute warps + the producer: 2 CTAs = 16 warps per SM, 4 per scheduler,
-// which leaves each thread 128 registers
-constexpr int kComputeWarps = 7;
+// 11 compute warps + the producer: 2 CTAs = 24 warps per SM, 6 per
+// scheduler, 80 registers per thread
+constexpr int kComputeWarps = 11;
 constexpr int kComputeThreads = kComputeWarps * 32;
 constexpr int kPipeThreads = kComputeThreads + 32;  // + the producer warp
 constexpr int kSlotWarps = kTileSlots / 128;        // slot mode: 128-slot slices of a tile
@@ -461,41 +461,64 @@ __device__ __forceinline__ void leave_and_hole(const Geom& g, const Pop<float>& 
 }
 
 // Item mode: the warp pushes particles [a, b) (tile-local slots, b - a <=
-// kItemSlots) of cell `cell`, lane l taking a + l, a + l + 32, ...; stayers
-// go back to HBM with coalesced stores, the cell's moments are flushed once.
-// `coef` points at the cell's 48 field coefficients (shared memory).
+// kItemSlots) of cell `cell`, lane l taking a + l, a + l + 32, ... A first
+// pass moves them: stayers go back to HBM with coalesced stores (and to the
+// stage for the second pass), the slots of leavers and drops are marked
+// (NaN position). The second pass sums the stayers' cloud-in-cell moments
+// and flushes the cell once. Keeping the 32 moment sums out of the mover
+// keeps the register count low enough for 6 warps per scheduler. `coef`
+// points at the cell's 48 field coefficients (shared memory).
 template <int kF>
 __device__ __forceinline__ void push_item(const Geom& g, const Pop<float>& P, const Push32Const& pc,
-                                          const PipeStage& st, const float* coef, int base, int cell, int cstart,
-                                          int a, int b, uint32_t& nmig, uint32_t& nrem) {
+                                          PipeStage& st, const float* coef, int base, int cell, int cstart, int a,
+                                          int b, uint32_t& nmig, uint32_t& nrem) {
     constexpr bool kStep = (kF & kPipeStep) != 0, kDep = (kF & kPipeDeposit) != 0;
     const int lane = threadIdx.x & 31;
     const CellInfo ci = cell_info(g, pc, cell);
+    if (kStep) {
+#pragma unroll 1
+        for (int s0 = a; s0 < b; s0 += 32) {
+            const int sl = s0 + lane;
+            PState<float> p;
+            int outcome = -1, dir = 0;
+            if (sl < b) {
+                p.x = st.s[0][sl]; p.y = st.s[1][sl]; p.z = st.s[2][sl];
+                p.u = st.s[3][sl]; p.v = st.s[4][sl]; p.w = st.s[5][sl];
+                outcome = step32f<true, (kF & kPipeGather) != 0, (kF & kPipeDipole) != 0>(g, pc, coef, ci, p, dir);
+                if (outcome == kStay) {
+                    const int gs = base + sl;
+                    P.x[gs] = p.x; P.y[gs] = p.y; P.z[gs] = p.z;
+                    P.u[gs] = p.u; P.v[gs] = p.v; P.w[gs] = p.w;
+                    if (kDep) {
+                        st.s[0][sl] = p.x; st.s[1][sl] = p.y; st.s[2][sl] = p.z;
+                        st.s[3][sl] = p.u; st.s[4][sl] = p.v; st.s[5][sl] = p.w;
+                    }
+                } else if (kDep) {
+                    st.s[0][sl] = __int_as_float(0x7fffffff);  // not deposited here
+                }
+            }
+            leave_and_hole(g, P, outcome, dir, ci, p, base + sl, cell, cstart, kDep, nmig, nrem);
+        }
+        __syncwarp();
+    }
+    if (!kDep) return;
     float acc[32];
 #pragma unroll
     for (int l = 0; l < 32; ++l) acc[l] = 0.f;
 #pragma unroll 1
     for (int s0 = a; s0 < b; s0 += 32) {
         const int sl = s0 + lane;
-        PState<float> p;
-        int outcome = -1, dir = 0;
         if (sl < b) {
-            p.x = st.s[0][sl]; p.y = st.s[1][sl]; p.z = st.s[2][sl];
-            p.u = st.s[3][sl]; p.v = st.s[4][sl]; p.w = st.s[5][sl];
-            outcome = kStep ? step32f<true, (kF & kPipeGather) != 0, (kF & kPipeDipole) != 0>(g, pc, coef, ci, p, dir)
-                            : kStay;
-            if (outcome == kStay) {
-                if (kStep) {
-                    const int gs = base + sl;
-                    P.x[gs] = p.x; P.y[gs] = p.y; P.z[gs] = p.z;
-                    P.u[gs] = p.u; P.v[gs] = p.v; P.w[gs] = p.w;
-                }
-                if (kDep) add_moments(acc, p);
+            PState<float> p;
+            p.x = st.s[0][sl];
+            if (p.x == p.x) {
+                p.y = st.s[1][sl]; p.z = st.s[2][sl];
+                p.u = st.s[3][sl]; p.v = st.s[4][sl]; p.w = st.s[5][sl];
+                add_moments(acc, p);
             }
         }
-        if (kStep) leave_and_hole(g, P, outcome, dir, ci, p, base + sl, cell, cstart, kDep, nmig, nrem);
     }
-    if (kDep) emit_corner_sums(g, warp_transpose_sum<float>(acc), ci.cx, ci.cy, ci.cz, P.q);
+    emit_corner_sums(g, warp_transpose_sum<float>(acc), ci.cx, ci.cy, ci.cz, P.q);
 }
 
 // warp_transpose_sum of acc over the lanes with `mine` set (the others add
