@@ -181,6 +181,9 @@ struct ipic3d_ctx {
     int64_t* st_off = nullptr;
     int32_t* st_cnt = nullptr;
     int* st_unknown = nullptr;
+    int* st_flags = nullptr;            // fused upload: unknown species, cell overflow
+    cudaStream_t copy_stream = nullptr; // host-to-device copies of the chunked upload
+    cudaEvent_t copy_ev = nullptr;
     // per-phase event timing
     bool profiling = false;
     cudaEvent_t ph_ev[IPIC3D_PHASE_COUNT][2] = {};
@@ -469,6 +472,109 @@ int scatter_pops(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, const std::vec
     return check_launch(ctx, nl);
 }
 
+// Fast path of the device upload, for populations whose slot layout exists:
+// the AoS records go to the device in chunks of whole cells on the copy
+// stream, and each chunk's fused classify + scatter (+ deposit) kernel runs
+// on the context stream as soon as its bytes have landed, so the kernels
+// hide behind the copies. Returns 0 when done, 1 when a species is unknown
+// (the host path creates it), 2 when a cell's slots were too few (the
+// slower path re-lays out), < 0 on error.
+template <typename T>
+int upload_fast(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, const ipic3d_particle* parts,
+                const std::vector<int64_t>& off, const uint32_t* ids) {
+    const int64_t nc = ctx->ncells(), n = off[nc];
+    const int npop = (int)pops.size();
+    for (auto& P : pops)
+        if ((int64_t)P.h_start.size() != nc + 1) return 2;
+    int rc;
+    size_t cap_off = 0, cap_f = 0;
+    if ((rc = grow(reinterpret_cast<char*&>(ctx->st_parts), ctx->st_parts_cap, (size_t)n * sizeof(ipic3d_particle))))
+        return rc;
+    if (ids && (rc = grow(ctx->st_ids, ctx->st_ids_cap, (size_t)n))) return rc;
+    dfree(ctx->st_off);
+    if ((rc = grow(ctx->st_off, cap_off, (size_t)nc + 1))) return rc;
+    if (!ctx->st_flags && (rc = grow(ctx->st_flags, cap_f, 2))) return rc;
+    if (!ctx->copy_stream) CU(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    if (!ctx->copy_ev) CU(cudaEventCreateWithFlags(&ctx->copy_ev, cudaEventDisableTiming));
+    cudaStream_t st = ctx->stream, cs = ctx->copy_stream;
+    const bool deposit = ctx->fp32 && ctx->cfg.projector == IPIC3D_PROJECT_CIC;
+    // the staging buffers are free once the context stream's earlier work is done
+    CU(cudaEventRecord(ctx->copy_ev, st));
+    CU(cudaStreamWaitEvent(cs, ctx->copy_ev, 0));
+    CU(cudaMemcpyAsync(ctx->st_off, off.data(), (nc + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, cs));
+    UploadPops<T> U{};
+    U.npop = npop;
+    U.relative = std::is_same<T, float>::value ? 1 : 0;
+    for (int k = 0; k < npop; ++k) {
+        auto& P = pops[k];
+        U.x[k] = P.x; U.y[k] = P.y; U.z[k] = P.z; U.u[k] = P.u; U.v[k] = P.v; U.w[k] = P.w;
+        U.id[k] = P.id;
+        U.start[k] = P.start;
+        U.count[k] = P.count;
+        CU(cudaMemsetAsync(P.hole_cnt, 0, nc * sizeof(int32_t), st));
+        CU(cudaMemsetAsync(P.arr_cnt, 0, nc * sizeof(int32_t), st));
+        CU(cudaMemsetAsync(P.dirty_flag, 0, nc * sizeof(int32_t), st));
+        CU(cudaMemsetAsync(P.pending_in_count, 0, sizeof(uint32_t), st));
+        CU(cudaMemsetAsync(P.ctr, 0, sizeof(StepCounters), st));
+    }
+    CU(cudaMemsetAsync(ctx->st_flags, 0, 2 * sizeof(int), st));
+    UploadDeposit dep{};
+    dep.on = deposit ? 1 : 0;
+    dep.sx = (int)ctx->props.size[0];
+    dep.sy = (int)ctx->props.size[1];
+    dep.sz = (int)ctx->props.size[2];
+    dep.J = ctx->J;
+    dep.rho = ctx->rho;
+    if (deposit) {
+        CU(cudaMemsetAsync(ctx->J, 0, ctx->nnode() * 3 * sizeof(double), st));
+        CU(cudaMemsetAsync(ctx->rho, 0, ctx->nnode() * sizeof(double), st));
+    }
+    SpeciesTable sp{};
+    sp.n = npop;
+    for (int k = 0; k < npop; ++k) {
+        sp.q[k] = pops[k].q;
+        sp.qom[k] = pops[k].qom;
+    }
+    UploadGeom g;
+    g.ncells = (int)nc;
+    g.sx = (int)ctx->props.size[0];
+    g.sy = (int)ctx->props.size[1];
+    g.sz = (int)ctx->props.size[2];
+    for (int a = 0; a < 3; ++a) {
+        g.origin[a] = ctx->props.origin[a];
+        g.w[a] = ctx->props.cell_width[a];
+    }
+    // chunks of about 32 MB of records, cut at cell boundaries
+    const int64_t chunk = std::max<int64_t>(1, (int64_t)(32u << 20) / (int64_t)sizeof(ipic3d_particle));
+    int nl = 0;
+    for (int64_t c0 = 0; c0 < nc;) {
+        int64_t c1 = c0 + 1;
+        while (c1 < nc && off[c1] - off[c0] < chunk) ++c1;
+        const int64_t p0 = off[c0], pn = off[c1] - off[c0];
+        if (pn > 0) {
+            CU(cudaMemcpyAsync(reinterpret_cast<char*>(ctx->st_parts) + p0 * sizeof(ipic3d_particle), parts + p0,
+                               (size_t)pn * sizeof(ipic3d_particle), cudaMemcpyHostToDevice, cs));
+            if (ids) CU(cudaMemcpyAsync(ctx->st_ids + p0, ids + p0, (size_t)pn * sizeof(uint32_t),
+                                        cudaMemcpyHostToDevice, cs));
+        }
+        CU(cudaEventRecord(ctx->copy_ev, cs));
+        CU(cudaStreamWaitEvent(st, ctx->copy_ev, 0));
+        nl += launch_upload_cells<T>(ctx->st_parts, ids ? ctx->st_ids : nullptr, ctx->st_off, (int)c0, (int)c1, sp, U,
+                                     g, dep, ctx->st_flags, st);
+        c0 = c1;
+    }
+    if (deposit) nl += launch_j_finalize(ctx->g, (ctx->cfg.flags & IPIC3D_F_J_DIV8) != 0, !ctx->fp32, st);
+    if ((rc = check_launch(ctx, nl))) return rc;
+    int flags[2] = {0, 0};
+    CU(cudaMemcpyAsync(flags, ctx->st_flags, sizeof(flags), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    if (flags[0]) return 1;
+    if (flags[1]) return 2;
+    ctx->j_valid = deposit;
+    ctx->particles_hint = (uint64_t)n;
+    return IPIC3D_OK;
+}
+
 // Upload through the device: one copy of the AoS records, then the species
 // classification and the scatter run on the GPU. Returns 1 when the host
 // path must be taken instead (a species the context does not know yet).
@@ -480,7 +586,8 @@ int upload_device(ipic3d_ctx* ctx, const ipic3d_particle* parts, const uint64_t*
     for (int64_t c = 0; c < nc; ++c) off[c + 1] = off[c] + (int64_t)cell_counts[c];
     const int64_t n = off[nc];
     if (n == 0) return 1;
-    int rc;
+    int rc = ctx->fp32 ? upload_fast(ctx, ctx->p32, parts, off, ids) : upload_fast(ctx, ctx->p64, parts, off, ids);
+    if (rc <= 1) return rc;  // done, error, or the host path (unknown species)
     size_t cap_off = 0, cap_cnt = 0, cap_u = 0;
     if ((rc = grow(reinterpret_cast<char*&>(ctx->st_parts), ctx->st_parts_cap, (size_t)n * sizeof(ipic3d_particle))))
         return rc;
@@ -880,6 +987,9 @@ int destroy_impl(ipic3d_ctx* ctx) {
     dfree(ctx->st_off);
     dfree(ctx->st_cnt);
     dfree(ctx->st_unknown);
+    dfree(ctx->st_flags);
+    if (ctx->copy_ev) cudaEventDestroy(ctx->copy_ev);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     for (auto& e : ctx->pend_ev)
         if (e) cudaEventDestroy(e);
     for (auto& pair : ctx->ph_ev)

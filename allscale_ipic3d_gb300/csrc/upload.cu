@@ -88,7 +88,148 @@ __global__ void k_scatter(const ipic3d_particle* __restrict__ p, const uint32_t*
     if (lane < U.npop) U.count[lane][c] = base[lane];
 }
 
+// Centred cloud-in-cell moments of one particle with weight wq (the charge):
+// acc[8 Q + m], Q in {u, v, w, 1}, m in {1, x, y, xy, z, xz, yz, xyz} about the
+// cell centre (the layout of the FP32 push's deposit).
+__device__ __forceinline__ void add_moments_q(float (&acc)[32], float x, float y, float z, float u, float v, float w,
+                                              float wq) {
+    x -= 0.5f; y -= 0.5f; z -= 0.5f;
+    const float mono[8] = {1.f, x, y, x * y, z, x * z, y * z, x * y * z};
+    const float Q[4] = {wq * u, wq * v, wq * w, wq};
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int m = 0; m < 8; ++m) acc[q * 8 + m] = fmaf(Q[q], mono[m], acc[q * 8 + m]);
+}
+
+template <bool kDeposit, typename T>
+__global__ void k_upload_cells(const ipic3d_particle* __restrict__ p, const uint32_t* __restrict__ ids,
+                               const int64_t* __restrict__ in_off, int c0, int c1, SpeciesTable sp, UploadPops<T> U,
+                               UploadGeom g, UploadDeposit dep, int* flags) {
+    const int c = c0 + (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (c >= c1) return;
+    const int cz = c % g.sz, cy = (c / g.sz) % g.sy, cx = c / (g.sy * g.sz);
+    const double ox = g.origin[0] + (double)cx * g.w[0];
+    const double oy = g.origin[1] + (double)cy * g.w[1];
+    const double oz = g.origin[2] + (double)cz * g.w[2];
+    const int64_t a = in_off[c], b = in_off[c + 1];
+    int base[kUploadMaxPops], cap[kUploadMaxPops];
+    int64_t start[kUploadMaxPops];
+    for (int k = 0; k < U.npop; ++k) {
+        base[k] = 0;
+        start[k] = U.start[k][c];
+        cap[k] = (int)(U.start[k][c + 1] - start[k]);
+    }
+    float acc[32];
+    if (kDeposit) {
+#pragma unroll
+        for (int l = 0; l < 32; ++l) acc[l] = 0.f;
+    }
+    bool unknown = false, full = false;
+    for (int64_t i0 = a; i0 < b; i0 += 32) {
+        const int64_t i = i0 + lane;
+        int s = -1;
+        ipic3d_particle q;
+        if (i < b) {
+            q = p[i];
+            for (int k = 0; k < sp.n; ++k)
+                if (sp.q[k] == q.q && sp.qom[k] == q.qom) { s = k; break; }
+            if (s < 0) unknown = true;
+        }
+        T x = 0, y = 0, z = 0;
+        if (s >= 0) {
+            if (U.relative) {
+                x = (T)((q.position[0] - ox) / g.w[0]);
+                y = (T)((q.position[1] - oy) / g.w[1]);
+                z = (T)((q.position[2] - oz) / g.w[2]);
+            } else {
+                x = (T)q.position[0];
+                y = (T)q.position[1];
+                z = (T)q.position[2];
+            }
+        }
+        for (int k = 0; k < U.npop; ++k) {
+            const unsigned bal = __ballot_sync(0xffffffffu, s == k);
+            if (s == k) {
+                const int r = base[k] + __popc(bal & ((1u << lane) - 1u));
+                if (r < cap[k]) {
+                    const int64_t slot = start[k] + r;
+                    U.x[k][slot] = x; U.y[k][slot] = y; U.z[k][slot] = z;
+                    U.u[k][slot] = (T)q.velocity[0];
+                    U.v[k][slot] = (T)q.velocity[1];
+                    U.w[k][slot] = (T)q.velocity[2];
+                    if (U.id[k]) U.id[k][slot] = ids ? ids[i] : (uint32_t)i;
+                } else {
+                    full = true;
+                }
+            }
+            base[k] += __popc(bal);
+        }
+        if (kDeposit && s >= 0)
+            add_moments_q(acc, (float)x, (float)y, (float)z, (float)q.velocity[0], (float)q.velocity[1],
+                          (float)q.velocity[2], (float)sp.q[s]);
+    }
+    if (__any_sync(0xffffffffu, unknown) && lane == 0) atomicExch(flags, 1);
+    if (__any_sync(0xffffffffu, full) && lane == 0) atomicExch(flags + 1, 1);
+    if (lane < U.npop) U.count[lane][c] = base[lane] < cap[lane] ? base[lane] : cap[lane];
+    if (kDeposit) {
+        // lane v: summed moment v = 8 Q + m; three axis butterflies give the
+        // corner sums (corner m, component Q); one FP64 atomic each
+        float v[32];
+#pragma unroll
+        for (int l = 0; l < 32; ++l) v[l] = acc[l];
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) {
+            const bool upper = (lane & off) != 0;
+#pragma unroll
+            for (int j = 0; j < off; ++j) {
+                const float send = upper ? v[j] : v[j + off];
+                const float keep = upper ? v[j + off] : v[j];
+                v[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+            }
+        }
+        float t = v[0];
+        const int m = lane & 7, qq = lane >> 3;
+#pragma unroll
+        for (int bit = 1; bit < 8; bit <<= 1) {
+            const float o = __shfl_xor_sync(0xffffffffu, t, bit);
+            t = (m & bit) ? fmaf(0.5f, o, t) : fmaf(0.5f, t, -o);
+        }
+        if (t != 0.f) {
+            const int64_t n = ((int64_t)(cx + (m & 1)) * (dep.sy + 1) + (cy + ((m >> 1) & 1))) * (dep.sz + 1) +
+                              (cz + (m >> 2));
+            if (qq < 3)
+                atomicAdd(dep.J + 3 * n + qq, (double)t);
+            else
+                atomicAdd(dep.rho + n, (double)t);
+        }
+    }
+}
+
 }  // namespace
+
+template <typename T>
+int launch_upload_cells(const void* parts, const uint32_t* ids, const int64_t* in_off, int c0, int c1,
+                        const SpeciesTable& sp, const UploadPops<T>& U, const UploadGeom& g, const UploadDeposit& dep,
+                        int* flags, cudaStream_t st) {
+    if (c1 <= c0) return 0;
+    const int64_t threads = (int64_t)(c1 - c0) * 32;
+    const unsigned blocks = (unsigned)((threads + 255) / 256);
+    if (dep.on)
+        k_upload_cells<true, T><<<blocks, 256, 0, st>>>((const ipic3d_particle*)parts, ids, in_off, c0, c1, sp, U, g,
+                                                        dep, flags);
+    else
+        k_upload_cells<false, T><<<blocks, 256, 0, st>>>((const ipic3d_particle*)parts, ids, in_off, c0, c1, sp, U,
+                                                         g, dep, flags);
+    return 1;
+}
+template int launch_upload_cells<float>(const void*, const uint32_t*, const int64_t*, int, int, const SpeciesTable&,
+                                        const UploadPops<float>&, const UploadGeom&, const UploadDeposit&, int*,
+                                        cudaStream_t);
+template int launch_upload_cells<double>(const void*, const uint32_t*, const int64_t*, int, int, const SpeciesTable&,
+                                         const UploadPops<double>&, const UploadGeom&, const UploadDeposit&, int*,
+                                         cudaStream_t);
 
 int launch_classify(const void* parts, int64_t n, const SpeciesTable& sp, uint8_t* sid, int* unknown,
                     cudaStream_t st) {

@@ -34,8 +34,25 @@ struct UploadPops {
     int32_t* count[kUploadMaxPops];
 };
 
+// Deposit of the uploaded particles (FP32 contexts): the node sums of J and
+// rho (raw, before the periodic fold and the normalisation).
+struct UploadDeposit {
+    int on;
+    int sx, sy, sz;  // cells per axis (nodes (s+1)^3)
+    double* J;
+    double* rho;
+};
+
 int launch_classify(const void* parts, int64_t n, const SpeciesTable& sp, uint8_t* sid, int* unknown,
                     cudaStream_t st);
+// One pass for cells [c0, c1): classification, scatter into the existing
+// slot layout, per-cell counts, and (dep.on) the cloud-in-cell deposit.
+// flags[0] = a particle of an unknown species, flags[1] = a cell's slots
+// were too few (the caller then re-lays out).
+template <typename T>
+int launch_upload_cells(const void* parts, const uint32_t* ids, const int64_t* in_off, int c0, int c1,
+                        const SpeciesTable& sp, const UploadPops<T>& U, const UploadGeom& g, const UploadDeposit& dep,
+                        int* flags, cudaStream_t st);
 int launch_count(const uint8_t* sid, const int64_t* in_off, int ncells, int npop, int32_t* counts, cudaStream_t st);
 template <typename T>
 int launch_scatter(const void* parts, const uint32_t* ids, const uint8_t* sid, const int64_t* in_off,
