@@ -134,7 +134,7 @@ struct Push32Set {
 // One population of one universe of a batch: everything a batched particle
 // kernel needs, read from a device table indexed by job.
 template <typename T>
-struct PopJob {
+struct alignas(16) PopJob {  // 16-byte multiple: the FP32 push bulk-copies records
     Geom g;
     Pop<T> P;
     Push32Const pc;         // FP32 populations: the push constants

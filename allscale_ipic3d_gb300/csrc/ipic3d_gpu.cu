@@ -1615,9 +1615,9 @@ int batch_enqueue_step(ipic3d_batch* b) {
     }
     n += launch_batch_begin<T>(jobs, nj, b->d_inst, ni, b->max_nodes, deposit, b->d_flag, st);
     if (nj > 0) {
-        n += launch_push_batch<T>(jobs, b->d_cta, b->nctas, 0, st);
+        n += launch_push_batch<T>(jobs, b->d_cta, b->nctas, 0, jobs_of<T>(b)[0].g, st);
         n += launch_push_pending_batch<T>(jobs, nj, st);
-        n += launch_place_batch<T>(jobs, b->d_place, b->nplace, st);
+        n += launch_place_batch<T>(jobs, nj, st);
         n += launch_pending_rotate_batch<T>(jobs, nj, st);
     }
     if (deposit) n += launch_j_finalize_batch(b->d_inst, ni, b->max_cells, st);

@@ -30,11 +30,12 @@ int launch_pending_count(const Pop<T>& P, int32_t* per_cell, cudaStream_t st);
 
 // batched ensemble: job tables built by the host (particles_fp64/32.cu)
 template <typename T>
-int launch_push_batch(const PopJob<T>* jobs, const int2* cta_job, int64_t nctas, int mode, cudaStream_t st);
+int launch_push_batch(const PopJob<T>* jobs, const int2* cta_job, int64_t nctas, int mode, const Geom& g0,
+                      cudaStream_t st);  // g0: the policy fields (mover, flags, deposit) shared by the jobs
 template <typename T>
 int launch_push_pending_batch(const PopJob<T>* jobs, int njobs, cudaStream_t st);
 template <typename T>
-int launch_place_batch(const PopJob<T>* jobs, const int2* blk_job, int64_t nblocks, cudaStream_t st);
+int launch_place_batch(const PopJob<T>* jobs, int njobs, cudaStream_t st);
 template <typename T>
 int launch_pending_rotate_batch(const PopJob<T>* jobs, int njobs, cudaStream_t st);
 template <typename T>

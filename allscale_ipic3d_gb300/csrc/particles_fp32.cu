@@ -16,6 +16,7 @@ bool g_pipe_ready[kMaxDevices] = {};
 int g_pipe_grid[kMaxDevices] = {};  // persistent CTAs of the pipelined push
 
 using PipeFn = void (*)(Geom, PopSet<float>, Push32Set, TileMap);
+using PipeJobsFn = void (*)(const PopJob<float>*, const int2*, int);
 
 // The compile-time policies that are instantiated (kPipe* bit sets): the
 // step with the dipole mover, the field-gather mover with or without the
@@ -33,6 +34,36 @@ constexpr int kPipeVariants[] = {
 template <int kF>
 constexpr PipeFn pipe_fn() {
     return k_push32_pipe<kPipeStages, 2, kF>;
+}
+
+template <int kF>
+constexpr PipeJobsFn pipe_jobs_fn() {
+    return k_push32_pipe_jobs<kPipeStages, 2, kF>;
+}
+
+PipeJobsFn pipe_jobs_kernel(int f) {
+    switch (f) {
+        case kPipeStep | kPipeDipole: return pipe_jobs_fn<kPipeStep | kPipeDipole>();
+        case kPipeStep | kPipeDipole | kPipeDeposit: return pipe_jobs_fn<kPipeStep | kPipeDipole | kPipeDeposit>();
+        case kPipeStep | kPipeGather: return pipe_jobs_fn<kPipeStep | kPipeGather>();
+        case kPipeStep | kPipeGather | kPipeDeposit: return pipe_jobs_fn<kPipeStep | kPipeGather | kPipeDeposit>();
+        case kPipeStep | kPipeGather | kPipeDipole: return pipe_jobs_fn<kPipeStep | kPipeGather | kPipeDipole>();
+        case kPipeStep | kPipeGather | kPipeDipole | kPipeDeposit:
+            return pipe_jobs_fn<kPipeStep | kPipeGather | kPipeDipole | kPipeDeposit>();
+        case kPipeDeposit: return pipe_jobs_fn<kPipeDeposit>();
+        default: return nullptr;
+    }
+}
+
+// The policy bits of a launch: mode 0 = step, 1 = deposit only.
+int pipe_policy(const Geom& g, int mode) {
+    int f = g.deposit ? kPipeDeposit : 0;
+    if (mode == 0) {
+        f |= kPipeStep;
+        if (g.mover == 1) f |= kPipeGather;
+        if (g.mover != 1 || (g.flags & 4u)) f |= kPipeDipole;
+    }
+    return f;
 }
 
 PipeFn pipe_kernel(int f) {
@@ -61,12 +92,15 @@ cudaError_t init_push32(int dev) {
     int min_per_sm = 1 << 30;
     for (int f : kPipeVariants) {
         PipeFn fn = pipe_kernel(f);
+        PipeJobsFn fj = pipe_jobs_kernel(f);
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(fj, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         if (e != cudaSuccess) return e;
-        int per_sm = 0;
+        int per_sm = 0, per_sm_j = 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kPipeThreads, bytes);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_j, fj, kPipeThreads, bytes);
         if (e != cudaSuccess) return e;
-        if (per_sm < min_per_sm) min_per_sm = per_sm;
+        min_per_sm = std::min(min_per_sm, std::min(per_sm, per_sm_j));
     }
     int sms = 0;
     cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -98,15 +132,8 @@ Push32Const push32_const(const Geom& g, const Pop<float>& P) {
 // instance of the step's policies, one launch for all populations of S
 template <>
 int launch_push<float>(const Geom& g, const PopSet<float>& S, int mode, cudaStream_t st) {
-    int f = g.deposit ? kPipeDeposit : 0;
-    if (mode == 0) {
-        f |= kPipeStep;
-        if (g.mover == 1) f |= kPipeGather;
-        if (g.mover != 1 || (g.flags & 4u)) f |= kPipeDipole;
-    } else if (!g.deposit) {
-        return 0;  // nothing to deposit
-    }
-    PipeFn fn = pipe_kernel(f);
+    if (mode != 0 && !g.deposit) return 0;  // nothing to deposit
+    PipeFn fn = pipe_kernel(pipe_policy(g, mode));
     if (!fn || S.n <= 0) return 0;
     TileMap tm{};
     tm.n = S.n;
@@ -151,11 +178,20 @@ int launch_cell_coef(const Geom& g, float* coef, cudaStream_t st) {
     return 1;
 }
 
+// the batched FP32 step: the pipelined push over every job's tiles
 template <>
 int launch_push_batch<float>(const PopJob<float>* jobs, const int2* cta_job, int64_t nctas, int mode,
-                             cudaStream_t st) {
+                             const Geom& g0, cudaStream_t st) {
     if (nctas <= 0) return 0;
-    k_push32_batch<3><<<(unsigned)nctas, kPushThreads, 0, st>>>(jobs, cta_job, mode);
+    if (mode != 0 && !g0.deposit) return 0;
+    PipeJobsFn fn = pipe_jobs_kernel(pipe_policy(g0, mode));
+    if (!fn) return 0;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int grid = g_pipe_grid[dev];
+    if (grid <= 0) grid = 1;  // init_push32 did not run on this device: the launch fails (no shared-memory opt-in)
+    if (grid > nctas) grid = (int)nctas;
+    fn<<<grid, kPipeThreads, pipe_smem_bytes<kPipeStages>(), st>>>(jobs, cta_job, (int)nctas);
     return 1;
 }
 
@@ -172,7 +208,7 @@ int launch_cell_coef_batch(const InstJob* inst, int ninst, int64_t max_cells, cu
     return 1;
 }
 
-template int launch_place_batch<float>(const PopJob<float>*, const int2*, int64_t, cudaStream_t);
+template int launch_place_batch<float>(const PopJob<float>*, int, cudaStream_t);
 template int launch_pending_rotate_batch<float>(const PopJob<float>*, int, cudaStream_t);
 template int launch_batch_begin<float>(const PopJob<float>*, int, const InstJob*, int, int64_t, int, uint32_t*,
                                        cudaStream_t);

@@ -100,12 +100,14 @@ __global__ void k_push_pending_batch(const PopJob<T>* __restrict__ jobs) {
     push_pending_body<T>(J.g, J.P, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
+// Placement of a batch: blockIdx.y = job, the job's warps stride over its
+// dirty-cell list (cells with holes or arrivals only).
 template <typename T>
-__global__ void k_place_batch(const PopJob<T>* __restrict__ jobs, const int2* __restrict__ blk_job) {
-    __shared__ PopJob<T> job;
-    const int2 bj = __ldg(blk_job + blockIdx.x);
-    load_job(job, jobs + bj.x);
-    place_body<T>(job.g, job.P, job.sort_tmp, bj.y + (int)(threadIdx.x >> 5));
+__global__ void k_place_batch(const PopJob<T>* __restrict__ jobs) {
+    const PopJob<T>& J = jobs[blockIdx.y];
+    const uint32_t n = J.P.ctr->dirty;
+    const uint32_t w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i = w0; i < n; i += nw) place_body<T>(J.g, J.P, J.sort_tmp, J.P.dirty_list[i]);
 }
 
 template <typename T>
@@ -169,7 +171,8 @@ __global__ void k_batch_status(const PopJob<T>* __restrict__ jobs, int njobs, Jo
 }
 
 template <typename T>
-int launch_push_batch(const PopJob<T>* jobs, const int2* cta_job, int64_t nctas, int mode, cudaStream_t st);
+int launch_push_batch(const PopJob<T>* jobs, const int2* cta_job, int64_t nctas, int mode, const Geom& g0,
+                      cudaStream_t st);
 
 template <typename T>
 int launch_push_batch_generic(const PopJob<T>* jobs, const int2* cta_job, int64_t nctas, int mode, cudaStream_t st) {
@@ -188,9 +191,9 @@ int launch_push_pending_batch_generic(const PopJob<T>* jobs, int njobs, cudaStre
 }
 
 template <typename T>
-int launch_place_batch(const PopJob<T>* jobs, const int2* blk_job, int64_t nblocks, cudaStream_t st) {
-    if (nblocks <= 0) return 0;
-    k_place_batch<T><<<(unsigned)nblocks, 256, 0, st>>>(jobs, blk_job);
+int launch_place_batch(const PopJob<T>* jobs, int njobs, cudaStream_t st) {
+    if (njobs <= 0) return 0;
+    k_place_batch<T><<<dim3(8, njobs), 256, 0, st>>>(jobs);
     return 1;
 }
 

@@ -127,9 +127,11 @@ struct __align__(16) PipeStage {
     alignas(16) float coef[kItemMaxCells * 48];      // item mode + field gather: cellcoef of the tile's cells
     alignas(16) int64_t start[kMaxCellsPerCta + 4];  // start[(c0 & ~1) ...]
     alignas(16) int32_t count[kMaxCellsPerCta + 8];  // count[(c0 & ~3) ...]
+    alignas(16) PopJob<float> job;                   // batched launch: the tile's job record
 };
 static_assert(offsetof(PipeStage, coef) % 16 == 0 && offsetof(PipeStage, start) % 16 == 0 &&
-                  offsetof(PipeStage, count) % 16 == 0 && sizeof(PipeStage) % 16 == 0,
+                  offsetof(PipeStage, count) % 16 == 0 && offsetof(PipeStage, job) % 16 == 0 &&
+                  sizeof(PipeStage) % 16 == 0 && sizeof(PopJob<float>) % 16 == 0,
               "bulk copies need 16-byte aligned shared-memory destinations");
 
 template <int kStages>
@@ -138,7 +140,8 @@ struct PipeSmem {
     uint64_t full[kStages];               // the stage's copies landed
     uint64_t empty[kStages];              // the compute warps are done with the stage
     int2 desc[kStages];                   // (first cell, number of cells) of the stage's tile
-    int pop[kStages];                     // population of the stage's tile
+    int pop[kStages];                     // population (batched launch: job) of the stage's tile
+    int ltile[kStages];                   // the tile's index within its population
     int next_item[kStages];               // item counter of the stage's tile
     int abort;                            // a wait expired: every warp stops
 };
@@ -176,15 +179,16 @@ __device__ __forceinline__ TileCopy tile_copy(const Pop<float>& P, int tile, int
     return t;
 }
 
-// Issued by the producer: the tile's copies into `st`, counted on `bar`;
+// Issued by the producer: the tile's copies into `st`, counted on `bar`
+// (`extra` more bytes are expected from copies the caller issues);
 // with `coef` (item mode, field gather) also the cells' field coefficients
 // (48 floats = 192 bytes per cell, contiguous from cell c0).
 __device__ __forceinline__ void issue_tile(const Pop<float>& P, const float* coef, int tile, int2 desc,
-                                           PipeStage& st, uint64_t* bar) {
+                                           PipeStage& st, uint64_t* bar, uint32_t extra = 0) {
     const TileCopy t = tile_copy(P, tile, desc);
     const bool with_coef = coef != nullptr && desc.y <= kItemMaxCells;
     const uint32_t coef_bytes = with_coef ? (uint32_t)desc.y * 192u : 0u;
-    mbar_arrive_expect_tx(bar, 6u * t.slot_bytes + t.s_bytes + t.c_bytes + coef_bytes);
+    mbar_arrive_expect_tx(bar, 6u * t.slot_bytes + t.s_bytes + t.c_bytes + coef_bytes + extra);
     float* const arr[6] = {P.x, P.y, P.z, P.u, P.v, P.w};
 #pragma unroll
     for (int a = 0; a < 6; ++a) bulk_load(st.s[a], arr[a] + t.base, t.slot_bytes, bar);
@@ -809,6 +813,109 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
         if (lane == 0) mbar_arrive(&sm.empty[s]);
     }
     if (cur >= 0) flush_counts(S.p[cur].ctr, nmig, nrem);
+}
+
+// The batched form: tiles of many universes' populations in one launch.
+// Global tile t is tile cta_job[t].y of job cta_job[t].x; the producer also
+// bulk-copies the job record (geometry, population, push constants) into the
+// stage, and the compute warps read everything about the tile from there.
+template <int kStages, int kMinBlocks, int kF>
+__global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
+    k_push32_pipe_jobs(const PopJob<float>* __restrict__ jobs, const int2* __restrict__ cta_job, int ntiles) {
+    constexpr bool kStep = (kF & kPipeStep) != 0;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    PipeSmem<kStages>& sm = *reinterpret_cast<PipeSmem<kStages>*>(smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int G = gridDim.x;
+    if (tid == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&sm.full[s], 1);
+            mbar_init(&sm.empty[s], kComputeWarps);
+        }
+        sm.abort = 0;
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const volatile int* abort = &sm.abort;
+
+    if (warp == kComputeWarps) {
+        // ---- producer ----
+        if (lane != 0) return;
+        auto issue = [&](int t, int s) {
+            const int2 cj = __ldg(cta_job + t);
+            const PopJob<float>* J = jobs + cj.x;
+            const Pop<float> P = J->P;
+            const float* coef = (kF & kPipeGather) ? J->g.cellcoef : nullptr;
+            const int2 d = __ldg(P.cta_cells + cj.y);
+            sm.desc[s] = d;
+            sm.pop[s] = cj.x;
+            sm.ltile[s] = cj.y;
+            sm.next_item[s] = 0;
+            issue_tile(P, coef, cj.y, d, sm.stage[s], &sm.full[s], (uint32_t)sizeof(PopJob<float>));
+            bulk_load(&sm.stage[s].job, J, (uint32_t)sizeof(PopJob<float>), &sm.full[s]);
+        };
+        int issued = 0;
+        for (int s = 0; s < kStages; ++s) {
+            const int t = blockIdx.x + s * G;
+            if (t >= ntiles) break;
+            issue(t, s);
+            ++issued;
+        }
+        bool failed = false;
+        int k = 0;
+        for (int t = blockIdx.x; t < ntiles; t += G, ++k) {
+            const int s = k % kStages;
+            if (!mbar_wait(&sm.empty[s], (uint32_t)(k / kStages) & 1u, abort)) {
+                failed = true;
+                break;
+            }
+            const bool store = kStep && sm.desc[s].y > kItemMaxCells;
+            if (store) {
+                const Pop<float>& P = sm.stage[s].job.P;
+                const TileCopy c = tile_copy(P, sm.ltile[s], sm.desc[s]);
+                float* const arr[6] = {P.x, P.y, P.z, P.u, P.v, P.w};
+#pragma unroll
+                for (int a = 0; a < 6; ++a) bulk_store(arr[a] + c.base, sm.stage[s].s[a], c.slot_bytes);
+                bulk_commit();
+            }
+            const int tn = t + kStages * G;
+            if (tn < ntiles) {
+                if (store) bulk_wait_read_all();  // the stores have read the stage
+                issue(tn, s);
+                ++issued;
+            }
+        }
+        if (failed) {
+            if (atomicExch(&sm.abort, 1) == 0) atomicAdd(&jobs[0].P.ctr->timeouts, 1u);
+            const int never = 0;
+            for (int kk = k; kk < issued; ++kk)
+                mbar_wait(&sm.full[kk % kStages], (uint32_t)(kk / kStages) & 1u, &never);
+        }
+        bulk_wait_all();
+        return;
+    }
+
+    // ---- compute warps ----
+    uint32_t nmig = 0, nrem = 0;
+    StepCounters* cur = nullptr;  // counters of the job whose counts are held
+    int k = 0;
+    for (int t = blockIdx.x; t < ntiles; t += G, ++k) {
+        const int s = k % kStages;
+        if (!__all_sync(0xffffffffu, mbar_wait(&sm.full[s], (uint32_t)(k / kStages) & 1u, abort))) {
+            if (lane == 0 && atomicExch(&sm.abort, 1) == 0) atomicAdd(&jobs[0].P.ctr->timeouts, 1u);
+            break;
+        }
+        const PopJob<float>& J = sm.stage[s].job;
+        if (J.P.ctr != cur) {
+            if (cur) flush_counts(cur, nmig, nrem);
+            cur = J.P.ctr;
+        }
+        push_tile_warp<kF>(J.g, J.P, J.pc, sm.ltile[s], sm.desc[s], sm.stage[s], &sm.next_item[s], nmig, nrem);
+        fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.empty[s]);
+    }
+    if (cur) flush_counts(cur, nmig, nrem);
 }
 
 }  // namespace ipg
