@@ -61,6 +61,8 @@ _SIGNATURES = [
     ("ipic3d_gpu_stats", C.c_int, [_vp, _vp]),
     ("ipic3d_gpu_profile", C.c_int, [_vp, C.c_int]),
     ("ipic3d_gpu_profile_read", C.c_int, [_vp, _vp, C.c_int]),
+    ("ipic3d_gpu_get_push_shape", C.c_int, [_vp, _vp]),
+    ("ipic3d_gpu_set_push_shape", C.c_int, [_vp, _vp]),
     ("ipic3d_gpu_project_noalloc", C.c_int, [_vp, C.c_uint32, _vp, _vp, _vp, _vp, _vp]),
     ("ipic3d_gpu_boris", C.c_int, [_vp, C.c_uint64, _vp, _vp, C.c_double, C.c_uint64, C.c_int]),
     ("ipic3d_gpu_batch_create", C.c_int, [C.c_uint32, _vp, _vp, C.POINTER(_vp)]),
@@ -71,6 +73,7 @@ _SIGNATURES = [
     ("ipic3d_gpu_batch_synchronize", C.c_int, [_vp]),
     ("ipic3d_gpu_batch_stream", _vp, [_vp]),
     ("ipic3d_gpu_batch_stats", C.c_int, [_vp, _vp]),
+    ("ipic3d_gpu_batch_get_push_shape", C.c_int, [_vp, _vp]),
     ("ipic3d_gpu_last_error", C.c_int, [C.c_char_p, C.c_size_t]),
 ]
 EXPORTED_SYMBOLS = [s[0] for s in _SIGNATURES]
@@ -259,6 +262,24 @@ class Simulation:
         _check(library().ipic3d_gpu_profile_read(self._ctx, C.byref(out), 1 if reset else 0))
         return out.as_dict()
 
+    def push_shape(self):
+        """Launch shape of the FP32 push (autotuned unless fixed)."""
+        out = abi.PushShape()
+        _check(library().ipic3d_gpu_get_push_shape(self._ctx, C.byref(out)))
+        return out.as_dict()
+
+    def set_push_shape(self, item=None, item_cells=None, blocks_per_sm=None):
+        """Fixes the push shape (no autotuning); with no argument, restarts
+        the autotuner (its trials run in the next steps)."""
+        if item is None and item_cells is None and blocks_per_sm is None:
+            _check(library().ipic3d_gpu_set_push_shape(self._ctx, None))
+            return
+        cur = self.push_shape()
+        s = abi.PushShape(item=cur["item"] if item is None else int(item),
+                          item_cells=cur["item_cells"] if item_cells is None else int(item_cells),
+                          blocks_per_sm=cur["blocks_per_sm"] if blocks_per_sm is None else int(blocks_per_sm))
+        _check(library().ipic3d_gpu_set_push_shape(self._ctx, C.byref(s)))
+
     @property
     def stream(self):
         return library().ipic3d_gpu_stream(self._ctx)
@@ -319,6 +340,11 @@ class Batch:
     def stats(self):
         out = Stats()
         _check(library().ipic3d_gpu_batch_stats(self._b, C.byref(out)))
+        return out.as_dict()
+
+    def push_shape(self):
+        out = abi.PushShape()
+        _check(library().ipic3d_gpu_batch_get_push_shape(self._b, C.byref(out)))
         return out.as_dict()
 
     @property

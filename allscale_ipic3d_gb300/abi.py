@@ -144,6 +144,14 @@ class Stats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class PushShape(C.Structure):
+    _fields_ = [("item", C.c_int32), ("item_cells", C.c_int32), ("blocks_per_sm", C.c_int32), ("tuned", C.c_int32),
+                ("tuning", C.c_int32), ("trials", C.c_int32), ("push_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 PHASES = ["push", "pending", "inject", "place", "fields", "moments", "unused6", "unused7"]
 
 

@@ -93,8 +93,7 @@ struct Pop {
     StepCounters* ctr;
     int64_t capacity;       // total slots
     double q, qom;
-    int32_t shape;          // launch shape of the FP32 push (kPushShape*)
-    int32_t pad;
+    int32_t pad[2];
 };
 
 // Up to kSetPops populations of one universe advanced by one launch
@@ -107,8 +106,16 @@ struct PopSet {
     int n;
 };
 
-// Launch shapes of the pipelined FP32 push (shared-memory stages per CTA).
-enum : int32_t { kPushStages3 = 0, kPushStages2 = 1, kPushShapeCount = 2 };
+// Launch shape of the pipelined FP32 push, chosen per context (or batch) by
+// the autotuner of ipic3d_gpu.cu: a tile of at most `item_cells` cells is
+// split into work items of `item` particles (one warp each), a sparser tile
+// is pushed slot by slot; `per_sm` persistent thread blocks run on each SM.
+struct PushShape {
+    int32_t item;        // a power of two, 32..1024
+    int32_t item_cells;  // 0..32 (0: every tile slot by slot)
+    int32_t per_sm;      // 1..the blocks that fit on an SM
+};
+constexpr PushShape kDefaultPushShape{256, 32, 2};
 
 // Every constant of the step in FP32, computed on the host: the kernel runs
 // no FP64 instruction per particle (GB300's FP64 rate is a small fraction of

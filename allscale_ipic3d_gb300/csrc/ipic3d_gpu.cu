@@ -13,12 +13,16 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/ipic3d_gpu.h"
+#include "autotune.h"
 #include "launch.h"
 #include "upload.h"
 
@@ -73,7 +77,6 @@ struct PopStore {
     Mover<T>*outbox = nullptr, *pending_in = nullptr, *pending_out = nullptr;
     uint32_t* pending_in_count = nullptr;
     StepCounters* ctr = nullptr;
-    int32_t shape = 0;             // launch shape of the FP32 push
     std::vector<int64_t> h_start;  // host copy of start[]
 
     void release() {
@@ -107,8 +110,7 @@ struct PopStore {
         P.capacity = capacity;
         P.q = q;
         P.qom = qom;
-        P.shape = shape;
-        P.pad = 0;
+        P.pad[0] = P.pad[1] = 0;
         return P;
     }
 };
@@ -190,6 +192,13 @@ struct ipic3d_ctx {
     bool ph_open[IPIC3D_PHASE_COUNT] = {};
     ipic3d_profile prof{};
     uint64_t push_particles = 0;
+    // launch shape of the FP32 push: autotuned (config block_size 0) unless
+    // fixed by ipic3d_gpu_set_push_shape
+    PushTuner tuner;
+    bool shape_fixed = false;
+    uint64_t tuned_particles = 0;  // particle count the shape was tuned for
+    bool tune_timing = false;      // this step is a trial: time the push
+    cudaEvent_t tune_ev[2] = {nullptr, nullptr};
 
     int npops() const { return fp32 ? (int)p32.size() : (int)p64.size(); }
     int64_t nfield() const { return (props.size[0] + 3) * (props.size[1] + 3) * (props.size[2] + 3); }
@@ -235,7 +244,6 @@ int alloc_pop(ipic3d_ctx* ctx, PopStore<T>& P, const std::vector<uint64_t>& coun
     P.h_start.assign(nc + 1, 0);
     for (int64_t c = 0; c < nc; ++c) P.h_start[c + 1] = P.h_start[c] + cell_capacity(ctx->cfg, counts[c]);
     P.capacity = P.h_start[nc];
-    P.shape = ctx->cfg.block_size == 3 ? kPushStages3 : kPushStages2;
     // every particle can wait at most once per step: capacity entries suffice
     P.pending_cap = (uint32_t)std::min<int64_t>(std::max<int64_t>(1 << 12, P.capacity), 0x7fffffff);
     int64_t inject_cap = 0;
@@ -827,8 +835,8 @@ int project_impl(ipic3d_ctx* ctx) {
     Geom g = ctx->g;
     g.deposit = 1;
     int n = 0;
-    for (auto& S : pop_sets(ctx->p32)) n += launch_push<float>(g, S, 1, st);
-    for (auto& S : pop_sets(ctx->p64)) n += launch_push<double>(g, S, 1, st);
+    for (auto& S : pop_sets(ctx->p32)) n += launch_push<float>(g, S, 1, ctx->tuner.shape(), st);
+    for (auto& S : pop_sets(ctx->p64)) n += launch_push<double>(g, S, 1, ctx->tuner.shape(), st);
     n += launch_j_finalize(g, (ctx->cfg.flags & IPIC3D_F_J_DIV8) != 0, !ctx->fp32, st);
     ctx->j_valid = true;
     return check_launch(ctx, n);
@@ -864,9 +872,12 @@ int move_impl(ipic3d_ctx* ctx, bool deposit) {
     }
     const auto s32 = pop_sets(ctx->p32);
     const auto s64 = pop_sets(ctx->p64);
+    const PushShape shp = ctx->tuner.next();
     ph_begin(ctx, IPIC3D_PHASE_PUSH);
-    for (auto& S : s32) n += launch_push<float>(g, S, 0, st);
-    for (auto& S : s64) n += launch_push<double>(g, S, 0, st);
+    if (ctx->tune_timing) CU(cudaEventRecord(ctx->tune_ev[0], st));
+    for (auto& S : s32) n += launch_push<float>(g, S, 0, shp, st);
+    for (auto& S : s64) n += launch_push<double>(g, S, 0, shp, st);
+    if (ctx->tune_timing) CU(cudaEventRecord(ctx->tune_ev[1], st));
     ph_end(ctx, IPIC3D_PHASE_PUSH);
     ctx->push_particles = ctx->particles_hint;
     ph_begin(ctx, IPIC3D_PHASE_PENDING);
@@ -903,6 +914,74 @@ int move_impl(ipic3d_ctx* ctx, bool deposit) {
         ph_end(ctx, IPIC3D_PHASE_MOMENTS);
     }
     return check_launch(ctx, n);
+}
+
+// ---- push-shape autotuning ---------------------------------------------------
+// Shapes the autotuner chose, per device and workload: a later context or
+// batch with the same workload starts from the cached shape without trials.
+using TuneKey = std::vector<int64_t>;
+std::mutex g_tune_mu;
+std::map<TuneKey, std::pair<PushShape, float>> g_tune_cache;
+
+int ilog2(uint64_t n) {
+    int k = 0;
+    while (n >>= 1) ++k;
+    return k;
+}
+
+// what a shape's speed depends on: the grid, the populations, the particle
+// count (to a factor of two), the mover, the deposit, the boundaries
+TuneKey tune_key(int dev, int kind, int64_t a, int64_t b, int64_t c, int pops, uint64_t particles,
+                 const ipic3d_config& cfg) {
+    TuneKey k{dev, kind, a, b, c, pops, ilog2(particles), cfg.mover, cfg.projector, cfg.solver, (int64_t)cfg.flags};
+    for (int ax = 0; ax < 3; ++ax) {
+        k.push_back(cfg.bc_low[ax]);
+        k.push_back(cfg.bc_high[ax]);
+    }
+    return k;
+}
+
+bool tune_lookup(const TuneKey& k, PushTuner& t) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune_cache.find(k);
+    if (it == g_tune_cache.end()) return false;
+    t.adopt(it->second.first, it->second.second);
+    return true;
+}
+
+void tune_store(const TuneKey& k, const PushTuner& t) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune_cache[k] = {t.shape(), t.best_ms()};
+}
+
+TuneKey ctx_tune_key(const ipic3d_ctx* ctx) {
+    return tune_key(ctx->device, 0, ctx->props.size[0], ctx->props.size[1], ctx->props.size[2], ctx->npops(),
+                    ctx->particles_hint, ctx->cfg);
+}
+
+// Before a run of steps: a tuning pass starts (or a cached shape is taken)
+// when the FP32 context tunes its shape and has particles it was not tuned
+// for (none yet, or a count off by more than a factor of two).
+void tune_prepare(ipic3d_ctx* ctx) {
+    if (!ctx->fp32 || ctx->cfg.block_size != 0 || ctx->shape_fixed || ctx->tuner.running()) return;
+    const uint64_t n = ctx->particles_hint, t = ctx->tuned_particles;
+    if (n == 0 || (t && n <= 2 * t && 2 * n >= t)) return;
+    ctx->tuned_particles = n;
+    drop_graph(ctx);  // captured with the previous shape
+    if (!tune_lookup(ctx_tune_key(ctx), ctx->tuner)) ctx->tuner.start(push32_blocks_per_sm(ctx->device));
+}
+
+// After a trial step: its push time to the tuner; a finished pass is cached.
+int tune_record(ipic3d_ctx* ctx) {
+    CU(cudaEventSynchronize(ctx->tune_ev[1]));
+    float ms = 0.f;
+    CU(cudaEventElapsedTime(&ms, ctx->tune_ev[0], ctx->tune_ev[1]));
+    ctx->tuner.record(ms);
+    if (!ctx->tuner.running()) {
+        tune_store(ctx_tune_key(ctx), ctx->tuner);
+        drop_graph(ctx);
+    }
+    return IPIC3D_OK;
 }
 
 // One timestep's kernel sequence (the body the graph captures).
@@ -995,6 +1074,8 @@ int destroy_impl(ipic3d_ctx* ctx) {
     for (auto& pair : ctx->ph_ev)
         for (auto& e : pair)
             if (e) cudaEventDestroy(e);
+    for (auto& e : ctx->tune_ev)
+        if (e) cudaEventDestroy(e);
     if (ctx->stream && ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return IPIC3D_OK;
@@ -1078,6 +1159,7 @@ int create_impl(const ipic3d_props* props, const ipic3d_config* cfg, cudaStream_
     CUB(cudaMallocHost(&ctx->h_pending, 2 * kMaxPops * sizeof(uint32_t)));
     std::memset(ctx->h_pending, 0, 2 * kMaxPops * sizeof(uint32_t));
     for (auto& e : ctx->pend_ev) CUB(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (auto& e : ctx->tune_ev) CUB(cudaEventCreate(&e));
 #undef CUB
     refresh_geom(ctx);
     // an empty particle set so that every call works before the first upload
@@ -1244,8 +1326,16 @@ int ipic3d_gpu_step(ipic3d_ctx* ctx, uint64_t num_steps) {
     // re-lay out when more than 0.5% of the particles wait for a slot
     const uint64_t pend_limit = std::max<uint64_t>(64, ctx->particles_hint / 200);
     uint64_t watch_from = 0;  // first step whose pending count is still meaningful
+    tune_prepare(ctx);
     for (uint64_t done = 0; done < num_steps;) {
-        if (use_graph) {
+        if (ctx->tuner.running()) {  // a trial step of the autotuner: outside the graph, push timed
+            ctx->tune_timing = true;
+            rc = enqueue_step(ctx);
+            ctx->tune_timing = false;
+            if (rc) return rc;
+            if ((rc = ph_collect(ctx))) return rc;
+            if ((rc = tune_record(ctx))) return rc;
+        } else if (use_graph) {
             if (!ctx->graph_valid) {
                 cudaGraph_t graph = nullptr;
                 CU(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
@@ -1421,6 +1511,44 @@ int ipic3d_gpu_profile_read(ipic3d_ctx* ctx, ipic3d_profile* out, int reset) {
     return IPIC3D_OK;
 }
 
+int ipic3d_gpu_get_push_shape(ipic3d_ctx* ctx, ipic3d_push_shape* out) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!out) return fail(IPIC3D_E_INVALID, "out == NULL");
+    std::memset(out, 0, sizeof(*out));
+    const PushShape& s = ctx->tuner.shape();
+    out->item = s.item;
+    out->item_cells = s.item_cells;
+    out->blocks_per_sm = s.per_sm;
+    out->tuned = ctx->tuner.tuned() ? 1 : 0;
+    out->tuning = ctx->tuner.running() ? 1 : 0;
+    out->trials = ctx->tuner.trials();
+    out->push_ms = ctx->tuner.best_ms();
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_set_push_shape(ipic3d_ctx* ctx, const ipic3d_push_shape* shape) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    drop_graph(ctx);  // captured with the previous shape
+    if (shape) {
+        if (shape->item <= 0 || shape->item_cells < 0 || shape->blocks_per_sm <= 0)
+            return fail(IPIC3D_E_INVALID, "push shape: item and blocks_per_sm must be positive, item_cells >= 0");
+        ctx->tuner.fix(PushShape{shape->item, shape->item_cells, shape->blocks_per_sm});
+        ctx->shape_fixed = true;
+        return IPIC3D_OK;
+    }
+    ctx->shape_fixed = false;
+    ctx->tuned_particles = 0;
+    if (ctx->fp32 && ctx->particles_hint > 0) {
+        ctx->tuned_particles = ctx->particles_hint;
+        ctx->tuner.start(push32_blocks_per_sm(ctx->device));
+    } else {
+        ctx->tuner.fix(kDefaultPushShape);
+    }
+    return IPIC3D_OK;
+}
+
 int ipic3d_gpu_boris(ipic3d_particle* particles, uint64_t n, const double E[3], const double B[3], double dt,
                      uint64_t nsteps, int push_position) {
     if (!particles || !E || !B) return fail(IPIC3D_E_INVALID, "NULL argument");
@@ -1484,9 +1612,19 @@ struct ipic3d_batch {
     bool graph_valid = false;
     uint64_t graph_kernels = 0;
     uint64_t steps = 0, launches = 0;
+    // launch shape of the FP32 batched push (autotuned as a context's)
+    PushTuner tuner;
+    bool tune_started = false;
+    bool tune_timing = false;
+    cudaEvent_t tune_ev[2] = {nullptr, nullptr};
 };
 
 namespace {
+
+TuneKey batch_tune_key(const ipic3d_batch* b, uint64_t particles, int64_t cells) {
+    return tune_key(b->device, 1, (int64_t)b->inst.size(), cells, 0, (int)(b->fp32 ? b->j32.size() : b->j64.size()),
+                    particles, b->cfg);
+}
 
 void batch_drop_graph(ipic3d_batch* b) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
@@ -1615,7 +1753,9 @@ int batch_enqueue_step(ipic3d_batch* b) {
     }
     n += launch_batch_begin<T>(jobs, nj, b->d_inst, ni, b->max_nodes, deposit, b->d_flag, st);
     if (nj > 0) {
-        n += launch_push_batch<T>(jobs, b->d_cta, b->nctas, 0, jobs_of<T>(b)[0].g, st);
+        if (b->tune_timing) CU(cudaEventRecord(b->tune_ev[0], st));
+        n += launch_push_batch<T>(jobs, b->d_cta, b->nctas, 0, jobs_of<T>(b)[0].g, b->tuner.next(), st);
+        if (b->tune_timing) CU(cudaEventRecord(b->tune_ev[1], st));
         n += launch_push_pending_batch<T>(jobs, nj, st);
         n += launch_place_batch<T>(jobs, nj, st);
         n += launch_pending_rotate_batch<T>(jobs, nj, st);
@@ -1673,9 +1813,44 @@ int batch_run(ipic3d_batch* b, uint64_t num_steps) {
     if ((rc = batch_tables<T>(b))) return rc;
     const bool use_graph = (b->cfg.flags & IPIC3D_F_USE_GRAPH) != 0;
     cudaStream_t st = b->stream;
+    // the first batched run with particles tunes the push shape (or takes a
+    // cached one)
+    if (b->fp32 && b->cfg.block_size == 0 && !b->tune_started && !jobs_of<T>(b).empty()) {
+        uint64_t particles = 0;
+        int64_t cells = 0;
+        for (auto* c : b->inst) {
+            particles += c->particles_hint;
+            cells += c->ncells();
+        }
+        if (particles > 0) {
+            b->tune_started = true;
+            batch_drop_graph(b);
+            if (!tune_lookup(batch_tune_key(b, particles, cells), b->tuner))
+                b->tuner.start(push32_blocks_per_sm(b->device));
+        }
+    }
     uint64_t watch_from = 0;
     for (uint64_t done = 0; done < num_steps;) {
-        if (use_graph) {
+        if (b->tuner.running()) {  // a trial step of the autotuner: outside the graph, push timed
+            b->tune_timing = true;
+            rc = batch_enqueue_step<T>(b);
+            b->tune_timing = false;
+            if (rc) return rc;
+            CU(cudaEventSynchronize(b->tune_ev[1]));
+            float ms = 0.f;
+            CU(cudaEventElapsedTime(&ms, b->tune_ev[0], b->tune_ev[1]));
+            b->tuner.record(ms);
+            if (!b->tuner.running()) {
+                uint64_t particles = 0;
+                int64_t cells = 0;
+                for (auto* c : b->inst) {
+                    particles += c->particles_hint;
+                    cells += c->ncells();
+                }
+                tune_store(batch_tune_key(b, particles, cells), b->tuner);
+                batch_drop_graph(b);
+            }
+        } else if (use_graph) {
             if (!b->graph_valid) {
                 cudaGraph_t graph = nullptr;
                 CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -1744,6 +1919,8 @@ void batch_free(ipic3d_batch* b) {
     if (b->h_flag) cudaFreeHost(b->h_flag);
     for (auto& e : b->flag_ev)
         if (e) cudaEventDestroy(e);
+    for (auto& e : b->tune_ev)
+        if (e) cudaEventDestroy(e);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }
@@ -1775,6 +1952,8 @@ int ipic3d_gpu_batch_create(uint32_t count, const ipic3d_props* props, const ipi
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_flag, 2 * sizeof(uint32_t));
     for (auto& ev : b->flag_ev)
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    for (auto& ev : b->tune_ev)
+        if (e == cudaSuccess) e = cudaEventCreate(&ev);
     if (e != cudaSuccess)
         return bail(fail(e == cudaErrorMemoryAllocation ? IPIC3D_E_NOMEM : IPIC3D_E_CUDA, "batch: %s",
                          cudaGetErrorString(e)));
@@ -1858,6 +2037,22 @@ int ipic3d_gpu_batch_stats(ipic3d_batch* b, ipic3d_stats* out) {
     }
     out->steps = b->steps;
     out->kernel_launches = b->launches;
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_batch_get_push_shape(ipic3d_batch* b, ipic3d_push_shape* out) {
+    int rc = batch_check(b);
+    if (rc) return rc;
+    if (!out) return fail(IPIC3D_E_INVALID, "out == NULL");
+    std::memset(out, 0, sizeof(*out));
+    const PushShape& s = b->tuner.shape();
+    out->item = s.item;
+    out->item_cells = s.item_cells;
+    out->blocks_per_sm = s.per_sm;
+    out->tuned = b->tuner.tuned() ? 1 : 0;
+    out->tuning = b->tuner.running() ? 1 : 0;
+    out->trials = b->tuner.trials();
+    out->push_ms = b->tuner.best_ms();
     return IPIC3D_OK;
 }
 

@@ -10,8 +10,9 @@ namespace ipg {
 
 // particles (particles_fp64.cu / particles_fp32.cu); the PopSet launchers
 // advance all populations of a set with one launch
+// `shp`: launch shape of the FP32 push (the FP64 push has one shape)
 template <typename T>
-int launch_push(const Geom& g, const PopSet<T>& S, int mode, cudaStream_t st);
+int launch_push(const Geom& g, const PopSet<T>& S, int mode, const PushShape& shp, cudaStream_t st);
 template <typename T>
 int launch_push_pending(const Geom& g, const PopSet<T>& S, cudaStream_t st);
 template <typename T>
@@ -31,7 +32,7 @@ int launch_pending_count(const Pop<T>& P, int32_t* per_cell, cudaStream_t st);
 // batched ensemble: job tables built by the host (particles_fp64/32.cu)
 template <typename T>
 int launch_push_batch(const PopJob<T>* jobs, const int2* cta_job, int64_t nctas, int mode, const Geom& g0,
-                      cudaStream_t st);  // g0: the policy fields (mover, flags, deposit) shared by the jobs
+                      const PushShape& shp, cudaStream_t st);  // g0: the policy fields (mover, flags, deposit) shared by the jobs
 template <typename T>
 int launch_push_pending_batch(const PopJob<T>* jobs, int njobs, cudaStream_t st);
 template <typename T>
@@ -48,6 +49,7 @@ int launch_batch_status(const PopJob<T>* jobs, int njobs, JobStatus* out, cudaSt
 int launch_cell_coef_batch(const InstJob* inst, int ninst, int64_t max_cells, cudaStream_t st);  // particles_fp32.cu
 Push32Const push32_const(const Geom& g, const Pop<float>& P);                                    // particles_fp32.cu
 cudaError_t init_push32(int dev);  // once per device, before any capture (particles_fp32.cu)
+int push32_blocks_per_sm(int dev);  // resident pipelined-push blocks per SM (after init_push32)
 int launch_ghost_batch(const InstJob* jobs, int ninst, int max_s, cudaStream_t st);              // fields.cu
 int launch_leapfrog_batch(const InstJob* jobs, int ninst, int max_s, bool refresh_node_b, cudaStream_t st);
 int launch_forward_batch(const InstJob* jobs, int ninst, int max_s, cudaStream_t st);

@@ -1,5 +1,6 @@
 // FP32 particle kernels: positions relative to the cell origin, FP32 push
 // with fused multiply-adds, FP64 node accumulation of the deposit.
+#include <algorithm>
 #include <mutex>
 
 #include "particles_impl.cuh"
@@ -13,10 +14,11 @@ constexpr int kMaxDevices = 64;
 constexpr int kPipeStages = 3;  // shared-memory stages per CTA (2 CTAs per SM)
 std::mutex g_pipe_mu;
 bool g_pipe_ready[kMaxDevices] = {};
-int g_pipe_grid[kMaxDevices] = {};  // persistent CTAs of the pipelined push
+int g_pipe_per_sm[kMaxDevices] = {};  // resident blocks per SM of the pipelined push
+int g_pipe_sms[kMaxDevices] = {};
 
-using PipeFn = void (*)(Geom, PopSet<float>, Push32Set, TileMap);
-using PipeJobsFn = void (*)(const PopJob<float>*, const int2*, int);
+using PipeFn = void (*)(Geom, PopSet<float>, Push32Set, TileMap, PushShape);
+using PipeJobsFn = void (*)(const PopJob<float>*, const int2*, int, PushShape);
 
 // The compile-time policies that are instantiated (kPipe* bit sets): the
 // step with the dipole mover, the field-gather mover with or without the
@@ -105,10 +107,44 @@ cudaError_t init_push32(int dev) {
     int sms = 0;
     cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    g_pipe_grid[dev] = (min_per_sm > 0 ? min_per_sm : 1) * sms;
+    g_pipe_per_sm[dev] = min_per_sm > 0 ? min_per_sm : 1;
+    g_pipe_sms[dev] = sms;
     g_pipe_ready[dev] = true;
     return cudaSuccess;
 }
+
+int push32_blocks_per_sm(int dev) {
+    if (dev < 0 || dev >= kMaxDevices) return 1;
+    std::lock_guard<std::mutex> lock(g_pipe_mu);
+    return g_pipe_per_sm[dev] > 0 ? g_pipe_per_sm[dev] : 1;
+}
+
+namespace {
+// Persistent grid of the pipelined push on the current device: shp.per_sm
+// blocks per SM (at most the resident count), no more than the tiles.
+// Without init_push32 on this device the launch fails (no shared-memory
+// opt-in) and the caller reports it.
+int pipe_grid(const PushShape& shp, int64_t tiles) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int per_sm = 1, sms = 1;
+    if (dev >= 0 && dev < kMaxDevices && g_pipe_sms[dev] > 0) {
+        per_sm = std::max(1, std::min(shp.per_sm, g_pipe_per_sm[dev]));
+        sms = g_pipe_sms[dev];
+    }
+    return (int)std::min<int64_t>((int64_t)per_sm * sms, tiles);
+}
+
+// the device-side limits of a shape (item a power of two from 32 to a
+// tile, item mode only where the cells' coefficients fit the stage)
+PushShape clamp_shape(PushShape s) {
+    int item = 32;
+    while (item * 2 <= std::min(kTileSlots, s.item)) item *= 2;
+    s.item = item;
+    s.item_cells = std::max(0, std::min(kItemMaxCells, s.item_cells));
+    return s;
+}
+}  // namespace
 
 Push32Const push32_const(const Geom& g, const Pop<float>& P) {
     Push32Const pc;
@@ -131,7 +167,7 @@ Push32Const push32_const(const Geom& g, const Pop<float>& P) {
 // the FP32 step: the pipelined persistent push (push32_pipe.cuh), the
 // instance of the step's policies, one launch for all populations of S
 template <>
-int launch_push<float>(const Geom& g, const PopSet<float>& S, int mode, cudaStream_t st) {
+int launch_push<float>(const Geom& g, const PopSet<float>& S, int mode, const PushShape& shp, cudaStream_t st) {
     if (mode != 0 && !g.deposit) return 0;  // nothing to deposit
     PipeFn fn = pipe_kernel(pipe_policy(g, mode));
     if (!fn || S.n <= 0) return 0;
@@ -144,12 +180,8 @@ int launch_push<float>(const Geom& g, const PopSet<float>& S, int mode, cudaStre
     }
     const int tiles = tm.first[S.n];
     if (tiles <= 0) return 0;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    int grid = g_pipe_grid[dev];
-    if (grid <= 0) grid = 1;  // init_push32 did not run on this device: the launch fails (no shared-memory opt-in)
-    if (grid > tiles) grid = tiles;
-    fn<<<grid, kPipeThreads, pipe_smem_bytes<kPipeStages>(), st>>>(g, S, pcs, tm);
+    fn<<<pipe_grid(shp, tiles), kPipeThreads, pipe_smem_bytes<kPipeStages>(), st>>>(g, S, pcs, tm,
+                                                                                    clamp_shape(shp));
     return 1;
 }
 
@@ -181,17 +213,13 @@ int launch_cell_coef(const Geom& g, float* coef, cudaStream_t st) {
 // the batched FP32 step: the pipelined push over every job's tiles
 template <>
 int launch_push_batch<float>(const PopJob<float>* jobs, const int2* cta_job, int64_t nctas, int mode,
-                             const Geom& g0, cudaStream_t st) {
+                             const Geom& g0, const PushShape& shp, cudaStream_t st) {
     if (nctas <= 0) return 0;
     if (mode != 0 && !g0.deposit) return 0;
     PipeJobsFn fn = pipe_jobs_kernel(pipe_policy(g0, mode));
     if (!fn) return 0;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    int grid = g_pipe_grid[dev];
-    if (grid <= 0) grid = 1;  // init_push32 did not run on this device: the launch fails (no shared-memory opt-in)
-    if (grid > nctas) grid = (int)nctas;
-    fn<<<grid, kPipeThreads, pipe_smem_bytes<kPipeStages>(), st>>>(jobs, cta_job, (int)nctas);
+    fn<<<pipe_grid(shp, nctas), kPipeThreads, pipe_smem_bytes<kPipeStages>(), st>>>(jobs, cta_job, (int)nctas,
+                                                                                    clamp_shape(shp));
     return 1;
 }
 

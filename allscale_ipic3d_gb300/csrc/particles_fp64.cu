@@ -5,7 +5,7 @@
 
 namespace ipg {
 template <>
-int launch_push<double>(const Geom& g, const PopSet<double>& S, int mode, cudaStream_t st) {
+int launch_push<double>(const Geom& g, const PopSet<double>& S, int mode, const PushShape&, cudaStream_t st) {
     return launch_push_generic<double>(g, S, mode, st);
 }
 template <>
@@ -21,7 +21,7 @@ template int launch_pending_count<double>(const Pop<double>&, int32_t*, cudaStre
 
 template <>
 int launch_push_batch<double>(const PopJob<double>* jobs, const int2* cta_job, int64_t nctas, int mode,
-                              const Geom&, cudaStream_t st) {
+                              const Geom&, const PushShape&, cudaStream_t st) {
     return launch_push_batch_generic<double>(jobs, cta_job, nctas, mode, st);
 }
 template <>

@@ -7,11 +7,6 @@
 
 namespace ipg {
 
-template <typename T>
-int launch_push(const Geom& g, const PopSet<T>& S, int mode, cudaStream_t st);
-template <typename T>
-int launch_push_pending(const Geom& g, const PopSet<T>& S, cudaStream_t st);
-
 // generic versions (the FP64 path); particles_fp32.cu specialises both
 template <typename T>
 int launch_push_generic(const Geom& g, const PopSet<T>& S, int mode, cudaStream_t st) {
@@ -169,10 +164,6 @@ __global__ void k_batch_status(const PopJob<T>* __restrict__ jobs, int njobs, Jo
     s.pad = 0;
     out[j] = s;
 }
-
-template <typename T>
-int launch_push_batch(const PopJob<T>* jobs, const int2* cta_job, int64_t nctas, int mode, const Geom& g0,
-                      cudaStream_t st);
 
 template <typename T>
 int launch_push_batch_generic(const PopJob<T>* jobs, const int2* cta_job, int64_t nctas, int mode, cudaStream_t st) {

@@ -117,9 +117,9 @@ constexpr int kComputeWarps = 11;
 constexpr int kComputeThreads = kComputeWarps * 32;
 constexpr int kPipeThreads = kComputeThreads + 32;  // + the producer warp
 constexpr int kSlotWarps = kTileSlots / 128;        // slot mode: 128-slot slices of a tile
-constexpr int kItemSlots = 256;                     // particles per item (8 per lane)
-
-constexpr int kItemMaxCells = 32;  // tiles of at most this many cells run in item mode
+// item mode (tiles of at most PushShape::item_cells cells, work items of
+// PushShape::item particles): the cells' field coefficients are staged
+constexpr int kItemMaxCells = 32;
 
 // Every member is a bulk-copy destination: 16-byte aligned offsets.
 struct __align__(16) PipeStage {
@@ -184,9 +184,9 @@ __device__ __forceinline__ TileCopy tile_copy(const Pop<float>& P, int tile, int
 // with `coef` (item mode, field gather) also the cells' field coefficients
 // (48 floats = 192 bytes per cell, contiguous from cell c0).
 __device__ __forceinline__ void issue_tile(const Pop<float>& P, const float* coef, int tile, int2 desc,
-                                           PipeStage& st, uint64_t* bar, uint32_t extra = 0) {
+                                           int item_cells, PipeStage& st, uint64_t* bar, uint32_t extra = 0) {
     const TileCopy t = tile_copy(P, tile, desc);
-    const bool with_coef = coef != nullptr && desc.y <= kItemMaxCells;
+    const bool with_coef = coef != nullptr && desc.y <= item_cells;
     const uint32_t coef_bytes = with_coef ? (uint32_t)desc.y * 192u : 0u;
     mbar_arrive_expect_tx(bar, 6u * t.slot_bytes + t.s_bytes + t.c_bytes + coef_bytes + extra);
     float* const arr[6] = {P.x, P.y, P.z, P.u, P.v, P.w};
@@ -465,7 +465,7 @@ __device__ __forceinline__ void leave_and_hole(const Geom& g, const Pop<float>& 
 }
 
 // Item mode: the warp pushes particles [a, b) (tile-local slots, b - a <=
-// kItemSlots) of cell `cell`, lane l taking a + l, a + l + 32, ... A first
+// PushShape::item) of cell `cell`, lane l taking a + l, a + l + 32, ... A first
 // pass moves them: stayers go back to HBM with coalesced stores (and to the
 // stage for the second pass), the slots of leavers and drops are marked
 // (NaN position). The second pass sums the stayers' cloud-in-cell moments
@@ -634,12 +634,12 @@ __device__ __forceinline__ void push_slots(const Geom& g, const Pop<float>& P, c
 // One compute warp's share of the tile in `st`.
 template <int kF>
 __device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& P, const Push32Const& pc, int tile,
-                                               int2 desc, PipeStage& st, int* next_item, uint32_t& nmig,
-                                               uint32_t& nrem) {
+                                               int2 desc, const PushShape& shp, PipeStage& st, int* next_item,
+                                               uint32_t& nmig, uint32_t& nrem) {
     const int lane = threadIdx.x & 31;
     const int base = tile * kTileSlots;
     const int c0 = desc.x, nc = desc.y;
-    if (nc > kItemMaxCells) {
+    if (nc > shp.item_cells) {
         for (int w = threadIdx.x >> 5; w < kSlotWarps; w += kComputeWarps)
             push_slots<kF>(g, P, pc, st, base, desc, w, nmig, nrem);
         return;
@@ -655,7 +655,8 @@ __device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& 
         lo = l < 0 ? 0 : l;
         hi = h > kTileSlots ? kTileSlots : h;
     }
-    const int items = hi > lo ? (hi - lo + kItemSlots - 1) / kItemSlots : 0;
+    const int sh = 31 - __clz(shp.item);  // items of 2^sh particles
+    const int items = hi > lo ? (hi - lo + (1 << sh) - 1) >> sh : 0;
     int incl = items;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -674,8 +675,8 @@ __device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& 
         const int clo = __shfl_sync(0xffffffffu, lo, src), chi = __shfl_sync(0xffffffffu, hi, src);
         const int cex = __shfl_sync(0xffffffffu, excl, src);
         const int cstart = __shfl_sync(0xffffffffu, cst, src);
-        const int a = clo + (j - cex) * kItemSlots;
-        const int b = a + kItemSlots < chi ? a + kItemSlots : chi;
+        const int a = clo + ((j - cex) << sh);
+        const int b = a + (1 << sh) < chi ? a + (1 << sh) : chi;
         push_item<kF>(g, P, pc, st, st.coef + src * 48, base, c0 + src, cstart, a, b, nmig, nrem);
     }
 }
@@ -705,11 +706,11 @@ __device__ __forceinline__ void flush_counts(StepCounters* ctr, uint32_t& nmig, 
 
 // The persistent kernel: CTA b pushes tiles b, b + G, b + 2G, ... (G =
 // gridDim.x) of the populations of S, numbered through tm, with kStages
-// shared-memory stages in flight.
+// shared-memory stages in flight; `shp` splits the tiles into work.
 template <int kStages, int kMinBlocks, int kF>
 __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
     k_push32_pipe(Geom g, const __grid_constant__ PopSet<float> S, const __grid_constant__ Push32Set pcs,
-                  const __grid_constant__ TileMap tm) {
+                  const __grid_constant__ TileMap tm, PushShape shp) {
     constexpr bool kStep = (kF & kPipeStep) != 0;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     PipeSmem<kStages>& sm = *reinterpret_cast<PipeSmem<kStages>*>(smem_raw);
@@ -740,7 +741,7 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
             sm.desc[s] = d;
             sm.pop[s] = pi;
             sm.next_item[s] = 0;
-            issue_tile(S.p[pi], coef, t - tm.first[pi], d, sm.stage[s], &sm.full[s]);
+            issue_tile(S.p[pi], coef, t - tm.first[pi], d, shp.item_cells, sm.stage[s], &sm.full[s]);
         };
         int issued = 0;  // tiles of this CTA whose copies were issued
         for (int s = 0; s < kStages; ++s) {
@@ -761,7 +762,7 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
             }
             // slot mode writes the tile back from the stage; item mode's warps
             // stored their stayers themselves
-            const bool store = kStep && sm.desc[s].y > kItemMaxCells;
+            const bool store = kStep && sm.desc[s].y > shp.item_cells;
             if (store) {
                 const Pop<float>& P = S.p[sm.pop[s]];
                 const TileCopy c = tile_copy(P, t - tm.first[sm.pop[s]], sm.desc[s]);
@@ -806,8 +807,8 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
             if (cur >= 0) flush_counts(S.p[cur].ctr, nmig, nrem);
             cur = pi;
         }
-        push_tile_warp<kF>(g, S.p[pi], pcs.c[pi], t - tm.first[pi], sm.desc[s], sm.stage[s], &sm.next_item[s],
-                           nmig, nrem);
+        push_tile_warp<kF>(g, S.p[pi], pcs.c[pi], t - tm.first[pi], sm.desc[s], shp, sm.stage[s],
+                           &sm.next_item[s], nmig, nrem);
         fence_proxy_async_smem();  // this warp's writes to the stage, before the bulk stores read it
         __syncwarp();
         if (lane == 0) mbar_arrive(&sm.empty[s]);
@@ -821,7 +822,8 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
 // stage, and the compute warps read everything about the tile from there.
 template <int kStages, int kMinBlocks, int kF>
 __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
-    k_push32_pipe_jobs(const PopJob<float>* __restrict__ jobs, const int2* __restrict__ cta_job, int ntiles) {
+    k_push32_pipe_jobs(const PopJob<float>* __restrict__ jobs, const int2* __restrict__ cta_job, int ntiles,
+                       PushShape shp) {
     constexpr bool kStep = (kF & kPipeStep) != 0;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     PipeSmem<kStages>& sm = *reinterpret_cast<PipeSmem<kStages>*>(smem_raw);
@@ -851,7 +853,7 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
             sm.pop[s] = cj.x;
             sm.ltile[s] = cj.y;
             sm.next_item[s] = 0;
-            issue_tile(P, coef, cj.y, d, sm.stage[s], &sm.full[s], (uint32_t)sizeof(PopJob<float>));
+            issue_tile(P, coef, cj.y, d, shp.item_cells, sm.stage[s], &sm.full[s], (uint32_t)sizeof(PopJob<float>));
             bulk_load(&sm.stage[s].job, J, (uint32_t)sizeof(PopJob<float>), &sm.full[s]);
         };
         int issued = 0;
@@ -869,7 +871,7 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
                 failed = true;
                 break;
             }
-            const bool store = kStep && sm.desc[s].y > kItemMaxCells;
+            const bool store = kStep && sm.desc[s].y > shp.item_cells;
             if (store) {
                 const Pop<float>& P = sm.stage[s].job.P;
                 const TileCopy c = tile_copy(P, sm.ltile[s], sm.desc[s]);
@@ -910,7 +912,8 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
             if (cur) flush_counts(cur, nmig, nrem);
             cur = J.P.ctr;
         }
-        push_tile_warp<kF>(J.g, J.P, J.pc, sm.ltile[s], sm.desc[s], sm.stage[s], &sm.next_item[s], nmig, nrem);
+        push_tile_warp<kF>(J.g, J.P, J.pc, sm.ltile[s], sm.desc[s], shp, sm.stage[s], &sm.next_item[s], nmig,
+                           nrem);
         fence_proxy_async_smem();
         __syncwarp();
         if (lane == 0) mbar_arrive(&sm.empty[s]);

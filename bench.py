@@ -155,10 +155,30 @@ def profiled_traffic(precision):
     return None
 
 
-def run_timed(sim, warmup, steps, sampler=None):
-    """W untimed steps, then K steps bracketed by CUDA events on the
-    library's stream (synchronised on both sides)."""
+def autotune(sim, limit=100):
+    """The push-shape autotuner's trial steps (FP32 contexts): ordinary steps
+    of the simulation, run before the warm-up and outside any timing, until
+    the shape is chosen. Returns the steps run."""
+    n = 0
+    while n < limit:
+        sim.step(1)
+        n += 1
+        if not sim.push_shape()["tuning"]:
+            break
+    return n
+
+
+def run_timed(sim, warmup, steps, sampler=None, pre_steps=None):
+    """The autotuner's trial steps (or `pre_steps` untimed steps, to keep
+    another precision at the same step count), W untimed steps, then K steps
+    bracketed by CUDA events on the library's stream (synchronised on both
+    sides). Returns (ms, particle-steps, launches, particles, steps before
+    the warm-up)."""
     import torch
+    if pre_steps is None:
+        pre_steps = autotune(sim)
+    else:
+        sim.step(pre_steps)
     sim.step(warmup)
     sim.synchronize()
     n0 = sim.particle_count()
@@ -175,7 +195,7 @@ def run_timed(sim, warmup, steps, sampler=None):
     ms = e0.elapsed_time(e1)
     n1 = sim.particle_count()
     launches = sim.stats()["kernel_launches"] - l0
-    return ms, 0.5 * (n0 + n1) * steps, launches, n0
+    return ms, 0.5 * (n0 + n1) * steps, launches, n0, pre_steps
 
 
 class _Null:
@@ -311,8 +331,14 @@ def ensemble_config(precision):
                            projector=abi.PROJECT_CIC, bc=abi.BC_PERIODIC, flags=abi.F_USE_GRAPH)
 
 
-def timed_batch(batch, warmup, steps, sampler=None):
+def timed_batch(batch, warmup, steps, sampler=None, pre_steps=None):
+    """As run_timed, for a batch: the autotuner's trial steps (or
+    `pre_steps`), W warm-up steps, K timed steps."""
     import torch
+    if pre_steps is None:
+        pre_steps = autotune(batch)
+    else:
+        batch.step(pre_steps)
     batch.step(warmup)
     batch.synchronize()
     st = torch.cuda.ExternalStream(batch.stream)
@@ -327,7 +353,7 @@ def timed_batch(batch, warmup, steps, sampler=None):
         e1.synchronize()
     torch.cuda.synchronize()
     s = batch.stats()
-    return e0.elapsed_time(e1), 0.5 * (n0 + s["particles"]) * steps, s["kernel_launches"] - l0
+    return e0.elapsed_time(e1), 0.5 * (n0 + s["particles"]) * steps, s["kernel_launches"] - l0, pre_steps
 
 
 def timed_plain(batch, count, steps):
@@ -337,6 +363,9 @@ def timed_plain(batch, count, steps):
     st = torch.cuda.ExternalStream(batch.stream)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     us = [batch.universe(i) for i in range(count)]
+    for u in us:  # untimed: each universe's autotuning and graph capture
+        autotune(u)
+        u.step(1)
     n0 = sum(u.particle_count() for u in us)
     torch.cuda.synchronize()
     e0.record(st)
@@ -369,8 +398,8 @@ def run_ensemble(count, warmup, steps, local):
     cells = int(sum(p.ncells for p in props))
     setup_s = time.perf_counter() - t_setup
     sampler = ClockSampler(local)
-    ms32, ps32, launches32 = timed_batch(b32, warmup, steps, sampler)
-    ms64, ps64, _ = timed_batch(b64, warmup, steps)
+    ms32, ps32, launches32, pre = timed_batch(b32, warmup, steps, sampler)
+    ms64, ps64, _, _ = timed_batch(b64, warmup, steps, pre_steps=pre)
     rel, lost = [], 0
     for i in range(count):
         c32, c64 = b32.universe(i).conserved(), b64.universe(i).conserved()
@@ -385,16 +414,18 @@ def run_ensemble(count, warmup, steps, local):
     msp32, psp32 = timed_plain(b32, count, steps)
     v32, v64 = ps32 / (ms32 * 1e-3), ps64 / (ms64 * 1e-3)
     vp64, vp32 = psp64 / (msp64 * 1e-3), psp32 / (msp32 * 1e-3)
+    shape32 = b32.push_shape()
     b32.close()
     b64.close()
     return {"workload": ENS_WORKLOAD, "universes": count, "cells": cells, "particles": total,
             "steps": steps, "warmup": warmup, "setup_s": round(setup_s, 1),
-            "fp32_batched": {"value": v32, "ms_per_step": ms32 / steps, "gpu_launches": int(launches32)},
+            "fp32_batched": {"value": v32, "ms_per_step": ms32 / steps, "gpu_launches": int(launches32),
+                             "push_shape": shape32, "autotune_steps": pre},
             "fp64_batched": {"value": v64, "ms_per_step": ms64 / steps},
             "fp64_plain": {"value": vp64, "ms_per_step": msp64 / steps},
             "fp32_plain": {"value": vp32, "ms_per_step": msp32 / steps},
             "fp32_batched_over_fp64_plain": v32 / vp64, "fp32_batched_over_fp64_batched": v32 / v64,
-            "kinetic_energy_rel_fp32_vs_fp64": {"after_steps": warmup + steps, "max": float(rel.max()),
+            "kinetic_energy_rel_fp32_vs_fp64": {"after_steps": pre + warmup + steps, "max": float(rel.max()),
                                                 "median": float(np.median(rel)), "worst": worst,
                                                 "particle_count_differences": lost},
             "stats_fp32": st32, "stats_fp64": st64,
@@ -504,6 +535,7 @@ def run_config(name, warmup, local):
            "warmup": warmup}
     species = sorted({(float(a), float(b)) for a, b in zip(parts["q"][:1000], parts["qom"][:1000])})
     cons = {}
+    pre = None
     for pname, prec in (("fp32", abi.FP32), ("fp64", abi.FP64)):
         sim = g.Simulation(props, abi.Config.make(precision=prec, **kw))
         if fields is not None:
@@ -516,16 +548,18 @@ def run_config(name, warmup, local):
         sim.upload_particles(parts[first], c0)
         sim.upload_particles(parts, counts)
         sampler = ClockSampler(local)
-        ms, ps, launches, n0 = run_timed(sim, warmup, steps, sampler if pname == "fp32" else None)
+        ms, ps, launches, n0, pre = run_timed(sim, warmup, steps, sampler if pname == "fp32" else None, pre)
         res[pname] = {"value": ps / (ms * 1e-3), "ms_per_step": ms / steps, "gpu_launches": int(launches),
                       "stats": sim.stats()}
         if pname == "fp32":
             res["clocks"] = sampler.summary()
+            res["push_shape"] = sim.push_shape()
+            res["autotune_steps"] = pre
         cons[pname] = sim.conserved()
         res[pname]["roofline"] = push_roofline(sim, pname, 5, props, len(species))
         sim.close()
     tot = lambda c: c["kinetic_energy"] + c["e_energy"] + c["b_energy"]
-    res["error_fp32_vs_fp64"] = {"steps": warmup + steps + 5,
+    res["error_fp32_vs_fp64"] = {"steps": pre + warmup + steps + 5,
                                  "total_energy_rel": abs(tot(cons["fp32"]) - tot(cons["fp64"])) / abs(tot(cons["fp64"])),
                                  "kinetic_energy_rel": abs(cons["fp32"]["kinetic_energy"] -
                                                            cons["fp64"]["kinetic_energy"]) /
@@ -606,7 +640,8 @@ def main():
     if dist:
         dist.barrier()
     sampler = ClockSampler(local)
-    ms32, psteps32, launches32, n0 = run_timed(sim32, args.warmup, args.steps, sampler)
+    ms32, psteps32, launches32, n0, tune_steps = run_timed(sim32, args.warmup, args.steps, sampler)
+    shape32 = sim32.push_shape()
     if dist:
         dist.barrier()
         t = torch.tensor([ms32, psteps32], device="cuda", dtype=torch.float64)
@@ -620,7 +655,8 @@ def main():
     if args.only == "fp32":
         roof = push_roofline(sim32, "fp32", 20, props, 2)
         out = {"metric": METRIC, "value": value32, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-               "ms_per_step": ms32 / args.steps, "roofline": roof, "stats": stats32, "gpu_launches": int(launches32)}
+               "ms_per_step": ms32 / args.steps, "roofline": roof, "stats": stats32, "gpu_launches": int(launches32),
+               "push_shape": shape32, "autotune_steps": tune_steps}
         if rank == 0:
             print(json.dumps(out))
         return 0
@@ -628,12 +664,12 @@ def main():
     # ---- FP64 GPU path, same inputs and steps ----
     sim64 = g.Simulation(props, make_config(abi.FP64))
     sim64.upload_particles(parts, counts)
-    ms64, psteps64, _, _ = run_timed(sim64, args.warmup, args.steps)
+    ms64, psteps64, _, _, _ = run_timed(sim64, args.warmup, args.steps, pre_steps=tune_steps)
     # error of the FP32 path against the FP64 GPU path: both ran the same
-    # warm-up + timed steps from the same particles
+    # autotune + warm-up + timed steps from the same particles
     c32, c64 = sim32.conserved(), sim64.conserved()
     tot = lambda c: c["kinetic_energy"] + c["e_energy"] + c["b_energy"]
-    err = {"steps": args.warmup + args.steps,
+    err = {"steps": tune_steps + args.warmup + args.steps,
            "total_energy_rel": abs(tot(c32) - tot(c64)) / abs(tot(c64)),
            "kinetic_energy_rel": abs(c32["kinetic_energy"] - c64["kinetic_energy"]) / abs(c64["kinetic_energy"]),
            "particles_fp32": c32["particles"], "particles_fp64": c64["particles"]}
@@ -693,7 +729,8 @@ def main():
         "config": {"workload": WORKLOAD, "cells": ncells, "particles": int(n0), "precision":
                    "fp32 push/deposit (cell-relative), fp64 node moments/fields/reductions",
                    "l2": "inputs larger than L2: particle state %.0f MB > 129 MB" % (n0 * 24 / 1e6),
-                   "graph": True, "parallelism": "replicas" if world > 1 else "single"},
+                   "graph": True, "parallelism": "replicas" if world > 1 else "single",
+                   "push_shape": shape32, "autotune_steps": tune_steps},
         "roofline": roof,
         "fp64": {"value": value64, "ms_per_step": ms64 / args.steps, "roofline": roof64, "stats": stats64},
         "fp32_over_fp64": value32 / value64,

@@ -103,7 +103,8 @@ typedef struct ipic3d_config {
        cell, plus `slack_min` slots) reserved for arrivals; 0 = defaults.     */
     double slack;
     int32_t slack_min;
-    int32_t block_size;     /* 0 = autotuned launch shape                  */
+    int32_t block_size;     /* 0 = autotuned FP32 push shape, else the
+                               default shape (ipic3d_push_shape)           */
     /* injection at the x=0 face (IPIC3D_F_INJECT_LOW_X, bc_low[0] OPEN):
        expected particles per face cell per step, their q, qom, drift and
        thermal velocities, and the seed of the counter-based generator.      */
@@ -219,6 +220,32 @@ int ipic3d_gpu_profile(ipic3d_ctx* ctx, int enable);
 /* Copies the accumulated times; reset != 0 clears them afterwards. */
 int ipic3d_gpu_profile_read(ipic3d_ctx* ctx, ipic3d_profile* out, int reset);
 
+/* ---- launch shape of the FP32 push (autotuned) ---------------------------- */
+/* No counterpart in the reference (its cell loop is a pfor over the grid,
+ * simulator.h:127-242). The FP32 push walks 1024-slot tiles of the
+ * cell-sorted particles: a tile of at most `item_cells` cells is cut into
+ * work items of `item` particles that warps claim one at a time, a sparser
+ * tile is pushed slot by slot, and `blocks_per_sm` persistent blocks run on
+ * each SM. With block_size 0 in the config, the first steps of a workload
+ * (after an upload with a particle count not seen before, within a factor
+ * of two) are trials of candidate shapes, outside the step graph and each
+ * an ordinary step; the fastest is kept and cached for later contexts of
+ * the same workload. FP64 contexts have one shape and report it untuned. */
+typedef struct ipic3d_push_shape {
+    int32_t item;           /* particles per work item, power of two, 32..1024    */
+    int32_t item_cells;     /* item mode for tiles of at most this many cells, 0..32 */
+    int32_t blocks_per_sm;  /* persistent thread blocks per SM, >= 1              */
+    int32_t tuned;          /* out: 1 = chosen by the autotuner (or its cache)    */
+    int32_t tuning;         /* out: 1 = trial steps are still to run              */
+    int32_t trials;         /* out: timed trial steps of the last tuning pass     */
+    double push_ms;         /* out: push time per step under the shape (tuned)    */
+} ipic3d_push_shape;
+int ipic3d_gpu_get_push_shape(ipic3d_ctx* ctx, ipic3d_push_shape* out);
+/* shape != NULL fixes the shape (no autotuning; out-of-range fields are
+ * clamped at launch); shape == NULL restarts the autotuner: the next steps
+ * are its trials. */
+int ipic3d_gpu_set_push_shape(ipic3d_ctx* ctx, const ipic3d_push_shape* shape);
+
 /* ---- element kernels (the reference's unit-level functions) ------------- */
 /* Particle::updateVelocity + updatePosition (particle.h:24-49) applied
  * nsteps times to n host particles with uniform E, B: the Boris KATs
@@ -256,6 +283,9 @@ void* ipic3d_gpu_batch_stream(ipic3d_batch* batch);
 /* Sums over the universes (steps = batched steps taken, kernel_launches =
  * the batch's own launches). */
 int ipic3d_gpu_batch_stats(ipic3d_batch* batch, ipic3d_stats* out);
+/* The batched push's shape: autotuned over the batch's first steps (config
+ * block_size 0), as a context's. */
+int ipic3d_gpu_batch_get_push_shape(ipic3d_batch* batch, ipic3d_push_shape* out);
 
 /* ---- projection without allocation -------------------------------------- */
 /* No counterpart in the reference. The current projection of
