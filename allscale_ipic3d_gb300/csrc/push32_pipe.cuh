@@ -1,6 +1,6 @@
 // The FP32 push as a persistent, warp-specialised, TMA-pipelined kernel.
 //
-// Each CTA has one producer warp and eight compute warps. The producer's
+// Each CTA has one producer warp and eleven compute warps. The producer's
 // elected lane streams 1024-slot tiles of a population through a ring of
 // shared-memory stages with bulk copies (cp.async.bulk, completion counted
 // on the stage's `full` mbarrier): x y z u v w of the tile's slots and the
@@ -12,7 +12,7 @@
 // the warps: a warp waits only for the data it works on.
 //
 // Work inside a tile. A tile whose cells are large (at most 32 cells) is cut
-// into items: the occupied slots of one cell, at most 256 at a time. Warps
+// into items: the occupied slots of one cell, PushShape::item at a time. Warps
 // take items from a per-stage counter; lane l pushes the item's particles
 // l, l + 32, ..., then a second pass over the stayers adds their cloud-in-
 // cell moments to the lane's accumulators, so a warp sums one cell and
@@ -260,10 +260,13 @@ __device__ __forceinline__ CellInfo cell_info(const Geom& g, const Push32Const& 
 // runs only for cells on a reflecting or open face; the rotation factor
 // 2 / (1 + |t|^2) comes from the hardware reciprocal plus one Newton-Raphson
 // step (r + r (1 - d r)). A leaver's move is returned in `dir` as
-// (dx + 1) | (dy + 1) << 2 | (dz + 1) << 4.
+// (dx + 1) | (dy + 1) << 2 | (dz + 1) << 4. Only qom and k_sub are read
+// from `sp` (the species' constants); the rest, which every population of
+// a launch shares, from `pc`.
 template <bool kSmemCoef, bool kGather, bool kDipole>
-__device__ __forceinline__ int step32f(const Geom& g, const Push32Const& pc, const float* __restrict__ coef,
-                                       const CellInfo& ci, PState<float>& p, int& dir) {
+__device__ __forceinline__ int step32f(const Geom& g, const Push32Const& pc, const Push32Const& sp,
+                                       const float* __restrict__ coef, const CellInfo& ci, PState<float>& p,
+                                       int& dir) {
     float E[6];
     if (kGather) {
         if (kSmemCoef)
@@ -284,7 +287,7 @@ __device__ __forceinline__ int step32f(const Geom& g, const Push32Const& pc, con
         E[5] = fmaf(fmaf(2.f * Z, Z, -fmaf(X, X, Y * Y)), fac1, E[5]);
     }
     const float bmag = fmaf(E[3], E[3], fmaf(E[4], E[4], E[5] * E[5]));
-    const float ratio = pc.k_sub * bmag;  // >= 0 or NaN
+    const float ratio = sp.k_sub * bmag;  // >= 0 or NaN
     // cell.h:947-952; a quotient beyond the int range (or NaN) leaves the
     // particle unmoved, as the reference's x86 conversion does
     int ns = 0;
@@ -294,7 +297,7 @@ __device__ __forceinline__ int step32f(const Geom& g, const Push32Const& pc, con
     }
     if (ns > 0) {
         const float dts = ns == 1 ? pc.dt : __fdividef(pc.dt, (float)ns);
-        const float k = pc.qom * 0.5f * dts;
+        const float k = sp.qom * 0.5f * dts;
         const float tx = k * E[3], ty = k * E[4], tz = k * E[5];
         const float den = fmaf(tx, tx, fmaf(ty, ty, fmaf(tz, tz, 1.f)));
         float inv = __fdividef(1.f, den);
@@ -466,16 +469,17 @@ __device__ __forceinline__ void leave_and_hole(const Geom& g, const Pop<float>& 
 
 // Item mode: the warp pushes particles [a, b) (tile-local slots, b - a <=
 // PushShape::item) of cell `cell`, lane l taking a + l, a + l + 32, ... A first
-// pass moves them: stayers go back to HBM with coalesced stores (and to the
-// stage for the second pass), the slots of leavers and drops are marked
-// (NaN position). The second pass sums the stayers' cloud-in-cell moments
-// and flushes the cell once. Keeping the 32 moment sums out of the mover
-// keeps the register count low enough for 6 warps per scheduler. `coef`
-// points at the cell's 48 field coefficients (shared memory).
+// pass moves them: stayers go back to the stage (the producer writes the
+// whole tile back with bulk stores), the slots of leavers and drops are
+// marked (NaN position; their slots are holes now, whose contents nothing
+// reads). The second pass sums the stayers' cloud-in-cell moments and
+// flushes the cell once. Keeping the 32 moment sums out of the mover keeps
+// the register count low enough for 6 warps per scheduler. `coef` points at
+// the cell's 48 field coefficients (shared memory).
 template <int kF>
 __device__ __forceinline__ void push_item(const Geom& g, const Pop<float>& P, const Push32Const& pc,
-                                          PipeStage& st, const float* coef, int base, int cell, int cstart, int a,
-                                          int b, uint32_t& nmig, uint32_t& nrem) {
+                                          const Push32Const& sp, PipeStage& st, const float* coef, int base, int cell,
+                                          int cstart, int a, int b, uint32_t& nmig, uint32_t& nrem) {
     constexpr bool kStep = (kF & kPipeStep) != 0, kDep = (kF & kPipeDeposit) != 0;
     const int lane = threadIdx.x & 31;
     const CellInfo ci = cell_info(g, pc, cell);
@@ -488,15 +492,11 @@ __device__ __forceinline__ void push_item(const Geom& g, const Pop<float>& P, co
             if (sl < b) {
                 p.x = st.s[0][sl]; p.y = st.s[1][sl]; p.z = st.s[2][sl];
                 p.u = st.s[3][sl]; p.v = st.s[4][sl]; p.w = st.s[5][sl];
-                outcome = step32f<true, (kF & kPipeGather) != 0, (kF & kPipeDipole) != 0>(g, pc, coef, ci, p, dir);
+                outcome =
+                    step32f<true, (kF & kPipeGather) != 0, (kF & kPipeDipole) != 0>(g, pc, sp, coef, ci, p, dir);
                 if (outcome == kStay) {
-                    const int gs = base + sl;
-                    P.x[gs] = p.x; P.y[gs] = p.y; P.z[gs] = p.z;
-                    P.u[gs] = p.u; P.v[gs] = p.v; P.w[gs] = p.w;
-                    if (kDep) {
-                        st.s[0][sl] = p.x; st.s[1][sl] = p.y; st.s[2][sl] = p.z;
-                        st.s[3][sl] = p.u; st.s[4][sl] = p.v; st.s[5][sl] = p.w;
-                    }
+                    st.s[0][sl] = p.x; st.s[1][sl] = p.y; st.s[2][sl] = p.z;
+                    st.s[3][sl] = p.u; st.s[4][sl] = p.v; st.s[5][sl] = p.w;
                 } else if (kDep) {
                     st.s[0][sl] = __int_as_float(0x7fffffff);  // not deposited here
                 }
@@ -555,7 +555,7 @@ __device__ __forceinline__ float run_transpose_sum(const float (&acc)[32], bool 
 // capacities are multiples of 8), and flushed per run of lanes of one cell.
 template <int kF>
 __device__ __forceinline__ void push_slots(const Geom& g, const Pop<float>& P, const Push32Const& pc,
-                                           PipeStage& st, int base, int2 desc, int slice, uint32_t& nmig,
+                                           const Push32Const& sp, PipeStage& st, int base, int2 desc, int slice, uint32_t& nmig,
                                            uint32_t& nrem) {
     constexpr bool kStep = (kF & kPipeStep) != 0, kDep = (kF & kPipeDeposit) != 0;
     constexpr int kPer = 4;
@@ -599,7 +599,8 @@ __device__ __forceinline__ void push_slots(const Geom& g, const Pop<float>& P, c
         if (j < nv) {
             p.x = st.s[0][sl]; p.y = st.s[1][sl]; p.z = st.s[2][sl];
             p.u = st.s[3][sl]; p.v = st.s[4][sl]; p.w = st.s[5][sl];
-            outcome = kStep ? step32f<false, (kF & kPipeGather) != 0, (kF & kPipeDipole) != 0>(g, pc, coef, ci, p, dir)
+            outcome = kStep ? step32f<false, (kF & kPipeGather) != 0, (kF & kPipeDipole) != 0>(g, pc, sp, coef, ci,
+                                                                                                 p, dir)
                             : kStay;
             if (outcome == kStay) {
                 if (kStep) {
@@ -633,7 +634,8 @@ __device__ __forceinline__ void push_slots(const Geom& g, const Pop<float>& P, c
 
 // One compute warp's share of the tile in `st`.
 template <int kF>
-__device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& P, const Push32Const& pc, int tile,
+__device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& P, const Push32Const& pc,
+                                               const Push32Const& sp, int tile,
                                                int2 desc, const PushShape& shp, PipeStage& st, int* next_item,
                                                uint32_t& nmig, uint32_t& nrem) {
     const int lane = threadIdx.x & 31;
@@ -641,7 +643,7 @@ __device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& 
     const int c0 = desc.x, nc = desc.y;
     if (nc > shp.item_cells) {
         for (int w = threadIdx.x >> 5; w < kSlotWarps; w += kComputeWarps)
-            push_slots<kF>(g, P, pc, st, base, desc, w, nmig, nrem);
+            push_slots<kF>(g, P, pc, sp, st, base, desc, w, nmig, nrem);
         return;
     }
     // item mode: lane i describes cell c0 + i: its occupied slots [lo, hi)
@@ -677,7 +679,7 @@ __device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& 
         const int cstart = __shfl_sync(0xffffffffu, cst, src);
         const int a = clo + ((j - cex) << sh);
         const int b = a + (1 << sh) < chi ? a + (1 << sh) : chi;
-        push_item<kF>(g, P, pc, st, st.coef + src * 48, base, c0 + src, cstart, a, b, nmig, nrem);
+        push_item<kF>(g, P, pc, sp, st, st.coef + src * 48, base, c0 + src, cstart, a, b, nmig, nrem);
     }
 }
 
@@ -760,9 +762,9 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
                 failed = true;
                 break;
             }
-            // slot mode writes the tile back from the stage; item mode's warps
-            // stored their stayers themselves
-            const bool store = kStep && sm.desc[s].y > shp.item_cells;
+            // the pushed tile goes back from the stage (stayers in place; the
+            // slots of leavers and drops are holes)
+            const bool store = kStep;
             if (store) {
                 const Pop<float>& P = S.p[sm.pop[s]];
                 const TileCopy c = tile_copy(P, t - tm.first[sm.pop[s]], sm.desc[s]);
@@ -807,7 +809,9 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
             if (cur >= 0) flush_counts(S.p[cur].ctr, nmig, nrem);
             cur = pi;
         }
-        push_tile_warp<kF>(g, S.p[pi], pcs.c[pi], t - tm.first[pi], sm.desc[s], shp, sm.stage[s],
+        // constants other than the species' are the same for every
+        // population of the launch: population 0's, at fixed offsets
+        push_tile_warp<kF>(g, S.p[pi], pcs.c[0], pcs.c[pi], t - tm.first[pi], sm.desc[s], shp, sm.stage[s],
                            &sm.next_item[s], nmig, nrem);
         fence_proxy_async_smem();  // this warp's writes to the stage, before the bulk stores read it
         __syncwarp();
@@ -871,7 +875,7 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
                 failed = true;
                 break;
             }
-            const bool store = kStep && sm.desc[s].y > shp.item_cells;
+            const bool store = kStep;
             if (store) {
                 const Pop<float>& P = sm.stage[s].job.P;
                 const TileCopy c = tile_copy(P, sm.ltile[s], sm.desc[s]);
@@ -912,8 +916,8 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
             if (cur) flush_counts(cur, nmig, nrem);
             cur = J.P.ctr;
         }
-        push_tile_warp<kF>(J.g, J.P, J.pc, sm.ltile[s], sm.desc[s], shp, sm.stage[s], &sm.next_item[s], nmig,
-                           nrem);
+        push_tile_warp<kF>(J.g, J.P, J.pc, J.pc, sm.ltile[s], sm.desc[s], shp, sm.stage[s], &sm.next_item[s],
+                           nmig, nrem);
         fence_proxy_async_smem();
         __syncwarp();
         if (lane == 0) mbar_arrive(&sm.empty[s]);
