@@ -186,6 +186,9 @@ struct ipic3d_ctx {
     int* st_flags = nullptr;            // fused upload: unknown species, cell overflow
     cudaStream_t copy_stream = nullptr; // host-to-device copies of the chunked upload
     cudaEvent_t copy_ev = nullptr;
+    // second stream of a step: kernels that run beside the push / placement
+    cudaStream_t aux_stream = nullptr;
+    cudaEvent_t aux_ev[4] = {nullptr, nullptr, nullptr, nullptr};  // fork, join (push), fork, join (place)
     // per-phase event timing
     bool profiling = false;
     cudaEvent_t ph_ev[IPIC3D_PHASE_COUNT][2] = {};
@@ -857,7 +860,12 @@ int solve_impl(ipic3d_ctx* ctx) {
 }
 
 // mover + export + import of all populations (+ injection), with the fused
-// deposit when the projector is on.
+// deposit when the projector is on. The pending push and the injection only
+// append to the outbox and the arrival lists and deposit with atomics, as the
+// push does: they run on a second stream beside the push (in its tail, as its
+// persistent blocks finish) and join before the placement; the J
+// finalisation, which needs every deposit but nothing of the placement, runs
+// beside the placement. With phase timing on, everything runs on one stream.
 int move_impl(ipic3d_ctx* ctx, bool deposit) {
     cudaStream_t st = ctx->stream;
     Geom g = ctx->g;
@@ -870,6 +878,16 @@ int move_impl(ipic3d_ctx* ctx, bool deposit) {
         CU(cudaMemsetAsync(ctx->J, 0, ctx->nnode() * 3 * sizeof(double), st));
         CU(cudaMemsetAsync(ctx->rho, 0, ctx->nnode() * sizeof(double), st));
     }
+    const bool fork = !ctx->profiling;
+    if (fork && !ctx->aux_stream) {
+        CU(cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
+        for (auto& e : ctx->aux_ev) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    cudaStream_t aux = fork ? ctx->aux_stream : st;
+    if (fork) {
+        CU(cudaEventRecord(ctx->aux_ev[0], st));
+        CU(cudaStreamWaitEvent(aux, ctx->aux_ev[0], 0));
+    }
     const auto s32 = pop_sets(ctx->p32);
     const auto s64 = pop_sets(ctx->p64);
     const PushShape shp = ctx->tuner.next();
@@ -881,8 +899,8 @@ int move_impl(ipic3d_ctx* ctx, bool deposit) {
     ph_end(ctx, IPIC3D_PHASE_PUSH);
     ctx->push_particles = ctx->particles_hint;
     ph_begin(ctx, IPIC3D_PHASE_PENDING);
-    for (auto& S : s32) n += launch_push_pending<float>(g, S, st);
-    for (auto& S : s64) n += launch_push_pending<double>(g, S, st);
+    for (auto& S : s32) n += launch_push_pending<float>(g, S, aux);
+    for (auto& S : s64) n += launch_push_pending<double>(g, S, aux);
     ph_end(ctx, IPIC3D_PHASE_PENDING);
     const bool inject = (ctx->cfg.flags & IPIC3D_F_INJECT_LOW_X) && ctx->cfg.bc_low[0] == IPIC3D_BC_OPEN &&
                         ctx->cfg.inject_per_cell > 0;
@@ -890,11 +908,21 @@ int move_impl(ipic3d_ctx* ctx, bool deposit) {
         ph_begin(ctx, IPIC3D_PHASE_INJECT);
         if (ctx->fp32)
             n += launch_inject<float>(g, ctx->p32[0].view(), ctx->cfg.inject_per_cell, ctx->cfg.inject_drift,
-                                      ctx->cfg.inject_vth, ctx->cfg.seed, ctx->d_step, st);
+                                      ctx->cfg.inject_vth, ctx->cfg.seed, ctx->d_step, aux);
         else
             n += launch_inject<double>(g, ctx->p64[0].view(), ctx->cfg.inject_per_cell, ctx->cfg.inject_drift,
-                                       ctx->cfg.inject_vth, ctx->cfg.seed, ctx->d_step, st);
+                                       ctx->cfg.inject_vth, ctx->cfg.seed, ctx->d_step, aux);
         ph_end(ctx, IPIC3D_PHASE_INJECT);
+    }
+    if (fork) {  // every append and deposit is done
+        CU(cudaEventRecord(ctx->aux_ev[1], aux));
+        CU(cudaStreamWaitEvent(st, ctx->aux_ev[1], 0));
+    }
+    const bool jfork = fork && deposit;
+    if (jfork) {
+        CU(cudaEventRecord(ctx->aux_ev[2], st));
+        CU(cudaStreamWaitEvent(aux, ctx->aux_ev[2], 0));
+        n += launch_j_finalize(g, (ctx->cfg.flags & IPIC3D_F_J_DIV8) != 0, !ctx->fp32, aux);
     }
     ph_begin(ctx, IPIC3D_PHASE_PLACE);
     for (auto& S : s32) n += launch_place<float>(g, S, st);
@@ -909,7 +937,10 @@ int move_impl(ipic3d_ctx* ctx, bool deposit) {
         ++n;
     }
     ph_end(ctx, IPIC3D_PHASE_PLACE);
-    if (deposit) {
+    if (jfork) {
+        CU(cudaEventRecord(ctx->aux_ev[3], aux));
+        CU(cudaStreamWaitEvent(st, ctx->aux_ev[3], 0));
+    } else if (deposit) {
         n += launch_j_finalize(g, (ctx->cfg.flags & IPIC3D_F_J_DIV8) != 0, !ctx->fp32, st);
         ph_end(ctx, IPIC3D_PHASE_MOMENTS);
     }
@@ -1069,6 +1100,9 @@ int destroy_impl(ipic3d_ctx* ctx) {
     dfree(ctx->st_flags);
     if (ctx->copy_ev) cudaEventDestroy(ctx->copy_ev);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    for (auto& e : ctx->aux_ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->aux_stream) cudaStreamDestroy(ctx->aux_stream);
     for (auto& e : ctx->pend_ev)
         if (e) cudaEventDestroy(e);
     for (auto& pair : ctx->ph_ev)
@@ -1612,6 +1646,10 @@ struct ipic3d_batch {
     bool graph_valid = false;
     uint64_t graph_kernels = 0;
     uint64_t steps = 0, launches = 0;
+    // second stream: the pending push beside the push, the J finalisation
+    // beside the placement (as a context's step)
+    cudaStream_t aux_stream = nullptr;
+    cudaEvent_t aux_ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // launch shape of the FP32 batched push (autotuned as a context's)
     PushTuner tuner;
     bool tune_started = false;
@@ -1752,15 +1790,30 @@ int batch_enqueue_step(ipic3d_batch* b) {
         if (b->fp32 && cfg.mover == IPIC3D_MOVER_FIELD) n += launch_cell_coef_batch(b->d_inst, ni, b->max_cells, st);
     }
     n += launch_batch_begin<T>(jobs, nj, b->d_inst, ni, b->max_nodes, deposit, b->d_flag, st);
+    cudaStream_t aux = b->aux_stream;
+    auto fork = [&](int e, cudaStream_t from, cudaStream_t to) -> int {
+        CU(cudaEventRecord(b->aux_ev[e], from));
+        CU(cudaStreamWaitEvent(to, b->aux_ev[e], 0));
+        return IPIC3D_OK;
+    };
+    int rc;
     if (nj > 0) {
+        if ((rc = fork(0, st, aux))) return rc;
         if (b->tune_timing) CU(cudaEventRecord(b->tune_ev[0], st));
         n += launch_push_batch<T>(jobs, b->d_cta, b->nctas, 0, jobs_of<T>(b)[0].g, b->tuner.next(), st);
         if (b->tune_timing) CU(cudaEventRecord(b->tune_ev[1], st));
-        n += launch_push_pending_batch<T>(jobs, nj, st);
+        n += launch_push_pending_batch<T>(jobs, nj, aux);
+        if ((rc = fork(1, aux, st))) return rc;
+    }
+    if (deposit) {
+        if ((rc = fork(2, st, aux))) return rc;
+        n += launch_j_finalize_batch(b->d_inst, ni, b->max_cells, aux);
+    }
+    if (nj > 0) {
         n += launch_place_batch<T>(jobs, nj, st);
         n += launch_pending_rotate_batch<T>(jobs, nj, st);
     }
-    if (deposit) n += launch_j_finalize_batch(b->d_inst, ni, b->max_cells, st);
+    if (deposit && (rc = fork(3, aux, st))) return rc;
     n += launch_batch_end<T>(jobs, b->d_inst, ni, b->d_flag, st);
     b->launches += (uint64_t)n;
     cudaError_t e = cudaGetLastError();
@@ -1921,6 +1974,9 @@ void batch_free(ipic3d_batch* b) {
         if (e) cudaEventDestroy(e);
     for (auto& e : b->tune_ev)
         if (e) cudaEventDestroy(e);
+    for (auto& e : b->aux_ev)
+        if (e) cudaEventDestroy(e);
+    if (b->aux_stream) cudaStreamDestroy(b->aux_stream);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }
@@ -1954,6 +2010,9 @@ int ipic3d_gpu_batch_create(uint32_t count, const ipic3d_props* props, const ipi
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
     for (auto& ev : b->tune_ev)
         if (e == cudaSuccess) e = cudaEventCreate(&ev);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->aux_stream, cudaStreamNonBlocking);
+    for (auto& ev : b->aux_ev)
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
     if (e != cudaSuccess)
         return bail(fail(e == cudaErrorMemoryAllocation ? IPIC3D_E_NOMEM : IPIC3D_E_CUDA, "batch: %s",
                          cudaGetErrorString(e)));
