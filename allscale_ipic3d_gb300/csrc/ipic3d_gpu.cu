@@ -163,9 +163,11 @@ struct ipic3d_ctx {
     uint64_t steps = 0, launches = 0, rebuilds = 0;
     uint64_t pending_last = 0, relayout_steps = 0;
     StepCounters last{};
-    cudaGraphExec_t graph = nullptr;
-    bool graph_valid = false;
-    uint64_t graph_kernels = 0;  // kernels one replay runs
+    // step graphs (StepKind): the whole step, or, in a run of steps with a
+    // field solver, the first solve alone, then the moves with the next
+    // step's solve beside the placement, the last move without it
+    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
+    uint64_t graph_kernels[4] = {0, 0, 0, 0};  // kernels one replay runs
     // pending-list watch: per step an async copy of the pending counts into
     // pinned memory, read one step later (ring of two)
     uint32_t* h_pending = nullptr;  // [2][kMaxPops]
@@ -213,10 +215,19 @@ struct ipic3d_ctx {
 namespace {
 
 void drop_graph(ipic3d_ctx* ctx) {
-    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
-    ctx->graph = nullptr;
-    ctx->graph_valid = false;
+    for (auto& gr : ctx->graph) {
+        if (gr) cudaGraphExecDestroy(gr);
+        gr = nullptr;
+    }
 }
+
+// What one replay of a step graph does.
+enum StepKind : int {
+    kStepFull = 0,       // field solve, then the move
+    kStepSolve = 1,      // the field solve alone (first step of a run)
+    kStepMoveSolve = 2,  // the move, the next step's solve beside its placement
+    kStepMove = 3,       // the move alone (last step of a run)
+};
 
 void release_pops(ipic3d_ctx* ctx) {
     for (auto& p : ctx->p32) p.release();
@@ -845,16 +856,21 @@ int project_impl(ipic3d_ctx* ctx) {
     return check_launch(ctx, n);
 }
 
-int solve_impl(ipic3d_ctx* ctx) {
-    cudaStream_t st = ctx->stream;
+// The solver's kernels (no ghost copy) on stream `st`; returns the launches.
+int enqueue_solver(ipic3d_ctx* ctx, cudaStream_t st) {
     int n = 0;
-    ph_begin(ctx, IPIC3D_PHASE_FIELDS);
     if (ctx->cfg.solver == IPIC3D_SOLVER_LEAPFROG)
         n += launch_leapfrog(ctx->g, (ctx->cfg.flags & IPIC3D_F_REFRESH_NODE_B) != 0, !ctx->fp32, st);
     else if (ctx->cfg.solver == IPIC3D_SOLVER_FORWARD)
         n += launch_forward(ctx->g, st);
     if (ctx->fp32 && ctx->cfg.mover == IPIC3D_MOVER_FIELD && ctx->cfg.solver != IPIC3D_SOLVER_STATIC)
         n += launch_cell_coef(ctx->g, ctx->cellcoef, st);
+    return n;
+}
+
+int solve_impl(ipic3d_ctx* ctx) {
+    ph_begin(ctx, IPIC3D_PHASE_FIELDS);
+    const int n = enqueue_solver(ctx, ctx->stream);
     ph_end(ctx, IPIC3D_PHASE_FIELDS);
     return check_launch(ctx, n);
 }
@@ -865,8 +881,12 @@ int solve_impl(ipic3d_ctx* ctx) {
 // push does: they run on a second stream beside the push (in its tail, as its
 // persistent blocks finish) and join before the placement; the J
 // finalisation, which needs every deposit but nothing of the placement, runs
-// beside the placement. With phase timing on, everything runs on one stream.
-int move_impl(ipic3d_ctx* ctx, bool deposit) {
+// beside the placement, and so does the next step's field solve
+// (`next_solve`: the ghost faces beside the push, the solver after the J
+// finalisation; they read and write fields and J only, the move and the
+// placement touch particles, J and interior nodes' reads only). With phase
+// timing on, everything runs on one stream.
+int move_impl(ipic3d_ctx* ctx, bool deposit, bool next_solve = false) {
     cudaStream_t st = ctx->stream;
     Geom g = ctx->g;
     g.deposit = deposit ? 1 : 0;
@@ -880,13 +900,19 @@ int move_impl(ipic3d_ctx* ctx, bool deposit) {
     }
     const bool fork = !ctx->profiling;
     if (fork && !ctx->aux_stream) {
-        CU(cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
+        // the higher priority: the solver chain on it is the longer branch
+        int least = 0, greatest = 0;
+        CU(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        CU(cudaStreamCreateWithPriority(&ctx->aux_stream, cudaStreamNonBlocking, greatest));
         for (auto& e : ctx->aux_ev) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
     cudaStream_t aux = fork ? ctx->aux_stream : st;
     if (fork) {
         CU(cudaEventRecord(ctx->aux_ev[0], st));
         CU(cudaStreamWaitEvent(aux, ctx->aux_ev[0], 0));
+        // the next step's ghost faces: they copy this step's solved fields
+        // into ghost nodes and ghost cells, which the move does not read
+        if (next_solve) n += launch_ghost(ctx->g, aux);
     }
     const auto s32 = pop_sets(ctx->p32);
     const auto s64 = pop_sets(ctx->p64);
@@ -918,11 +944,12 @@ int move_impl(ipic3d_ctx* ctx, bool deposit) {
         CU(cudaEventRecord(ctx->aux_ev[1], aux));
         CU(cudaStreamWaitEvent(st, ctx->aux_ev[1], 0));
     }
-    const bool jfork = fork && deposit;
+    const bool jfork = fork && (deposit || next_solve);
     if (jfork) {
         CU(cudaEventRecord(ctx->aux_ev[2], st));
         CU(cudaStreamWaitEvent(aux, ctx->aux_ev[2], 0));
-        n += launch_j_finalize(g, (ctx->cfg.flags & IPIC3D_F_J_DIV8) != 0, !ctx->fp32, aux);
+        if (deposit) n += launch_j_finalize(g, (ctx->cfg.flags & IPIC3D_F_J_DIV8) != 0, !ctx->fp32, aux);
+        if (next_solve) n += enqueue_solver(ctx, aux);
     }
     ph_begin(ctx, IPIC3D_PHASE_PLACE);
     for (auto& S : s32) n += launch_place<float>(g, S, st);
@@ -940,9 +967,17 @@ int move_impl(ipic3d_ctx* ctx, bool deposit) {
     if (jfork) {
         CU(cudaEventRecord(ctx->aux_ev[3], aux));
         CU(cudaStreamWaitEvent(st, ctx->aux_ev[3], 0));
-    } else if (deposit) {
-        n += launch_j_finalize(g, (ctx->cfg.flags & IPIC3D_F_J_DIV8) != 0, !ctx->fp32, st);
-        ph_end(ctx, IPIC3D_PHASE_MOMENTS);
+    } else {
+        if (deposit) {
+            n += launch_j_finalize(g, (ctx->cfg.flags & IPIC3D_F_J_DIV8) != 0, !ctx->fp32, st);
+            ph_end(ctx, IPIC3D_PHASE_MOMENTS);
+        }
+        if (next_solve) {
+            n += launch_ghost(ctx->g, st);
+            ph_begin(ctx, IPIC3D_PHASE_FIELDS);
+            n += enqueue_solver(ctx, st);
+            ph_end(ctx, IPIC3D_PHASE_FIELDS);
+        }
     }
     return check_launch(ctx, n);
 }
@@ -1015,16 +1050,41 @@ int tune_record(ipic3d_ctx* ctx) {
     return IPIC3D_OK;
 }
 
-// One timestep's kernel sequence (the body the graph captures).
-int enqueue_step(ipic3d_ctx* ctx) {
+// The kernel sequence of one step graph (kStepFull: one whole timestep).
+int enqueue_step(ipic3d_ctx* ctx, int kind = kStepFull) {
     const bool project = ctx->cfg.projector == IPIC3D_PROJECT_CIC;
     int rc;
-    if (ctx->cfg.solver != IPIC3D_SOLVER_STATIC) {
+    if ((kind == kStepFull || kind == kStepSolve) && ctx->cfg.solver != IPIC3D_SOLVER_STATIC) {
         int n = launch_ghost(ctx->g, ctx->stream);
         if ((rc = check_launch(ctx, n))) return rc;
         if ((rc = solve_impl(ctx))) return rc;
     }
-    return move_impl(ctx, project);  // advances the device step counter
+    if (kind == kStepSolve) return IPIC3D_OK;
+    return move_impl(ctx, project, kind == kStepMoveSolve);  // advances the device step counter
+}
+
+// Replays step graph `kind`, capturing it first if needed.
+int run_graph(ipic3d_ctx* ctx, int kind) {
+    if (!ctx->graph[kind]) {
+        cudaGraph_t graph = nullptr;
+        CU(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        const uint64_t before = ctx->launches;
+        const int rc = enqueue_step(ctx, kind);
+        ctx->graph_kernels[kind] = ctx->launches - before;
+        ctx->launches = before;  // capturing runs nothing
+        cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+        if (rc) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (e != cudaSuccess) return fail(IPIC3D_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&ctx->graph[kind], graph, cudaGraphInstantiateFlagUseNodePriority);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fail(IPIC3D_E_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    }
+    CU(cudaGraphLaunch(ctx->graph[kind], ctx->stream));
+    ctx->launches += ctx->graph_kernels[kind];
+    return IPIC3D_OK;
 }
 
 // Reads the step counters back; rebuilds the layout when particles wait for
@@ -1361,6 +1421,11 @@ int ipic3d_gpu_step(ipic3d_ctx* ctx, uint64_t num_steps) {
     const uint64_t pend_limit = std::max<uint64_t>(64, ctx->particles_hint / 200);
     uint64_t watch_from = 0;  // first step whose pending count is still meaningful
     tune_prepare(ctx);
+    // a run of graph steps with a field solver solves the next step's fields
+    // beside the current step's placement: the first solve alone, the last
+    // step without a solve after it
+    const bool overlap = use_graph && ctx->cfg.solver != IPIC3D_SOLVER_STATIC;
+    bool presolved = false;
     for (uint64_t done = 0; done < num_steps;) {
         if (ctx->tuner.running()) {  // a trial step of the autotuner: outside the graph, push timed
             ctx->tune_timing = true;
@@ -1369,27 +1434,13 @@ int ipic3d_gpu_step(ipic3d_ctx* ctx, uint64_t num_steps) {
             if (rc) return rc;
             if ((rc = ph_collect(ctx))) return rc;
             if ((rc = tune_record(ctx))) return rc;
+        } else if (overlap) {
+            if (!presolved && (rc = run_graph(ctx, kStepSolve))) return rc;
+            const bool last = done + 1 == num_steps || ctx->tuner.running();
+            if ((rc = run_graph(ctx, last ? kStepMove : kStepMoveSolve))) return rc;
+            presolved = !last;
         } else if (use_graph) {
-            if (!ctx->graph_valid) {
-                cudaGraph_t graph = nullptr;
-                CU(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-                const uint64_t before = ctx->launches;
-                rc = enqueue_step(ctx);
-                ctx->graph_kernels = ctx->launches - before;
-                ctx->launches = before;  // capturing runs nothing
-                cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
-                if (rc) {
-                    if (graph) cudaGraphDestroy(graph);
-                    return rc;
-                }
-                if (e != cudaSuccess) return fail(IPIC3D_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
-                e = cudaGraphInstantiate(&ctx->graph, graph, 0);
-                cudaGraphDestroy(graph);
-                if (e != cudaSuccess) return fail(IPIC3D_E_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
-                ctx->graph_valid = true;
-            }
-            CU(cudaGraphLaunch(ctx->graph, ctx->stream));
-            ctx->launches += ctx->graph_kernels;
+            if ((rc = run_graph(ctx, kStepFull))) return rc;
         } else {
             if ((rc = enqueue_step(ctx))) return rc;
             if ((rc = ph_collect(ctx))) return rc;
