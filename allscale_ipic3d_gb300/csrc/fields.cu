@@ -53,7 +53,46 @@ struct SolverArgs {
     double* field;        // (s+3)^3 x 9
     double* bc;           // (s+2)^3 x 3
     const double* J;      // (s+1)^3 x 3
+    // J as the E update reads it: jmode 0, final (folded, normalised); else
+    // raw node sums of the deposit, folded over the periodic images and
+    // normalised on the read exactly as k_j_finalize (jmode 1: / vol [/ 8])
+    // or k_j_finalize_mul (jmode 2: * jinv) would store them
+    int jmode, jdiv8;
+    double jvol, jinv;
 };
+
+// J of node m (per axis in [0, s]) as the J finalisation stores it: the sum
+// over the node's images {0, s} on each axis where it lies on the boundary,
+// in the finalisation's order, then normalised.
+__device__ __forceinline__ void final_j(const SolverArgs& A, int mx, int my, int mz, double (&a)[3]) {
+    const int s = A.s, nd = A.s + 1;
+    const int x = mx == s ? 0 : mx, y = my == s ? 0 : my, z = mz == s ? 0 : mz;
+    const int nxs = x == 0 ? 2 : 1, nys = y == 0 ? 2 : 1, nzs = z == 0 ? 2 : 1;
+    a[0] = a[1] = a[2] = 0.0;
+    for (int i = 0; i < nxs; ++i)
+        for (int j = 0; j < nys; ++j)
+            for (int k = 0; k < nzs; ++k) {
+                const double* p = A.J + 3 * fidx(nd, i ? s : x, j ? s : y, k ? s : z);
+                a[0] += p[0]; a[1] += p[1]; a[2] += p[2];
+            }
+    for (int c = 0; c < 3; ++c) {
+        if (A.jmode == 1) {
+            a[c] = a[c] / A.jvol;
+            if (A.jdiv8) a[c] = a[c] / 8.0;
+        } else {
+            a[c] *= A.jinv;
+        }
+    }
+}
+
+__device__ __forceinline__ void read_j(const SolverArgs& A, int mx, int my, int mz, double (&a)[3]) {
+    if (A.jmode == 0) {
+        const double* p = A.J + 3 * fidx(A.s + 1, mx, my, mz);
+        a[0] = p[0]; a[1] = p[1]; a[2] = p[2];
+    } else {
+        final_j(A, mx, my, mz, a);
+    }
+}
 
 // d / w: the reference's division (kMul false) or the product with 1 / w
 // (kMul: equal bit for bit when w is a power of two; the FP32 path's solver
@@ -73,12 +112,13 @@ __device__ __forceinline__ void leapfrog_e_body(SolverArgs A, int64_t t0, int64_
         int x, y, z;
         split3(t, n, n, x, y, z);
         ++x; ++y; ++z;
-        const int nb = A.s + 2, nf = A.s + 3, nd = A.s + 1;
+        const int nb = A.s + 2, nf = A.s + 3;
         const double* B0 = A.bc + 3 * fidx(nb, x, y, z);
         const double* Bxm = A.bc + 3 * fidx(nb, x - 1, y, z);
         const double* Bym = A.bc + 3 * fidx(nb, x, y - 1, z);
         const double* Bzm = A.bc + 3 * fidx(nb, x, y, z - 1);
-        const double* J = A.J + 3 * fidx(nd, x - 1, y - 1, z - 1);
+        double J[3];
+        read_j(A, x - 1, y - 1, z - 1, J);
         double* E = A.field + 9 * fidx(nf, x, y, z);
         E[0] = E[0] + A.dt * (c2 * (over<kMul>(B0[2] - Bym[2], A.wy, A.iwy) - over<kMul>(B0[1] - Bzm[1], A.wz, A.iwz)) -
                               J[0]);
@@ -169,7 +209,8 @@ __device__ __forceinline__ void forward_e_body(SolverArgs A, int64_t t0, int64_t
         ++x; ++y; ++z;
         double cx, cy, cz;
         curl_b(A, x, y, z, cx, cy, cz);
-        const double* J = A.J + 3 * fidx(A.s + 1, x - 1, y - 1, z - 1);
+        double J[3];
+        read_j(A, x - 1, y - 1, z - 1, J);
         double* E = A.field + 9 * fidx(A.s + 3, x, y, z);
         E[0] += (A.c * cx - J[0]) * A.dt;
         E[1] += (A.c * cy - J[1]) * A.dt;
@@ -273,6 +314,10 @@ __host__ __device__ inline SolverArgs solver_args(const Geom& g) {
     A.bc = g.bcfield;
     A.J = g.J;
     A.n32 = g.node32;
+    A.jmode = 0;
+    A.jdiv8 = 0;
+    A.jvol = g.vol;
+    A.jinv = 1.0;
     return A;
 }
 
@@ -488,15 +533,23 @@ static bool pow2(double v) {
     return std::frexp(v, &e) == 0.5;
 }
 
-int launch_leapfrog(const Geom& g, bool refresh_node_b, bool exact, cudaStream_t st) {
+// raw J: read as the J finalisation (div8 / exact as launch_j_finalize's)
+// would store it
+static void set_raw_j(SolverArgs& A, const Geom& g, bool div8, bool exact);
+
+int launch_leapfrog(const Geom& g, bool refresh_node_b, bool exact, cudaStream_t st, bool raw_j, bool div8,
+                    cudaEvent_t after_e) {
     SolverArgs A = solver_args(g);
+    if (raw_j) set_raw_j(A, g, div8, exact);
     const int64_t ne = (int64_t)(g.sx + 1) * (g.sx + 1) * (g.sx + 1);
     const bool mul = !exact || (pow2(g.w[0]) && pow2(g.w[1]) && pow2(g.w[2]));
     if (mul) {
         k_leapfrog_e<true><<<grid_for(ne, 256), 256, 0, st>>>(A);
+        if (after_e) cudaEventRecord(after_e, st);
         k_leapfrog_b<true><<<grid_for((int64_t)g.sx * g.sx * g.sx, 256), 256, 0, st>>>(A);
     } else {
         k_leapfrog_e<false><<<grid_for(ne, 256), 256, 0, st>>>(A);
+        if (after_e) cudaEventRecord(after_e, st);
         k_leapfrog_b<false><<<grid_for((int64_t)g.sx * g.sx * g.sx, 256), 256, 0, st>>>(A);
     }
     if (refresh_node_b) {
@@ -506,13 +559,22 @@ int launch_leapfrog(const Geom& g, bool refresh_node_b, bool exact, cudaStream_t
     return 2;
 }
 
-int launch_forward(const Geom& g, cudaStream_t st) {
+int launch_forward(const Geom& g, cudaStream_t st, bool raw_j, bool div8, bool exact, cudaEvent_t after_e) {
     SolverArgs A = solver_args(g);
+    if (raw_j) set_raw_j(A, g, div8, exact);
     const int64_t ne = (int64_t)(g.sx + 1) * (g.sx + 1) * (g.sx + 1);
     k_forward_e<<<grid_for(ne, 256), 256, 0, st>>>(A);
+    if (after_e) cudaEventRecord(after_e, st);
     k_forward_b<<<grid_for((int64_t)g.sx * g.sx * g.sx, 256), 256, 0, st>>>(A);
     k_interp_c2n<<<grid_for(ne, 256), 256, 0, st>>>(A);
     return 3;
+}
+
+static void set_raw_j(SolverArgs& A, const Geom& g, bool div8, bool exact) {
+    A.jdiv8 = div8 ? 1 : 0;
+    A.jvol = g.vol;
+    A.jinv = div8 ? 1.0 / g.vol / 8.0 : 1.0 / g.vol;
+    A.jmode = exact && !pow2(g.vol) ? 1 : 2;  // launch_j_finalize's choice
 }
 
 int launch_j_finalize(const Geom& g, bool div8, bool exact, cudaStream_t st) {

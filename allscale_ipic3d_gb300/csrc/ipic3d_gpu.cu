@@ -190,7 +190,8 @@ struct ipic3d_ctx {
     cudaEvent_t copy_ev = nullptr;
     // second stream of a step: kernels that run beside the push / placement
     cudaStream_t aux_stream = nullptr;
-    cudaEvent_t aux_ev[4] = {nullptr, nullptr, nullptr, nullptr};  // fork, join (push), fork, join (place)
+    // fork, join (push), fork, join (placement), the next step's E update done
+    cudaEvent_t aux_ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     // per-phase event timing
     bool profiling = false;
     cudaEvent_t ph_ev[IPIC3D_PHASE_COUNT][2] = {};
@@ -857,12 +858,17 @@ int project_impl(ipic3d_ctx* ctx) {
 }
 
 // The solver's kernels (no ghost copy) on stream `st`; returns the launches.
-int enqueue_solver(ipic3d_ctx* ctx, cudaStream_t st) {
+// raw_j: J holds the deposit's raw node sums, which the E update folds and
+// normalises as the J finalisation would; after_e: recorded after the E
+// update (the last read of J).
+int enqueue_solver(ipic3d_ctx* ctx, cudaStream_t st, bool raw_j = false, cudaEvent_t after_e = nullptr) {
+    const bool div8 = (ctx->cfg.flags & IPIC3D_F_J_DIV8) != 0;
     int n = 0;
     if (ctx->cfg.solver == IPIC3D_SOLVER_LEAPFROG)
-        n += launch_leapfrog(ctx->g, (ctx->cfg.flags & IPIC3D_F_REFRESH_NODE_B) != 0, !ctx->fp32, st);
+        n += launch_leapfrog(ctx->g, (ctx->cfg.flags & IPIC3D_F_REFRESH_NODE_B) != 0, !ctx->fp32, st, raw_j, div8,
+                             after_e);
     else if (ctx->cfg.solver == IPIC3D_SOLVER_FORWARD)
-        n += launch_forward(ctx->g, st);
+        n += launch_forward(ctx->g, st, raw_j, div8, !ctx->fp32, after_e);
     if (ctx->fp32 && ctx->cfg.mover == IPIC3D_MOVER_FIELD && ctx->cfg.solver != IPIC3D_SOLVER_STATIC)
         n += launch_cell_coef(ctx->g, ctx->cellcoef, st);
     return n;
@@ -882,11 +888,14 @@ int solve_impl(ipic3d_ctx* ctx) {
 // persistent blocks finish) and join before the placement; the J
 // finalisation, which needs every deposit but nothing of the placement, runs
 // beside the placement, and so does the next step's field solve
-// (`next_solve`: the ghost faces beside the push, the solver after the J
-// finalisation; they read and write fields and J only, the move and the
-// placement touch particles, J and interior nodes' reads only). With phase
-// timing on, everything runs on one stream.
-int move_impl(ipic3d_ctx* ctx, bool deposit, bool next_solve = false) {
+// (`next_solve`: the ghost faces beside the push, the solver once every
+// deposit is in; they read and write fields and J only, the move and the
+// placement touch particles, J and interior nodes' reads only). Then the
+// E update reads the raw deposit sums and folds and normalises them itself:
+// no J finalisation, and J and rho are cleared for the next step's deposit
+// once it has read them (`cleared`: a step that starts so skips its own
+// clear). With phase timing on, everything runs on one stream.
+int move_impl(ipic3d_ctx* ctx, bool deposit, bool next_solve = false, bool cleared = false) {
     cudaStream_t st = ctx->stream;
     Geom g = ctx->g;
     g.deposit = deposit ? 1 : 0;
@@ -895,8 +904,10 @@ int move_impl(ipic3d_ctx* ctx, bool deposit, bool next_solve = false) {
     for (auto& P : ctx->p64) CU(cudaMemsetAsync(P.ctr, 0, offsetof(StepCounters, lost), st));
     if (deposit) {
         ph_begin(ctx, IPIC3D_PHASE_MOMENTS);
-        CU(cudaMemsetAsync(ctx->J, 0, ctx->nnode() * 3 * sizeof(double), st));
-        CU(cudaMemsetAsync(ctx->rho, 0, ctx->nnode() * sizeof(double), st));
+        if (!cleared) {
+            CU(cudaMemsetAsync(ctx->J, 0, ctx->nnode() * 3 * sizeof(double), st));
+            CU(cudaMemsetAsync(ctx->rho, 0, ctx->nnode() * sizeof(double), st));
+        }
     }
     const bool fork = !ctx->profiling;
     if (fork && !ctx->aux_stream) {
@@ -945,11 +956,16 @@ int move_impl(ipic3d_ctx* ctx, bool deposit, bool next_solve = false) {
         CU(cudaStreamWaitEvent(st, ctx->aux_ev[1], 0));
     }
     const bool jfork = fork && (deposit || next_solve);
+    const bool raw_j = jfork && deposit && next_solve;
     if (jfork) {
         CU(cudaEventRecord(ctx->aux_ev[2], st));
         CU(cudaStreamWaitEvent(aux, ctx->aux_ev[2], 0));
-        if (deposit) n += launch_j_finalize(g, (ctx->cfg.flags & IPIC3D_F_J_DIV8) != 0, !ctx->fp32, aux);
-        if (next_solve) n += enqueue_solver(ctx, aux);
+        if (raw_j) {
+            n += enqueue_solver(ctx, aux, true, ctx->aux_ev[4]);
+        } else {
+            if (deposit) n += launch_j_finalize(g, (ctx->cfg.flags & IPIC3D_F_J_DIV8) != 0, !ctx->fp32, aux);
+            if (next_solve) n += enqueue_solver(ctx, aux);
+        }
     }
     ph_begin(ctx, IPIC3D_PHASE_PLACE);
     for (auto& S : s32) n += launch_place<float>(g, S, st);
@@ -964,6 +980,11 @@ int move_impl(ipic3d_ctx* ctx, bool deposit, bool next_solve = false) {
         ++n;
     }
     ph_end(ctx, IPIC3D_PHASE_PLACE);
+    if (raw_j) {  // the E update has read J: clear J and rho for the next step
+        CU(cudaStreamWaitEvent(st, ctx->aux_ev[4], 0));
+        CU(cudaMemsetAsync(ctx->J, 0, ctx->nnode() * 3 * sizeof(double), st));
+        CU(cudaMemsetAsync(ctx->rho, 0, ctx->nnode() * sizeof(double), st));
+    }
     if (jfork) {
         CU(cudaEventRecord(ctx->aux_ev[3], aux));
         CU(cudaStreamWaitEvent(st, ctx->aux_ev[3], 0));
@@ -1059,8 +1080,15 @@ int enqueue_step(ipic3d_ctx* ctx, int kind = kStepFull) {
         if ((rc = check_launch(ctx, n))) return rc;
         if ((rc = solve_impl(ctx))) return rc;
     }
-    if (kind == kStepSolve) return IPIC3D_OK;
-    return move_impl(ctx, project, kind == kStepMoveSolve);  // advances the device step counter
+    if (kind == kStepSolve) {  // a move follows: J and rho cleared for its deposit
+        if (project) {
+            CU(cudaMemsetAsync(ctx->J, 0, ctx->nnode() * 3 * sizeof(double), ctx->stream));
+            CU(cudaMemsetAsync(ctx->rho, 0, ctx->nnode() * sizeof(double), ctx->stream));
+        }
+        return IPIC3D_OK;
+    }
+    // advances the device step counter
+    return move_impl(ctx, project, kind == kStepMoveSolve, kind == kStepMoveSolve || kind == kStepMove);
 }
 
 // Replays step graph `kind`, capturing it first if needed.

@@ -57,8 +57,13 @@ int launch_j_finalize_batch(const InstJob* jobs, int ninst, int64_t max_cells, c
 
 // fields (fields.cu)
 int launch_ghost(const Geom& g, cudaStream_t st);
-int launch_leapfrog(const Geom& g, bool refresh_node_b, bool exact, cudaStream_t st);
-int launch_forward(const Geom& g, cudaStream_t st);
+// raw_j: g.J holds the deposit's raw node sums (no J finalisation yet); the E
+// update folds and normalises them on the read as launch_j_finalize(g, div8,
+// exact) would. after_e (may be null) is recorded once the E update is done.
+int launch_leapfrog(const Geom& g, bool refresh_node_b, bool exact, cudaStream_t st, bool raw_j = false,
+                    bool div8 = false, cudaEvent_t after_e = nullptr);
+int launch_forward(const Geom& g, cudaStream_t st, bool raw_j = false, bool div8 = false, bool exact = true,
+                   cudaEvent_t after_e = nullptr);
 // exact: the reference's divisions (FP64 parity); else one multiplication
 int launch_j_finalize(const Geom& g, bool div8, bool exact, cudaStream_t st);
 int launch_node32(const Geom& g, float4* node32, cudaStream_t st);

@@ -55,3 +55,58 @@ def test_fused_field_step_matches_separate_kernels(prec, solver, flags, n):
     np.testing.assert_array_equal(a["velocity"], b["velocity"])
     run.close()
     phases.close()
+
+
+def sparse_particles(props, cells, seed):
+    """One particle in each listed cell (x, y, z), grouped by cell, slow
+    enough to stay put for a few steps; cells two apart share no node (up to
+    the periodic fold), so every node's deposit is one addition."""
+    rng = np.random.default_rng(seed)
+    s = props.shape
+    counts = np.zeros(props.ncells, np.uint64)
+    order = sorted(cells, key=lambda c: (c[0] * s[1] + c[1]) * s[2] + c[2])
+    p = np.zeros(len(order), abi.PARTICLE_DTYPE)
+    w = np.array(props.cell_width)
+    for i, c in enumerate(order):
+        counts[(c[0] * s[1] + c[1]) * s[2] + c[2]] = 1
+        p[i]["position"] = np.array(props.origin) + (np.array(c) + 0.3 + 0.4 * rng.random(3)) * w
+        p[i]["velocity"] = rng.normal(0.0, 0.002, 3)
+    p["q"] = -0.5
+    p["qom"] = -1.0
+    return p, counts
+
+
+@pytest.mark.parametrize("prec,width,flags", [
+    (abi.FP64, (0.6, 0.5, 0.7), 0),                    # J finalised by division (vol not a power of two)
+    (abi.FP64, (0.5, 0.5, 0.5), abi.F_J_DIV8),         # by one multiplication, with the extra / 8
+    (abi.FP32, (0.6, 0.5, 0.7), abi.F_REFRESH_NODE_B),
+])
+def test_raw_j_read_matches_j_finalisation(prec, width, flags):
+    """With the projector on, a graph run reads the deposit's raw node sums in
+    the E update (periodic fold and normalisation on the read, no J
+    finalisation kernel) except after its last step; eager steps finalise J
+    every step. Fields, J, rho and particles agree bit for bit."""
+    props, _, _ = scenario(7301, (8, 8, 8), width=width, dt=0.05, ppc=1)
+    parts, counts = sparse_particles(props, [(0, 0, 0), (7, 3, 0), (3, 7, 5), (5, 0, 7), (2, 4, 3)], 7302)
+    rng = np.random.default_rng(7303)
+    f = rng.normal(0.0, 0.02, abi.field_shape(props))
+    bc = rng.normal(0.0, 0.02, abi.bcfield_shape(props))
+    kw = dict(precision=prec, mover=abi.MOVER_FIELD, solver=abi.SOLVER_LEAPFROG, projector=abi.PROJECT_CIC,
+              bc=abi.BC_PERIODIC)
+    run = gpu_sim(props, abi.Config.make(flags=abi.F_TRACK_IDS | abi.F_USE_GRAPH | flags, **kw))
+    eager = gpu_sim(props, abi.Config.make(flags=abi.F_TRACK_IDS | flags, **kw))
+    for s in (run, eager):
+        s.upload_fields(f, bc, None)
+        s.upload_particles(parts, counts)
+    if prec == abi.FP32:  # no autotuner trials: the same steps in both
+        for s in (run, eager):
+            s.set_push_shape(256, 32, 2)
+    run.step(6)
+    eager.step(6)
+    for a, b in zip(run.download_fields(), eager.download_fields()):
+        np.testing.assert_array_equal(a, b)
+    a, b = align_by_id(run.download_particles(), eager.download_particles())
+    np.testing.assert_array_equal(a["position"], b["position"])
+    np.testing.assert_array_equal(a["velocity"], b["velocity"])
+    run.close()
+    eager.close()
