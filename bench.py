@@ -241,16 +241,16 @@ def push_roofline(sim, precision, nsteps, props, pops):
             "peak_source": src + ", burst copy", "phase_ms_per_step": phases}
 
 
-def cpu_port_run(props, parts, counts, warmup, steps, budget_s):
+def cpu_port_run(props, parts, counts, warmup, steps, budget_s, cfg=None):
     """The CPU oracle on the host cores: warmup steps, then up to `steps`
-    steps or until budget_s seconds."""
+    steps or until budget_s seconds (config `cfg`, default the headline's)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle
     from common import OracleSim
     lib = oracle.load()
     threads = os.cpu_count() or 1
     lib.oracle_set_threads(threads)
-    sim = OracleSim(props, make_config(0, graph=False))
+    sim = OracleSim(props, cfg if cfg is not None else make_config(0, graph=False))
     sim.upload_particles(parts, counts)
     for _ in range(warmup):
         sim.step(1)
@@ -524,13 +524,46 @@ def config_c5():
             "outflow +x, dt 0.05", props, parts, counts, None, kw, 50)
 
 
+UDIST_N = 33554432
+
+
+def config_udist():
+    """The reference's own benchmark mode `:U:N` (benchmark.h:13-25, 81-92):
+    32^3 cells of width 10, dt 0.15, N = 33,554,432 electrons (q -1, q/m -25,
+    the distribution's species) uniform over the universe with velocities
+    U(-0.2, 0.2) per component, the reference's default policies (dipole
+    mover with no external field, static fields, no projection, reflecting
+    walls). The reference times 5 steps after 2 warm-up steps; here 20."""
+    from allscale_ipic3d_gb300 import abi
+    rng = np.random.default_rng(12345)
+    n, w, N = 32, 10.0, UDIST_N
+    pos = rng.random((N, 3)) * (n * w)
+    cell = np.minimum((pos // w).astype(np.int64), n - 1)
+    cid = (cell[:, 0] * n + cell[:, 1]) * n + cell[:, 2]
+    order = np.argsort(cid, kind="stable")
+    parts = np.zeros(N, abi.PARTICLE_DTYPE)
+    parts["position"] = pos[order]
+    del pos
+    parts["velocity"] = rng.uniform(-0.2, 0.2, (N, 3))
+    parts["q"] = -1.0
+    parts["qom"] = -25.0
+    counts = np.bincount(cid, minlength=n ** 3).astype(np.uint64)
+    props = abi.Props.make(size=(n, n, n), cell_width=(w, w, w), dt=0.15)
+    kw = dict(mover=abi.MOVER_DIPOLE, solver=abi.SOLVER_STATIC, projector=abi.PROJECT_NONE, bc=abi.BC_REFLECT,
+              flags=abi.F_USE_GRAPH)
+    return ("the reference's :U:N benchmark mode: 32^3 cells of width 10, N = 33,554,432 electrons uniform "
+            "over the universe, velocities U(-0.2,0.2), dipole mover without external field, static fields, "
+            "no projection, reflecting walls, dt 0.15", props, parts, counts, None, kw, 20)
+
+
 def run_config(name, warmup, local):
     """FP32 and FP64 on the same inputs: particle-steps/s, the FP32 push's
     live roofline, the FP32 energy error against FP64 after the run."""
     import allscale_ipic3d_gb300 as g
     from allscale_ipic3d_gb300 import abi
     t0 = time.perf_counter()
-    desc, props, parts, counts, fields, kw, steps = {"c1": config_c1, "c3": config_c3, "c5": config_c5}[name]()
+    desc, props, parts, counts, fields, kw, steps = {"c1": config_c1, "c3": config_c3, "c5": config_c5,
+                                                     "udist": config_udist}[name]()
     res = {"workload": desc, "cells": props.ncells, "particles": int(len(parts)), "steps": steps,
            "warmup": warmup}
     species = sorted({(float(a), float(b)) for a, b in zip(parts["q"][:1000], parts["qom"][:1000])})
@@ -567,6 +600,12 @@ def run_config(name, warmup, local):
                                  "particles_fp32": cons["fp32"]["particles"],
                                  "particles_fp64": cons["fp64"]["particles"]}
     res["fp32_over_fp64"] = res["fp32"]["value"] / res["fp64"]["value"]
+    if name == "udist":  # the reference's own CPU algorithm (the oracle port) on the same universe
+        cfg = abi.Config.make(precision=abi.FP64, **{k: v for k, v in kw.items() if k != "flags"})
+        v, cores, done, secs = cpu_port_run(props, parts, counts, 2, 5, 60.0, cfg)
+        res["cpu_port"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                           "sample": "the full universe, %d timed steps (%.1f s) after 2 warm-up steps, all host "
+                                     "threads (the reference's benchmark.h protocol)" % (done, secs)}
     res["species"] = species
     res["setup_and_run_s"] = round(time.perf_counter() - t0, 1)
     return res
@@ -581,7 +620,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", default="all", choices=["all", "fp32", "ensemble", "c1", "c3", "c5"],
+    ap.add_argument("--only", default="all", choices=["all", "fp32", "ensemble", "c1", "c3", "c5", "udist"],
                     help="fp32: only the FP32 timed run and its roofline (small profiling runs); "
                          "ensemble: only the batched ensemble; c1/c3/c5: that configuration alone")
     ap.add_argument("--universes", type=int, default=256, help="universes of the batched ensemble")
@@ -619,7 +658,7 @@ def main():
     import allscale_ipic3d_gb300 as g
     from allscale_ipic3d_gb300 import abi
 
-    if args.only in ("c1", "c3", "c5"):
+    if args.only in ("c1", "c3", "c5", "udist"):
         res = run_config(args.only, args.warmup, local)
         if rank == 0:
             print(json.dumps({"metric": METRIC, "unit": UNIT, args.only: res}))
