@@ -226,6 +226,10 @@ __device__ __forceinline__ void file_hole(const Pop<T>& P, int c, int64_t cstart
 // t = (a * n1 + b) * n2 + c for t in [0, n0 * n1 * n2): 32-bit divisions
 // when t fits (64-bit division by a runtime divisor is a long software
 // sequence on the GPU).
+// Blocks of the batched placement for a universe of `ncells` cells: one per
+// 512 cells (256 threads, a cell per 8 lanes: 32 cells at a time).
+__host__ __device__ inline int place_blocks(int ncells) { return ncells > 0 ? (ncells + 511) / 512 : 1; }
+
 __device__ __forceinline__ void split3(int64_t t, int n1, int n2, int& a, int& b, int& c) {
     if (t < 0x7fffffff) {
         const unsigned u = (unsigned)t, r = u / (unsigned)n2;

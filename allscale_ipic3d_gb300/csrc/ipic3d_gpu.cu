@@ -1690,7 +1690,7 @@ int ipic3d_gpu_boris(ipic3d_particle* particles, uint64_t n, const double E[3], 
 // batched step the host lists every (universe, species) population as a
 // PopJob (its Geom, its Pop view and push constants) and every universe as
 // an InstJob, plus two block maps: push CTA -> (job, CTA of the job) and
-// placement block -> (job, first cell). The tables are rebuilt only when a
+// placement block -> (job, block of the job). The tables are rebuilt only when a
 // population's layout changed (upload, re-layout): the host compares the
 // job records byte for byte.
 
@@ -1814,8 +1814,8 @@ int batch_tables(ipic3d_batch* b) {
     for (size_t j = 0; j < nj.size(); ++j) {
         const int64_t nb = (nj[j].P.capacity + kSlotsPerCta - 1) / kSlotsPerCta;
         for (int64_t k = 0; k < nb; ++k) cta.push_back(make_int2((int)j, (int)k));
-        const int nc = nj[j].g.ncells;
-        for (int c0 = 0; c0 < nc; c0 += 8) place.push_back(make_int2((int)j, c0));
+        const int npb = place_blocks(nj[j].g.ncells);
+        for (int k = 0; k < npb; ++k) place.push_back(make_int2((int)j, k));
     }
     for (auto& I : ni) {
         max_s = std::max(max_s, std::max(I.g.sx, std::max(I.g.sy, I.g.sz)));
@@ -1889,7 +1889,7 @@ int batch_enqueue_step(ipic3d_batch* b) {
         n += launch_j_finalize_batch(b->d_inst, ni, b->max_cells, aux);
     }
     if (nj > 0) {
-        n += launch_place_batch<T>(jobs, nj, st);
+        n += launch_place_batch<T>(jobs, b->d_place, b->nplace, st);
         n += launch_pending_rotate_batch<T>(jobs, nj, st);
     }
     if (deposit && (rc = fork(3, aux, st))) return rc;

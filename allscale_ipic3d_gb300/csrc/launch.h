@@ -35,8 +35,10 @@ int launch_push_batch(const PopJob<T>* jobs, const int2* cta_job, int64_t nctas,
                       const PushShape& shp, cudaStream_t st);  // g0: the policy fields (mover, flags, deposit) shared by the jobs
 template <typename T>
 int launch_push_pending_batch(const PopJob<T>* jobs, int njobs, cudaStream_t st);
+// tab: nblocks entries (job, block of the job), place_blocks(ncells) blocks
+// per job (device.cuh)
 template <typename T>
-int launch_place_batch(const PopJob<T>* jobs, int njobs, cudaStream_t st);
+int launch_place_batch(const PopJob<T>* jobs, const int2* tab, int64_t nblocks, cudaStream_t st);
 template <typename T>
 int launch_pending_rotate_batch(const PopJob<T>* jobs, int njobs, cudaStream_t st);
 template <typename T>

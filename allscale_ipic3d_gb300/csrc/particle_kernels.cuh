@@ -756,10 +756,16 @@ __global__ void k_inject(Geom g, Pop<T> P, InjectParams ip) {
 // arrivals append after the last particle, surplus holes are closed by moving
 // the cell's last particles into them. Arrivals beyond the cell's slots go to
 // the pending list and are pushed and placed again next step.
-// place_body is the work of the warp of cell c (warp-uniform c).
-template <typename T>
+// place_body is the work of a group of kG lanes (kG = 8: four cells per warp
+// at once; the kernel waits on memory, so four cells' loads in flight per
+// warp) on cell c (uniform within the group).
+constexpr int kPlaceLanes = 8;
+
+template <typename T, int kG = kPlaceLanes>
 __device__ __forceinline__ void place_body(const Geom& g, const Pop<T>& P, int32_t* sort_tmp, int c) {
-    const int lane = threadIdx.x & 31;
+    static_assert(kG == 8 || kG == 16 || kG == 32, "group of 8, 16 or 32 lanes");
+    const int wl = threadIdx.x & 31, lane = wl & (kG - 1);
+    const unsigned gmask = (kG == 32 ? 0xffffffffu : ((1u << kG) - 1u)) << (wl & ~(kG - 1));
     if (c >= g.ncells) return;
     const int nh = P.hole_cnt[c], na_all = P.arr_cnt[c];
     if (nh == 0 && na_all == 0) return;
@@ -769,7 +775,7 @@ __device__ __forceinline__ void place_body(const Geom& g, const Pop<T>& P, int32
     const int na = na_all < cap ? na_all : cap;
     const int free_slots = cap - (cnt - nh);
     const int np = na < free_slots ? na : free_slots;
-    for (int i = np + lane; i < na; i += 32) {
+    for (int i = np + lane; i < na; i += kG) {
         const Mover<T> m = P.outbox[P.arr_list[s0 + i]];
         uint32_t pi = atomicAdd(&P.ctr->pending_out, 1u);
         if (pi < P.pending_cap) P.pending_out[pi] = m;
@@ -778,18 +784,18 @@ __device__ __forceinline__ void place_body(const Geom& g, const Pop<T>& P, int32
     // holes in ascending order (rank sort; hole counts are small; one hole
     // is sorted already)
     if (nh > 1) {
-        for (int i = lane; i < nh; i += 32) {
+        for (int i = lane; i < nh; i += kG) {
             const int32_t h = P.hole_list[s0 + i];
             int r = 0;
             for (int j = 0; j < nh; ++j) r += P.hole_list[s0 + j] < h;
             sort_tmp[s0 + r] = h;
         }
-        __syncwarp();
+        __syncwarp(gmask);
     }
     const int32_t* H = (nh > 1 ? sort_tmp : P.hole_list) + s0;
     const int m = nh < np ? nh : np;
-    for (int i = lane; i < m; i += 32) write_slot(P, H[i], P.outbox[P.arr_list[s0 + i]]);
-    for (int i = nh + lane; i < np; i += 32) write_slot(P, s0 + cnt + (i - nh), P.outbox[P.arr_list[s0 + i]]);
+    for (int i = lane; i < m; i += kG) write_slot(P, H[i], P.outbox[P.arr_list[s0 + i]]);
+    for (int i = nh + lane; i < np; i += kG) write_slot(P, s0 + cnt + (i - nh), P.outbox[P.arr_list[s0 + i]]);
     const int newcount = cnt - nh + np;
     if (nh > np) {
         const int64_t lim = s0 + newcount, end = s0 + cnt;
@@ -801,7 +807,7 @@ __device__ __forceinline__ void place_body(const Geom& g, const Pop<T>& P, int32
         }
         const int L0 = lo;  // H[np, L0) < lim <= H[L0, nh)
         int filled = 0;
-        for (int64_t b = lim; b < end; b += 32) {
+        for (int64_t b = lim; b < end; b += kG) {
             const int64_t t = b + lane;
             bool valid = false;
             if (t < end) {
@@ -812,8 +818,8 @@ __device__ __forceinline__ void place_body(const Geom& g, const Pop<T>& P, int32
                 }
                 valid = !(a < nh && H[a] == t);
             }
-            const unsigned bal = __ballot_sync(0xffffffffu, valid);
-            const int idx = filled + __popc(bal & ((1u << lane) - 1u));
+            const unsigned bal = __ballot_sync(gmask, valid);  // bits of this group's lanes only
+            const int idx = filled + __popc(bal & ((1u << wl) - 1u));
             if (valid) move_slot(P, t, H[np + idx]);
             filled += __popc(bal);
         }
@@ -827,15 +833,16 @@ __device__ __forceinline__ void place_body(const Geom& g, const Pop<T>& P, int32
 }
 
 // The cells of the step's dirty lists (the only ones with holes or
-// arrivals), one warp per cell, warps striding over the list of population
-// blockIdx.y.
+// arrivals), one group of kPlaceLanes lanes per cell, groups striding over
+// the list of population blockIdx.y.
 template <typename T>
 __global__ void k_place(Geom g, const __grid_constant__ PopSet<T> S) {
     const Pop<T>& P = S.p[blockIdx.y];
     int32_t* sort_tmp = S.sort_tmp[blockIdx.y];
     const uint32_t n = P.ctr->dirty;
-    const uint32_t w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t i = w0; i < n; i += nw) place_body<T>(g, P, sort_tmp, P.dirty_list[i]);
+    const uint32_t g0 = (blockIdx.x * blockDim.x + threadIdx.x) / kPlaceLanes,
+                   ng = (gridDim.x * blockDim.x) / kPlaceLanes;
+    for (uint32_t i = g0; i < n; i += ng) place_body<T>(g, P, sort_tmp, P.dirty_list[i]);
 }
 
 // Moves this step's pending list to the next step's input (thread t0 = 0

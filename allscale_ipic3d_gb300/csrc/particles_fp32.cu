@@ -236,7 +236,7 @@ int launch_cell_coef_batch(const InstJob* inst, int ninst, int64_t max_cells, cu
     return 1;
 }
 
-template int launch_place_batch<float>(const PopJob<float>*, int, cudaStream_t);
+template int launch_place_batch<float>(const PopJob<float>*, const int2*, int64_t, cudaStream_t);
 template int launch_pending_rotate_batch<float>(const PopJob<float>*, int, cudaStream_t);
 template int launch_batch_begin<float>(const PopJob<float>*, int, const InstJob*, int, int64_t, int, uint32_t*,
                                        cudaStream_t);

@@ -28,7 +28,7 @@ template <>
 int launch_push_pending_batch<double>(const PopJob<double>* jobs, int njobs, cudaStream_t st) {
     return launch_push_pending_batch_generic<double>(jobs, njobs, st);
 }
-template int launch_place_batch<double>(const PopJob<double>*, int, cudaStream_t);
+template int launch_place_batch<double>(const PopJob<double>*, const int2*, int64_t, cudaStream_t);
 template int launch_pending_rotate_batch<double>(const PopJob<double>*, int, cudaStream_t);
 template int launch_batch_begin<double>(const PopJob<double>*, int, const InstJob*, int, int64_t, int, uint32_t*,
                                         cudaStream_t);

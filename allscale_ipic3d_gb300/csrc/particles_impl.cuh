@@ -97,12 +97,17 @@ __global__ void k_push_pending_batch(const PopJob<T>* __restrict__ jobs) {
 
 // Placement of a batch: blockIdx.y = job, the job's warps stride over its
 // dirty-cell list (cells with holes or arrivals only).
+// Batched placement: block b is block tab[b].y of the place_blocks(ncells)
+// blocks of job tab[b].x (its share grows with the universe), groups of
+// kPlaceLanes lanes striding over the job's dirty list.
 template <typename T>
-__global__ void k_place_batch(const PopJob<T>* __restrict__ jobs) {
-    const PopJob<T>& J = jobs[blockIdx.y];
+__global__ void k_place_batch(const PopJob<T>* __restrict__ jobs, const int2* __restrict__ tab) {
+    const int2 e = tab[blockIdx.x];
+    const PopJob<T>& J = jobs[e.x];
     const uint32_t n = J.P.ctr->dirty;
-    const uint32_t w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t i = w0; i < n; i += nw) place_body<T>(J.g, J.P, J.sort_tmp, J.P.dirty_list[i]);
+    const uint32_t g0 = ((uint32_t)e.y * blockDim.x + threadIdx.x) / kPlaceLanes,
+                   ng = ((uint32_t)place_blocks(J.g.ncells) * blockDim.x) / kPlaceLanes;
+    for (uint32_t i = g0; i < n; i += ng) place_body<T>(J.g, J.P, J.sort_tmp, J.P.dirty_list[i]);
 }
 
 template <typename T>
@@ -182,9 +187,9 @@ int launch_push_pending_batch_generic(const PopJob<T>* jobs, int njobs, cudaStre
 }
 
 template <typename T>
-int launch_place_batch(const PopJob<T>* jobs, int njobs, cudaStream_t st) {
-    if (njobs <= 0) return 0;
-    k_place_batch<T><<<dim3(8, njobs), 256, 0, st>>>(jobs);
+int launch_place_batch(const PopJob<T>* jobs, const int2* tab, int64_t nblocks, cudaStream_t st) {
+    if (nblocks <= 0) return 0;
+    k_place_batch<T><<<(unsigned)nblocks, 256, 0, st>>>(jobs, tab);
     return 1;
 }
 
