@@ -208,11 +208,12 @@ __device__ __forceinline__ int fast_div(int a, int d, float inv_d) {
     return q;
 }
 
-// Puts cell c on the step's dirty list (once per step: the flag is cleared
-// by the placement that processes the cell).
+// Flags cell c as touched this step (holes or arrivals): a plain store, no
+// round trip; k_dirty_compact lists the flagged cells for the placement,
+// which clears the flag.
 template <typename T>
 __device__ __forceinline__ void mark_dirty(const Pop<T>& P, int c) {
-    if (atomicExch(P.dirty_flag + c, 1) == 0) P.dirty_list[atomicAdd(&P.ctr->dirty, 1u)] = c;
+    P.dirty_flag[c] = 1;
 }
 
 // Files slot `slot` as a hole of cell c (its slots start at cstart).
@@ -220,7 +221,7 @@ template <typename T>
 __device__ __forceinline__ void file_hole(const Pop<T>& P, int c, int64_t cstart, int64_t slot) {
     const int k = atomicAdd(P.hole_cnt + c, 1);
     P.hole_list[cstart + k] = (int32_t)slot;
-    if (k == 0) mark_dirty(P, c);
+    mark_dirty(P, c);
 }
 
 // t = (a * n1 + b) * n2 + c for t in [0, n0 * n1 * n2): 32-bit divisions

@@ -427,7 +427,7 @@ __device__ __forceinline__ void move_slot(const Pop<T>& P, int64_t from, int64_t
 template <typename T>
 __device__ __forceinline__ void register_arrival(const Pop<T>& P, uint32_t o, const Mover<T>& m) {
     int k = atomicAdd(P.arr_cnt + m.cell, 1);
-    if (k == 0) mark_dirty(P, m.cell);
+    mark_dirty(P, m.cell);
     int64_t s = P.start[m.cell];
     if (k < (int)(P.start[m.cell + 1] - s)) {
         P.arr_list[s + k] = (int32_t)o;
@@ -830,6 +830,31 @@ __device__ __forceinline__ void place_body(const Geom& g, const Pop<T>& P, int32
         P.arr_cnt[c] = 0;
         P.dirty_flag[c] = 0;
     }
+}
+
+// Lists the cells flagged this step (holes or arrivals) of cells [c0, c1) of
+// population P on its dirty list (order: warp by warp, ascending within a
+// warp; the placement does not depend on the order). 32 x n threads from
+// thread t0 with stride `stride`.
+template <typename T>
+__device__ __forceinline__ void dirty_compact_body(const Pop<T>& P, int c0, int c1, int64_t t0, int64_t stride) {
+    const int lane = threadIdx.x & 31;
+    for (int64_t base = t0 - lane; base + c0 < c1; base += stride) {
+        const int c = (int)(c0 + base + lane);
+        const bool d = c < c1 && P.dirty_flag[c] != 0;
+        const unsigned b = __ballot_sync(0xffffffffu, d);
+        if (!b) continue;
+        uint32_t o = 0;
+        if (lane == 0) o = atomicAdd(&P.ctr->dirty, (uint32_t)__popc(b));
+        o = __shfl_sync(0xffffffffu, o, 0) + __popc(b & ((1u << lane) - 1u));
+        if (d) P.dirty_list[o] = c;
+    }
+}
+
+template <typename T>
+__global__ void k_dirty_compact(int ncells, const __grid_constant__ PopSet<T> S) {
+    dirty_compact_body<T>(S.p[blockIdx.y], 0, ncells, blockIdx.x * (int64_t)blockDim.x + threadIdx.x,
+                          (int64_t)gridDim.x * blockDim.x);
 }
 
 // The cells of the step's dirty lists (the only ones with holes or

@@ -47,11 +47,15 @@ int launch_inject(const Geom& g, const Pop<T>& P, double per_cell, const double 
 template <typename T>
 int launch_place(const Geom& g, const PopSet<T>& S, cudaStream_t st) {
     if (S.n <= 0) return 0;
-    // a warp per dirty cell, at most one per cell; 8 warps per block
+    // the flagged cells onto the dirty lists (a thread per cell)
+    int64_t cb = ((int64_t)g.ncells + 255) / 256;
+    if (cb > 152 * 8) cb = 152 * 8;
+    k_dirty_compact<T><<<dim3((unsigned)cb, S.n), 256, 0, st>>>(g.ncells, S);
+    // a group of kPlaceLanes lanes per dirty cell
     int64_t blocks = ((int64_t)g.ncells + 7) / 8;
     if (blocks > 152 * 8) blocks = 152 * 8;
     k_place<T><<<dim3((unsigned)blocks, S.n), 256, 0, st>>>(g, S);
-    return 1;
+    return 2;
 }
 
 template <typename T>
@@ -97,6 +101,16 @@ __global__ void k_push_pending_batch(const PopJob<T>* __restrict__ jobs) {
 
 // Placement of a batch: blockIdx.y = job, the job's warps stride over its
 // dirty-cell list (cells with holes or arrivals only).
+// Batched dirty lists: block b lists the flagged cells of the 512-cell
+// range tab[b].y of job tab[b].x.
+template <typename T>
+__global__ void k_dirty_compact_batch(const PopJob<T>* __restrict__ jobs, const int2* __restrict__ tab) {
+    const int2 e = tab[blockIdx.x];
+    const PopJob<T>& J = jobs[e.x];
+    const int c0 = e.y * 512, c1 = c0 + 512 < J.g.ncells ? c0 + 512 : J.g.ncells;
+    dirty_compact_body<T>(J.P, c0, c1, threadIdx.x, blockDim.x);
+}
+
 // Batched placement: block b is block tab[b].y of the place_blocks(ncells)
 // blocks of job tab[b].x (its share grows with the universe), groups of
 // kPlaceLanes lanes striding over the job's dirty list.
@@ -189,8 +203,9 @@ int launch_push_pending_batch_generic(const PopJob<T>* jobs, int njobs, cudaStre
 template <typename T>
 int launch_place_batch(const PopJob<T>* jobs, const int2* tab, int64_t nblocks, cudaStream_t st) {
     if (nblocks <= 0) return 0;
+    k_dirty_compact_batch<T><<<(unsigned)nblocks, 256, 0, st>>>(jobs, tab);
     k_place_batch<T><<<(unsigned)nblocks, 256, 0, st>>>(jobs, tab);
-    return 1;
+    return 2;
 }
 
 template <typename T>

@@ -429,42 +429,81 @@ __device__ __forceinline__ void emit_corner_sums(const Geom& g, float s, int cx,
 // Leaver bookkeeping of one warp step: outbox (one warp-aggregated append),
 // arrival list of the destination, cooperative deposit; the old slot is
 // filed as a hole of its cell (leavers and drops). `dir` is step32f's move.
+// The round trips (the destination's arrival slot, the outbox slots, the
+// hole slots) are issued together before any result is used, and cells are
+// flagged with plain stores (k_dirty_compact lists them). kOneCell: every
+// lane's slot is in `cell` (item mode), so the warp files its holes with one
+// aggregated atomic.
+template <bool kOneCell>
 __device__ __forceinline__ void leave_and_hole(const Geom& g, const Pop<float>& P, int outcome, int dir,
                                                const CellInfo& ci, const PState<float>& p, int slot, int cell,
                                                int cstart, bool deposit, uint32_t& nmig, uint32_t& nrem) {
     const int lane = threadIdx.x & 31;
-    const bool leave = outcome == kMove;
-    const unsigned lb = __ballot_sync(0xffffffffu, leave);
+    const unsigned below = (1u << lane) - 1u;
+    const bool leave = outcome == kMove, hole = leave || outcome == kDrop;
+    const unsigned lb = __ballot_sync(0xffffffffu, leave), hb = __ballot_sync(0xffffffffu, hole);
+    if (!hb) return;  // (every leaver leaves a hole)
+    // hole slots
+    int hk = 0;
+    if (kOneCell) {
+        if (lane == __ffs(hb) - 1) hk = atomicAdd(P.hole_cnt + cell, __popc(hb));
+    } else if (hole) {
+        hk = atomicAdd(P.hole_cnt + cell, 1);
+    }
+    int nx = 0, ny = 0, nz = 0;
     if (lb) {
         // destination cell (periodic wrap of the index, as the outbox expects)
-        int nx = ci.cx + (dir & 3) - 1, ny = ci.cy + ((dir >> 2) & 3) - 1, nz = ci.cz + ((dir >> 4) & 3) - 1;
+        nx = ci.cx + (dir & 3) - 1;
+        ny = ci.cy + ((dir >> 2) & 3) - 1;
+        nz = ci.cz + ((dir >> 4) & 3) - 1;
         nx = nx < 0 ? nx + g.sx : (nx >= g.sx ? nx - g.sx : nx);
         ny = ny < 0 ? ny + g.sy : (ny >= g.sy ? ny - g.sy : ny);
         nz = nz < 0 ? nz + g.sz : (nz >= g.sz ? nz - g.sz : nz);
+        const int dc = cell_id(g, nx, ny, nz);
+        int ak = 0;
+        int64_t ds = 0, de = 0;
+        uint32_t id = 0u;
+        if (leave) {
+            ak = atomicAdd(P.arr_cnt + dc, 1);  // the arrival slot of the destination
+            ds = P.start[dc];
+            de = P.start[dc + 1];
+            if (P.id) id = P.id[slot];
+        }
         const int leader = __ffs(lb) - 1;
         uint32_t o = 0;
         if (lane == leader) o = atomicAdd(&P.ctr->outbox, (uint32_t)__popc(lb));
-        o = __shfl_sync(0xffffffffu, o, leader) + __popc(lb & ((1u << lane) - 1u));
+        o = __shfl_sync(0xffffffffu, o, leader) + __popc(lb & below);
         if (leave) {
             Mover<float> m;
-            m.cell = cell_id(g, nx, ny, nz);
-            m.id = P.id ? P.id[slot] : 0u;
+            m.cell = dc;
+            m.id = id;
             m.x = p.x; m.y = p.y; m.z = p.z;
             m.u = p.u; m.v = p.v; m.w = p.w;
-            if (o < P.outbox_cap) {
-                P.outbox[o] = m;
-                register_arrival(P, o, m);
-            } else {
-                atomicAdd(&P.ctr->lost, 1u);
+            mark_dirty(P, dc);
+            // the outbox holds every particle of the population plus the
+            // pending and injected ones: o is always below its capacity
+            const bool in_box = o < P.outbox_cap;
+            if (in_box) P.outbox[o] = m;
+            else atomicAdd(&P.ctr->lost, 1u);
+            if (ak < (int)(de - ds)) {
+                P.arr_list[ds + ak] = in_box ? (int32_t)o : 0;
+            } else {  // the destination's slots are short: wait a step
+                const uint32_t pi = atomicAdd(&P.ctr->pending_out, 1u);
+                if (pi < P.pending_cap) P.pending_out[pi] = m;
+                else atomicAdd(&P.ctr->lost, 1u);
             }
             ++nmig;
         }
         if (deposit) deposit_leavers32(g, lb, nx, ny, nz, p, P.q);
     }
-    if (outcome == kMove || outcome == kDrop) {
-        file_hole(P, cell, cstart, slot);
-        if (outcome == kDrop) ++nrem;
+    if (kOneCell) {
+        hk = __shfl_sync(0xffffffffu, hk, __ffs(hb) - 1) + __popc(hb & below);
+        if (lane == 0) mark_dirty(P, cell);
+    } else if (hole) {
+        mark_dirty(P, cell);
     }
+    if (hole) P.hole_list[cstart + hk] = (int32_t)slot;
+    if (outcome == kDrop) ++nrem;
 }
 
 // Item mode: the warp pushes particles [a, b) (tile-local slots, b - a <=
@@ -501,7 +540,7 @@ __device__ __forceinline__ void push_item(const Geom& g, const Pop<float>& P, co
                     st.s[0][sl] = __int_as_float(0x7fffffff);  // not deposited here
                 }
             }
-            leave_and_hole(g, P, outcome, dir, ci, p, base + sl, cell, cstart, kDep, nmig, nrem);
+            leave_and_hole<true>(g, P, outcome, dir, ci, p, base + sl, cell, cstart, kDep, nmig, nrem);
         }
         __syncwarp();
     }
@@ -613,7 +652,7 @@ __device__ __forceinline__ void push_slots(const Geom& g, const Pop<float>& P, c
                 }
             }
         }
-        if (kStep) leave_and_hole(g, P, outcome, dir, ci, p, base + sl, cell, cstart, kDep, nmig, nrem);
+        if (kStep) leave_and_hole<false>(g, P, outcome, dir, ci, p, base + sl, cell, cstart, kDep, nmig, nrem);
     }
     if (!kDep) return;
     const unsigned todo = __ballot_sync(0xffffffffu, has_acc);
