@@ -768,7 +768,10 @@ __device__ __forceinline__ void place_body(const Geom& g, const Pop<T>& P, int32
     const unsigned gmask = (kG == 32 ? 0xffffffffu : ((1u << kG) - 1u)) << (wl & ~(kG - 1));
     if (c >= g.ncells) return;
     const int nh = P.hole_cnt[c], na_all = P.arr_cnt[c];
-    if (nh == 0 && na_all == 0) return;
+    if (nh == 0 && na_all == 0) {  // nothing to place: only the flag to clear
+        if (lane == 0) P.dirty_flag[c] = 0;
+        return;
+    }
     const int64_t s0 = P.start[c];
     const int cap = (int)(P.start[c + 1] - s0);
     const int cnt = P.count[c];
