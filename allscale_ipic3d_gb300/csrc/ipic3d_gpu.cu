@@ -171,6 +171,10 @@ struct ipic3d_ctx {
     // pending-list watch: per step an async copy of the pending counts into
     // pinned memory, read one step later (ring of two)
     uint32_t* h_pending = nullptr;  // [2][kMaxPops]
+    // after a run of steps: every population's counters and pending count,
+    // copied in one go (pinned)
+    StepCounters* h_ctr = nullptr;  // [kMaxPops]
+    uint32_t* h_pin = nullptr;      // [kMaxPops]
     cudaEvent_t pend_ev[2] = {nullptr, nullptr};
     uint64_t particles_hint = 0;
     // species table of the populations (index = population) and the device
@@ -567,8 +571,9 @@ int upload_fast(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, const ipic3d_pa
         g.origin[a] = ctx->props.origin[a];
         g.w[a] = ctx->props.cell_width[a];
     }
-    // chunks of about 32 MB of records, cut at cell boundaries
-    const int64_t chunk = std::max<int64_t>(1, (int64_t)(32u << 20) / (int64_t)sizeof(ipic3d_particle));
+    // chunks of about 16 MB of records, cut at cell boundaries (the last
+    // chunk's kernel runs after the last copy: small chunks keep that short)
+    const int64_t chunk = std::max<int64_t>(1, (int64_t)(16u << 20) / (int64_t)sizeof(ipic3d_particle));
     int nl = 0;
     for (int64_t c0 = 0; c0 < nc;) {
         int64_t c1 = c0 + 1;
@@ -1118,6 +1123,21 @@ int run_graph(ipic3d_ctx* ctx, int kind) {
 // Reads the step counters back; rebuilds the layout when particles wait for
 // a slot; reports lost particles.
 int after_steps(ipic3d_ctx* ctx, bool force_relayout = false) {
+    // the counters of every population: asynchronous copies, one wait
+    const int np = std::min(ctx->npops(), kMaxPops);
+    int k = 0;
+    for (auto& P : ctx->p32)
+        if (k < np) {
+            CU(cudaMemcpyAsync(ctx->h_ctr + k, P.ctr, sizeof(StepCounters), cudaMemcpyDeviceToHost, ctx->stream));
+            CU(cudaMemcpyAsync(ctx->h_pin + k++, P.pending_in_count, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+        }
+    for (auto& P : ctx->p64)
+        if (k < np) {
+            CU(cudaMemcpyAsync(ctx->h_ctr + k, P.ctr, sizeof(StepCounters), cudaMemcpyDeviceToHost, ctx->stream));
+            CU(cudaMemcpyAsync(ctx->h_pin + k++, P.pending_in_count, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+        }
     CU(cudaStreamSynchronize(ctx->stream));
     StepCounters total{};
     uint32_t pending = 0;
@@ -1130,20 +1150,7 @@ int after_steps(ipic3d_ctx* ctx, bool force_relayout = false) {
         total.pending_out += c.pending_out;
         pending += pin;
     };
-    for (auto& P : ctx->p32) {
-        StepCounters c;
-        uint32_t pin;
-        CU(cudaMemcpy(&c, P.ctr, sizeof(c), cudaMemcpyDeviceToHost));
-        CU(cudaMemcpy(&pin, P.pending_in_count, sizeof(pin), cudaMemcpyDeviceToHost));
-        acc(c, pin);
-    }
-    for (auto& P : ctx->p64) {
-        StepCounters c;
-        uint32_t pin;
-        CU(cudaMemcpy(&c, P.ctr, sizeof(c), cudaMemcpyDeviceToHost));
-        CU(cudaMemcpy(&pin, P.pending_in_count, sizeof(pin), cudaMemcpyDeviceToHost));
-        acc(c, pin);
-    }
+    for (int i = 0; i < k; ++i) acc(ctx->h_ctr[i], ctx->h_pin[i]);
     ctx->last = total;
     ctx->pending_last = pending;
     if (total.lost) return fail(IPIC3D_E_CAPACITY, "%u particles lost: pending list full", total.lost);
@@ -1179,6 +1186,8 @@ int destroy_impl(ipic3d_ctx* ctx) {
     dfree(ctx->d_partial);
     dfree(ctx->d_result);
     if (ctx->h_pending) cudaFreeHost(ctx->h_pending);
+    if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
+    if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
     dfree(ctx->st_parts);
     dfree(ctx->st_ids);
     dfree(ctx->st_sid);
@@ -1279,6 +1288,8 @@ int create_impl(const ipic3d_props* props, const ipic3d_config* cfg, cudaStream_
     CUB(cudaMemsetAsync(ctx->node32, 0, ctx->nfield() * 2 * sizeof(float4), ctx->stream));
     CUB(cudaMemsetAsync(ctx->d_step, 0, sizeof(uint64_t), ctx->stream));
     CUB(cudaMallocHost(&ctx->h_pending, 2 * kMaxPops * sizeof(uint32_t)));
+    CUB(cudaMallocHost(&ctx->h_ctr, kMaxPops * sizeof(StepCounters)));
+    CUB(cudaMallocHost(&ctx->h_pin, kMaxPops * sizeof(uint32_t)));
     std::memset(ctx->h_pending, 0, 2 * kMaxPops * sizeof(uint32_t));
     for (auto& e : ctx->pend_ev) CUB(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     for (auto& e : ctx->tune_ev) CUB(cudaEventCreate(&e));
@@ -1462,12 +1473,12 @@ int ipic3d_gpu_step(ipic3d_ctx* ctx, uint64_t num_steps) {
             if (rc) return rc;
             if ((rc = ph_collect(ctx))) return rc;
             if ((rc = tune_record(ctx))) return rc;
-        } else if (overlap) {
+        } else if (overlap && (presolved || done + 1 < num_steps)) {
             if (!presolved && (rc = run_graph(ctx, kStepSolve))) return rc;
-            const bool last = done + 1 == num_steps || ctx->tuner.running();
+            const bool last = done + 1 == num_steps;
             if ((rc = run_graph(ctx, last ? kStepMove : kStepMoveSolve))) return rc;
             presolved = !last;
-        } else if (use_graph) {
+        } else if (use_graph) {  // a lone step (or no field solver): one graph
             if ((rc = run_graph(ctx, kStepFull))) return rc;
         } else {
             if ((rc = enqueue_step(ctx))) return rc;
