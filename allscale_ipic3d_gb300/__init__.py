@@ -45,6 +45,7 @@ _SIGNATURES = [
     ("ipic3d_gpu_destroy", C.c_int, [_vp]),
     ("ipic3d_gpu_upload_particles", C.c_int, [_vp, _vp, _vp, _vp]),
     ("ipic3d_gpu_reserve", C.c_int, [_vp, C.c_uint64]),
+    ("ipic3d_gpu_init_uniform", C.c_int, [_vp, C.c_uint64]),
     ("ipic3d_gpu_particle_count", C.c_int, [_vp, C.POINTER(C.c_uint64)]),
     ("ipic3d_gpu_download_particles", C.c_int, [_vp, _vp, C.c_uint64, _vp, _vp]),
     ("ipic3d_gpu_cell_counts", C.c_int, [_vp, _vp]),
@@ -181,6 +182,11 @@ class Simulation:
             raise ValueError("cell_counts sum to %d but %d particles given" % (int(c.sum()), len(p)))
         i = None if ids is None else np.ascontiguousarray(ids, dtype=np.uint32)
         _check(library().ipic3d_gpu_upload_particles(self._ctx, abi.vptr(p), abi.vptr(c), abi.vptr(i)))
+
+    def init_uniform(self, num_particles):
+        """initCells(uniform) of the reference's :U:N benchmark mode, made on
+        the device with the reference's random streams (cell.h:638-697)."""
+        _check(library().ipic3d_gpu_init_uniform(self._ctx, int(num_particles)))
 
     def particle_count(self):
         n = C.c_uint64()

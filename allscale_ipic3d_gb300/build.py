@@ -27,6 +27,7 @@ SOURCES = {
     "particles_fp32.cu": ["--ftz=true", "--prec-div=false", "--prec-sqrt=false"],
     "fields.cu": ["-fmad=false"],
     "upload.cu": ["-fmad=false"],
+    "init.cu": ["-fmad=false"],
     "noalloc.cu": ["-fmad=false"],
 }
 

@@ -505,10 +505,11 @@ int scatter_pops(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, const std::vec
 // on the context stream as soon as its bytes have landed, so the kernels
 // hide behind the copies. Returns 0 when done, 1 when a species is unknown
 // (the host path creates it), 2 when a cell's slots were too few (the
-// slower path re-lays out), < 0 on error.
+// slower path re-lays out), < 0 on error. on_device: the records are in the
+// staging buffer already (made on the device), one kernel over all cells.
 template <typename T>
 int upload_fast(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, const ipic3d_particle* parts,
-                const std::vector<int64_t>& off, const uint32_t* ids) {
+                const std::vector<int64_t>& off, const uint32_t* ids, bool on_device = false) {
     const int64_t nc = ctx->ncells(), n = off[nc];
     const int npop = (int)pops.size();
     for (auto& P : pops)
@@ -573,13 +574,14 @@ int upload_fast(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, const ipic3d_pa
     }
     // chunks of about 16 MB of records, cut at cell boundaries (the last
     // chunk's kernel runs after the last copy: small chunks keep that short)
-    const int64_t chunk = std::max<int64_t>(1, (int64_t)(16u << 20) / (int64_t)sizeof(ipic3d_particle));
+    const int64_t chunk = on_device ? std::max<int64_t>(1, n)
+                                    : std::max<int64_t>(1, (int64_t)(16u << 20) / (int64_t)sizeof(ipic3d_particle));
     int nl = 0;
     for (int64_t c0 = 0; c0 < nc;) {
         int64_t c1 = c0 + 1;
         while (c1 < nc && off[c1] - off[c0] < chunk) ++c1;
         const int64_t p0 = off[c0], pn = off[c1] - off[c0];
-        if (pn > 0) {
+        if (pn > 0 && !on_device) {
             CU(cudaMemcpyAsync(reinterpret_cast<char*>(ctx->st_parts) + p0 * sizeof(ipic3d_particle), parts + p0,
                                (size_t)pn * sizeof(ipic3d_particle), cudaMemcpyHostToDevice, cs));
             if (ids) CU(cudaMemcpyAsync(ctx->st_ids + p0, ids + p0, (size_t)pn * sizeof(uint32_t),
@@ -663,6 +665,59 @@ int upload_device(ipic3d_ctx* ctx, const ipic3d_particle* parts, const uint64_t*
     if (relaid) drop_graph(ctx);
     ctx->j_valid = false;
     ctx->particles_hint = (uint64_t)n;
+    return IPIC3D_OK;
+}
+
+// initCells(uniform) of the reference's :U:N benchmark mode (cell.h:638-697)
+// made on the device (init.cu) and stored like an upload: the populations
+// (the injection species first, as an upload orders them, then the
+// electrons) are laid out for the known per-cell counts.
+int init_uniform_impl(ipic3d_ctx* ctx, uint64_t n) {
+    const int64_t nc = ctx->ncells();
+    if (n > 0x7fffffffull) return fail(IPIC3D_E_INVALID, "%llu particles: at most 2^31 - 1", (unsigned long long)n);
+    std::vector<uint64_t> counts(nc), zeros(nc, 0);
+    std::vector<int64_t> off(nc + 1, 0);
+    const uint64_t per = n / (uint64_t)nc, rem = n % (uint64_t)nc;
+    for (int64_t c = 0; c < nc; ++c) {
+        counts[c] = per + ((uint64_t)c < rem ? 1 : 0);
+        off[c + 1] = off[c] + (int64_t)counts[c];
+    }
+    const std::pair<double, double> electron{-1.0, -25.0};  // species::electron (cell.h:107-118)
+    std::vector<std::pair<double, double>> sp;
+    if (ctx->cfg.flags & IPIC3D_F_INJECT_LOW_X) sp.push_back({ctx->cfg.inject_q, ctx->cfg.inject_qom});
+    if (sp.empty() || sp[0] != electron) sp.push_back(electron);
+    drop_graph(ctx);
+    release_pops(ctx);
+    ctx->species = sp;
+    int rc;
+    for (auto& x : sp) {
+        const std::vector<uint64_t>& cnt = x == electron ? counts : zeros;
+        if (ctx->fp32) {
+            ctx->p32.emplace_back();
+            ctx->p32.back().q = x.first;
+            ctx->p32.back().qom = x.second;
+            if ((rc = alloc_pop(ctx, ctx->p32.back(), cnt, 0))) return rc;
+        } else {
+            ctx->p64.emplace_back();
+            ctx->p64.back().q = x.first;
+            ctx->p64.back().qom = x.second;
+            if ((rc = alloc_pop(ctx, ctx->p64.back(), cnt, 0))) return rc;
+        }
+    }
+    if (n == 0) {
+        ctx->j_valid = false;
+        ctx->particles_hint = 0;
+        return IPIC3D_OK;
+    }
+    if ((rc = grow(reinterpret_cast<char*&>(ctx->st_parts), ctx->st_parts_cap, (size_t)n * sizeof(ipic3d_particle))))
+        return rc;
+    int nl = launch_init_uniform((int)ctx->props.size[0], (int)ctx->props.size[1], (int)ctx->props.size[2],
+                                 ctx->props.origin, ctx->props.cell_width, n, ctx->st_parts, ctx->stream);
+    if ((rc = check_launch(ctx, nl))) return rc;
+    rc = ctx->fp32 ? upload_fast(ctx, ctx->p32, nullptr, off, nullptr, true)
+                   : upload_fast(ctx, ctx->p64, nullptr, off, nullptr, true);
+    if (rc < 0) return rc;
+    if (rc > 0) return fail(IPIC3D_E_CUDA, "device initialisation: the scatter found an unexpected layout");
     return IPIC3D_OK;
 }
 
@@ -1347,6 +1402,14 @@ int ipic3d_gpu_upload_particles(ipic3d_ctx* ctx, const ipic3d_particle* particle
         if (rc <= 0) return rc;  // done (0) or failed (< 0); 1 = take the host path
     }
     return upload_impl(ctx, particles, cell_counts, ids);
+}
+
+int ipic3d_gpu_init_uniform(ipic3d_ctx* ctx, uint64_t num_particles) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if ((rc = init_uniform_impl(ctx, num_particles))) return rc;
+    CU(cudaStreamSynchronize(ctx->stream));
+    return IPIC3D_OK;
 }
 
 int ipic3d_gpu_reserve(ipic3d_ctx* ctx, uint64_t n) {

@@ -76,6 +76,11 @@ int launch_reduce_particles(const Pop<T>& P, int ncells, double* partial, cudaSt
 int launch_reduce_fields(const Geom& g, double* partial, cudaStream_t st);
 int launch_reduce_final(const double* partial, int blocks, int kq, double* out, cudaStream_t st);
 
+// initCells(uniform) of the reference's :U:N mode into `out` (AoS records,
+// grouped by cell), its random streams replayed on the device (init.cu)
+int launch_init_uniform(int sx, int sy, int sz, const double origin[3], const double w[3], uint64_t num_particles,
+                        void* out, cudaStream_t st);
+
 // misc (ipic3d_gpu.cu)
 // records a status and message for ipic3d_gpu_last_error (this thread)
 int set_last_error(int status, const char* msg);

@@ -138,6 +138,14 @@ int ipic3d_gpu_upload_particles(ipic3d_ctx* ctx, const ipic3d_particle* particle
 /* Reserves room for at least `n` particles (allocation happens here, not in
  * ipic3d_gpu_step). */
 int ipic3d_gpu_reserve(ipic3d_ctx* ctx, uint64_t n);
+/* initCells(properties, num_particles, uniform<>) (cell.h:638-697), the
+ * universe of the reference's ":U:N" benchmark mode, made on the device:
+ * floor(N / cells) particles per cell (+1 for the first N mod cells cells),
+ * positions uniform in the cell and velocities U(-0.2, 0.2) per component
+ * from the reference's per-cell std::minstd_rand streams (bit-identical
+ * values), electrons (q = -1, q/m = -25). Replaces the context's particles
+ * as an upload does (ids = index in cell order). */
+int ipic3d_gpu_init_uniform(ipic3d_ctx* ctx, uint64_t num_particles);
 /* Number of particles currently stored. */
 int ipic3d_gpu_particle_count(ipic3d_ctx* ctx, uint64_t* n);
 /* Downloads particles grouped by cell (row-major) with per-cell counts; the
