@@ -529,31 +529,22 @@ UDIST_N = 33554432
 
 def config_udist():
     """The reference's own benchmark mode `:U:N` (benchmark.h:13-25, 81-92):
-    32^3 cells of width 10, dt 0.15, N = 33,554,432 electrons (q -1, q/m -25,
-    the distribution's species) uniform over the universe with velocities
-    U(-0.2, 0.2) per component, the reference's default policies (dipole
-    mover with no external field, static fields, no projection, reflecting
-    walls). The reference times 5 steps after 2 warm-up steps; here 20."""
+    32^3 cells of width 10, dt 0.15, N = 33,554,432 electrons (q -1, q/m -25)
+    from the reference's initCells(uniform) (cell.h:638-697): its per-cell
+    random streams, made on the device (ipic3d_gpu_init_uniform), positions
+    uniform in the cell, velocities U(-0.2, 0.2); the reference's default
+    policies (dipole mover with no external field, static fields, no
+    projection, reflecting walls). The reference times 5 steps after 2
+    warm-up steps; here 20. No host particles: `parts` is None."""
     from allscale_ipic3d_gb300 import abi
-    rng = np.random.default_rng(12345)
-    n, w, N = 32, 10.0, UDIST_N
-    pos = rng.random((N, 3)) * (n * w)
-    cell = np.minimum((pos // w).astype(np.int64), n - 1)
-    cid = (cell[:, 0] * n + cell[:, 1]) * n + cell[:, 2]
-    order = np.argsort(cid, kind="stable")
-    parts = np.zeros(N, abi.PARTICLE_DTYPE)
-    parts["position"] = pos[order]
-    del pos
-    parts["velocity"] = rng.uniform(-0.2, 0.2, (N, 3))
-    parts["q"] = -1.0
-    parts["qom"] = -25.0
-    counts = np.bincount(cid, minlength=n ** 3).astype(np.uint64)
+    n, w = 32, 10.0
     props = abi.Props.make(size=(n, n, n), cell_width=(w, w, w), dt=0.15)
     kw = dict(mover=abi.MOVER_DIPOLE, solver=abi.SOLVER_STATIC, projector=abi.PROJECT_NONE, bc=abi.BC_REFLECT,
               flags=abi.F_USE_GRAPH)
-    return ("the reference's :U:N benchmark mode: 32^3 cells of width 10, N = 33,554,432 electrons uniform "
-            "over the universe, velocities U(-0.2,0.2), dipole mover without external field, static fields, "
-            "no projection, reflecting walls, dt 0.15", props, parts, counts, None, kw, 20)
+    return ("the reference's :U:N benchmark mode: 32^3 cells of width 10, N = 33,554,432 electrons from the "
+            "reference's initCells(uniform) streams (made on the device), velocities U(-0.2,0.2), dipole mover "
+            "without external field, static fields, no projection, reflecting walls, dt 0.15", props, None, None,
+            None, kw, 20)
 
 
 def run_config(name, warmup, local):
@@ -564,22 +555,28 @@ def run_config(name, warmup, local):
     t0 = time.perf_counter()
     desc, props, parts, counts, fields, kw, steps = {"c1": config_c1, "c3": config_c3, "c5": config_c5,
                                                      "udist": config_udist}[name]()
-    res = {"workload": desc, "cells": props.ncells, "particles": int(len(parts)), "steps": steps,
-           "warmup": warmup}
-    species = sorted({(float(a), float(b)) for a, b in zip(parts["q"][:1000], parts["qom"][:1000])})
+    res = {"workload": desc, "cells": props.ncells, "particles": int(len(parts)) if parts is not None else UDIST_N,
+           "steps": steps, "warmup": warmup}
+    species = [(-1.0, -25.0)] if parts is None else \
+        sorted({(float(a), float(b)) for a, b in zip(parts["q"][:1000], parts["qom"][:1000])})
     cons = {}
     pre = None
     for pname, prec in (("fp32", abi.FP32), ("fp64", abi.FP64)):
         sim = g.Simulation(props, abi.Config.make(precision=prec, **kw))
         if fields is not None:
             sim.upload_fields(fields[0], fields[1], None)
-        # register the species with a few particles, so that the large upload
-        # takes the device path (one copy, classification on the GPU)
-        first = np.unique(parts[["q", "qom"]][:100000], return_index=True)[1]
-        c0 = np.zeros(props.ncells, np.uint64)
-        c0[0] = len(first)
-        sim.upload_particles(parts[first], c0)
-        sim.upload_particles(parts, counts)
+        if parts is None:  # the reference's :U:N universe, made on the device
+            t_init = time.perf_counter()
+            sim.init_uniform(UDIST_N)
+            res.setdefault("init_ms", {})[pname] = round(1e3 * (time.perf_counter() - t_init), 2)
+        else:
+            # register the species with a few particles, so that the large
+            # upload takes the device path (one copy, classification on the GPU)
+            first = np.unique(parts[["q", "qom"]][:100000], return_index=True)[1]
+            c0 = np.zeros(props.ncells, np.uint64)
+            c0[0] = len(first)
+            sim.upload_particles(parts[first], c0)
+            sim.upload_particles(parts, counts)
         sampler = ClockSampler(local)
         ms, ps, launches, n0, pre = run_timed(sim, warmup, steps, sampler if pname == "fp32" else None, pre)
         res[pname] = {"value": ps / (ms * 1e-3), "ms_per_step": ms / steps, "gpu_launches": int(launches),
@@ -602,6 +599,13 @@ def run_config(name, warmup, local):
     res["fp32_over_fp64"] = res["fp32"]["value"] / res["fp64"]["value"]
     if name == "udist":  # the reference's own CPU algorithm (the oracle port) on the same universe
         cfg = abi.Config.make(precision=abi.FP64, **{k: v for k, v in kw.items() if k != "flags"})
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle
+        parts = np.zeros(UDIST_N, abi.PARTICLE_DTYPE)
+        counts = np.zeros(props.ncells, np.uint64)
+        t_init = time.perf_counter()
+        oracle.load().oracle_init_uniform_bench(C.byref(props), UDIST_N, abi.vptr(parts), abi.vptr(counts))
+        res.setdefault("init_ms", {})["cpu_port"] = round(1e3 * (time.perf_counter() - t_init), 2)
         v, cores, done, secs = cpu_port_run(props, parts, counts, 2, 5, 60.0, cfg)
         res["cpu_port"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                            "sample": "the full universe, %d timed steps (%.1f s) after 2 warm-up steps, all host "
