@@ -109,6 +109,15 @@ def _check(rc):
         raise GpuPathError(rc, buf.value.decode(errors="replace"))
 
 
+def trace_text(rows):
+    """The reference's ConservedQuantities.out text for trace rows: its
+    header, then per row the cycle and four doubles in the default C++ stream
+    format (6 significant digits), tab separated (simulator.h:65-90)."""
+    lines = ["Cycle \t Total Moment \t E energy \t B energy \t Total KE "]
+    lines += ["\t".join([str(int(r[0]))] + ["%g" % v for v in r[1:]]) for r in rows]
+    return "\n".join(lines) + "\n"
+
+
 def boris(particles, E, B, dt, nsteps=1, push_position=True):
     """Particle::updateVelocity (+ updatePosition) applied nsteps times on the
     GPU (particle.h:24-49); `particles` is a PARTICLE_DTYPE array, modified in
@@ -258,6 +267,24 @@ class Simulation:
         out = Stats()
         _check(library().ipic3d_gpu_stats(self._ctx, C.byref(out)))
         return out.as_dict()
+
+    def conserved_trace(self, steps, every=1, path=None):
+        """Runs `steps` steps, one call per cycle, and returns the rows the
+        reference's debug build writes (writeOutputData, simulator.h:65-90):
+        [cycle, total momentum, E energy, B energy, kinetic energy] before
+        every `every`-th cycle and before the last, from the device's
+        reductions. With `path`, also writes them in the reference's
+        ConservedQuantities.out format."""
+        rows = []
+        for i in range(int(steps)):
+            if every > 0 and (i % every == 0 or i + 1 == steps):
+                c = self.conserved()
+                rows.append([i, c["total_momentum"], c["e_energy"], c["b_energy"], c["kinetic_energy"]])
+            self.step(1)
+        if path is not None:
+            with open(path, "w") as f:
+                f.write(trace_text(rows))
+        return rows
 
     def profile(self, enable=True):
         """Per-phase CUDA-event timing of the following steps (no graph)."""

@@ -31,6 +31,7 @@
 
 #include <chrono>
 #include <cstdint>
+#include <ostream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -57,6 +58,13 @@ struct Options {
     int bc_low[3] = {IPIC3D_BC_REFLECT, IPIC3D_BC_REFLECT, IPIC3D_BC_REFLECT};
     int bc_high[3] = {IPIC3D_BC_REFLECT, IPIC3D_BC_REFLECT, IPIC3D_BC_REFLECT};
     uint32_t flags = IPIC3D_F_USE_GRAPH;      // IPIC3D_F_* (J_DIV8, GATHER_DIV_VOL, ...)
+    // The reference's debug-build trace (ENABLE_DEBUG_OUTPUT: writeOutputHeader
+    // and writeOutputData, simulator.h:65-90): when set, the header and the
+    // conserved quantities before every trace_every-th cycle and before the
+    // last are written to *trace, from the device's reductions. The steps then
+    // run one call per cycle.
+    std::ostream* trace = nullptr;
+    int trace_every = 1;
 };
 
 inline Options& options() {
@@ -281,7 +289,22 @@ Durations simulate(std::uint64_t numSteps, Universe& universe) {
     detail::check(ipic3d_gpu_upload_particles(c.ctx, parts.empty() ? nullptr : parts.data(), counts.data(), nullptr),
                   "ipic3d_gpu_upload_particles");
     auto end_first = start;
-    if (numSteps > 0) {
+    if (opt.trace) {
+        *opt.trace << "Cycle \t Total Moment \t E energy \t B energy \t Total KE \n";
+        for (std::uint64_t i = 0; i < numSteps; ++i) {
+            if (opt.trace_every > 0 && (i % (std::uint64_t)opt.trace_every == 0 || i + 1 == numSteps)) {
+                ipic3d_conserved q;
+                detail::check(ipic3d_gpu_conserved(c.ctx, &q), "ipic3d_gpu_conserved");
+                *opt.trace << i << "\t" << q.total_momentum << "\t" << q.e_energy << "\t" << q.b_energy << "\t"
+                           << q.kinetic_energy << "\n";
+            }
+            detail::check(ipic3d_gpu_step(c.ctx, 1), "ipic3d_gpu_step");
+            if (i == 0) {
+                detail::check(ipic3d_gpu_synchronize(c.ctx), "ipic3d_gpu_synchronize");
+                end_first = clock::now();
+            }
+        }
+    } else if (numSteps > 0) {
         detail::check(ipic3d_gpu_step(c.ctx, 1), "ipic3d_gpu_step");
         detail::check(ipic3d_gpu_synchronize(c.ctx), "ipic3d_gpu_synchronize");
         end_first = clock::now();

@@ -8,6 +8,7 @@
 //   policy 1: cic_projector + leapfrog_field_solver + field_particle_mover
 #include <cstdio>
 #include <cstdlib>
+#include <fstream>
 #include <vector>
 
 #include "ipic3d_gpu_simulator.hpp"
@@ -134,6 +135,11 @@ int main(int argc, char** argv) {
         for (auto& b : u.bcfield.data) b.Bc = {0.0, 0.0, 0.1};
     }
     dump((prefix + "_in.bin").c_str(), u);
+    std::ofstream trace;
+    if (argc > 5) {  // the debug-build trace of the conserved quantities
+        trace.open(argv[5]);
+        ipic3d_gpu::options().trace = &trace;
+    }
     try {
         if (policy == 0)
             ipic3d_gpu::simulate<ipic3d_gpu::no_projector, ipic3d_gpu::static_field_solver,

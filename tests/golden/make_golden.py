@@ -9,7 +9,12 @@ Fixtures (all small):
   inp_runs.json      test.inp / tiny.inp driver runs (src/ipic3d.cxx): the
                      distribution parameters, sha256 of the initial and final
                      particle bytes, per-cell counts after ncycles steps and
-                     the conserved quantities.
+                     the conserved quantities; `trace`: the conserved
+                     quantities before every cycle, as the reference's debug
+                     build writes them (simulator.h:65-90). The shipped
+                     outputs/<name>ConservedQuantities.out come from an older
+                     initialisation; only their field-energy columns agree
+                     with the current sources, and those are checked here.
   moves_small.npz    seeded scenarios through simulateSteps with the default
                      policies (mover + export + import): inputs and outputs.
   project_small.npz  projectToDensityField over all nodes.
@@ -64,6 +69,13 @@ def ref_simulate(props, parts, counts, steps):
     return out[:m].copy(), oc, ids[:m].copy()
 
 
+def trace_line(row):
+    """One line of the reference's ConservedQuantities.out: the cycle and four
+    doubles in the default C++ stream format (6 significant digits), tab
+    separated (simulator.h:83-89)."""
+    return "\t".join([str(int(row[0]))] + ["%g" % v for v in row[1:]])
+
+
 def inp_runs():
     res = {}
     for name in ("test", "tiny"):
@@ -84,6 +96,21 @@ def inp_runs():
         c, e, m = 299792458.0, 1.602176565e-19, 1.672621777e-27
         vmod = c / np.sqrt(1.0 + (m * c * c) / (1e7 * e))
         steps = ncyc.value
+        # the conserved quantities before every cycle (writeOutputData with
+        # FieldOutputCycle 1): one step at a time
+        trace = []
+        cur, cur_counts = parts, counts
+        for i in range(steps):
+            cq = abi.Conserved()
+            ref.ref_conserved(C.byref(props), abi.vptr(cur), abi.vptr(cur_counts), abi.vptr(field), C.byref(cq))
+            trace.append([i, cq.total_momentum, cq.e_energy, cq.b_energy, cq.kinetic_energy])
+            cur, cur_counts, _ = ref_simulate(props, cur, cur_counts, 1)
+        ref_lines = open(os.path.join(oracle.REFERENCE_ROOT, "outputs", name + "ConservedQuantities.out")).read()
+        ref_cols = {int(c[0]): c for c in (l.split("\t") for l in ref_lines.strip().splitlines()[1:])}
+        for row in trace:  # the file's cycles (its own output cycle): E energy, B energy
+            line = trace_line(row).split("\t")
+            if row[0] in ref_cols:
+                assert [line[2], line[3]] == ref_cols[row[0]][2:4], (name, line, ref_cols[row[0]])
         out, oc, ids = ref_simulate(props, parts, counts, steps)
         cons = abi.Conserved()
         ref.ref_conserved(C.byref(props), abi.vptr(out), abi.vptr(oc), abi.vptr(field), C.byref(cons))
@@ -93,7 +120,7 @@ def inp_runs():
             "initial_counts_sha256": sha(counts), "initial_particles_sha256": sha(parts),
             "final_counts": oc.tolist(), "final_total": int(oc.sum()),
             "final_particles_sha256": sha(out), "final_ids_sha256": sha(ids),
-            "conserved": cons.as_dict(),
+            "conserved": cons.as_dict(), "trace": trace,
         }
         print(name, N, "->", int(oc.sum()))
     with open(os.path.join(HERE, "inp_runs.json"), "w") as f:

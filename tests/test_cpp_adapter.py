@@ -85,7 +85,8 @@ def test_adapter_standin_matches_c_abi(tmp_path, policy, fp32):
     exe = compile_cpp("adapter_standin.cpp", str(tmp_path / "standin"))
     pre = str(tmp_path / "run")
     steps = 5
-    r = subprocess.run([exe, str(policy), str(fp32), str(steps), pre], capture_output=True, text=True)
+    trace = str(tmp_path / "ConservedQuantities.out")
+    r = subprocess.run([exe, str(policy), str(fp32), str(steps), pre, trace], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     parts, counts = read_dump(pre + "_in.bin")
     out, out_counts = read_dump(pre + "_out.bin")
@@ -109,8 +110,11 @@ def test_adapter_standin_matches_c_abi(tmp_path, policy, fp32):
     sim = Simulation(props, cfg)
     sim.upload_fields(f, bc, np.zeros(abi.density_shape(props)))
     sim.upload_particles(parts, counts)
-    sim.step(steps)
+    rows = sim.conserved_trace(steps)  # one step per call, the conserved quantities before each
     p2, c2, _ = sim.download_particles()
+    if policy == 0:  # the trace the drop-in wrote equals the C ABI's, in the reference's format
+        from allscale_ipic3d_gb300 import trace_text
+        assert open(trace).read() == trace_text(rows)
     np.testing.assert_array_equal(out_counts, c2)
     a, b = sorted_by_cell(out, out_counts), sorted_by_cell(p2, c2)
     if policy == 0:  # no floating-point atomics on the particles' data path

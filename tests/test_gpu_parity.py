@@ -44,6 +44,28 @@ def test_inp_driver_run_counts_bit_exact(name):
     assert got.tolist() == run["final_counts"]
 
 
+@pytest.mark.parametrize("name", ["test", "tiny"])
+def test_inp_conserved_trace(name, tmp_path):
+    """The trace of the reference's debug build (conserved quantities before
+    every cycle, simulator.h:65-90) from the device's reductions: total
+    momentum and kinetic energy per cycle against the reference's, to 1e-12
+    relative, and the written file in the reference's format."""
+    from allscale_ipic3d_gb300 import trace_text
+    run = golden_json("inp_runs.json")[name]
+    props, parts, counts = init_inp(run)
+    sim = gpu_sim(props, reference_config(flags=abi.F_USE_GRAPH))
+    sim.upload_particles(parts, counts)
+    path = str(tmp_path / (name + "ConservedQuantities.out"))
+    rows = sim.conserved_trace(run["ncycles"], path=path)
+    assert [r[0] for r in rows] == [r[0] for r in run["trace"]]
+    for got, ref in zip(rows, run["trace"]):
+        for col in (1, 4):
+            assert abs(got[col] - ref[col]) <= 1e-12 * abs(ref[col]), (got[0], col, got[col], ref[col])
+            assert "%g" % got[col] == "%g" % ref[col], (got[0], col)
+    assert open(path).read() == trace_text(rows)
+    assert sim.cell_counts().tolist() == run["final_counts"]
+
+
 @pytest.mark.parametrize("graph", [False, True])
 def test_inp_steps_one_at_a_time_and_graph(graph):
     run = golden_json("inp_runs.json")["test"]

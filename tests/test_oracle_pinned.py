@@ -127,3 +127,19 @@ def test_trilinear_known_answers():
     assert lib.oracle_trilinear(abi.vptr(c), abi.vptr(half), 0.75) == 4.0
     assert lib.oracle_trilinear(abi.vptr(c), abi.vptr(np.zeros(3)), 3.0) == 0.0
     assert lib.oracle_trilinear(abi.vptr(c), abi.vptr(np.ones(3)), 1.0) == 6.0
+
+
+def test_inp_conserved_trace():
+    """The conserved quantities before every cycle of the test.inp run (the
+    trace of the reference's debug build, simulator.h:65-90): total momentum
+    and kinetic energy per cycle equal to 1e-12 relative, and printed alike."""
+    run = golden_json("inp_runs.json")["test"]
+    props, parts, counts = init_inp(run)
+    sim = OracleSim(props, reference_config())
+    sim.upload_particles(parts, counts)
+    for row in run["trace"]:
+        c = sim.conserved()
+        for k, col in (("total_momentum", 1), ("kinetic_energy", 4)):
+            assert abs(c[k] - row[col]) <= 1e-12 * abs(row[col]), (row[0], k, c[k], row[col])
+            assert "%g" % c[k] == "%g" % row[col], (row[0], k)
+        sim.step(1)
