@@ -31,6 +31,8 @@
 
 #include <chrono>
 #include <cstdint>
+#include <cstdio>
+#include <fstream>
 #include <ostream>
 #include <stdexcept>
 #include <string>
@@ -65,6 +67,13 @@ struct Options {
     // run one call per cycle.
     std::ostream* trace = nullptr;
     int trace_every = 1;
+    // With the trace: the per-cell particle counts before cycle 0 and before
+    // every cycle i with (i + 1) % density_every == 0, written to
+    // density_prefix + "%06d" (t = (i + 1) / density_every) as the
+    // reference's "t,x,y,z,density" files (simulator.h:92-113), from the
+    // device's cell counts. Off when density_every is 0.
+    std::string density_prefix;
+    int density_every = 0;
 };
 
 inline Options& options() {
@@ -250,6 +259,27 @@ struct Context {
     }
 };
 
+// One "t,x,y,z,density" file of the reference's debug output
+// (simulator.h:92-113): per cell, its corner (cell index times width) and
+// its particle count, from the device's cell counts.
+template <class Props>
+void write_density(ipic3d_ctx* ctx, const Props& p, int t, const std::string& prefix) {
+    const int64_t sx = p.size.x, sy = p.size.y, sz = p.size.z;
+    std::vector<uint64_t> counts((size_t)(sx * sy * sz));
+    check(ipic3d_gpu_cell_counts(ctx, counts.data()), "ipic3d_gpu_cell_counts");
+    char name[32];
+    std::snprintf(name, sizeof name, "%06d", t);
+    std::ofstream out(prefix + name);
+    out << "t,x,y,z,density\n";
+    for (int64_t x = 0; x < sx; x++)
+        for (int64_t y = 0; y < sy; y++)
+            for (int64_t z = 0; z < sz; z++) {
+                const double dx = x * p.cellWidth.x, dy = y * p.cellWidth.y, dz = z * p.cellWidth.z;
+                out << t << "," << dx << "," << dy << "," << dz << "," << counts[(size_t)((x * sy + y) * sz + z)]
+                    << "\n";
+            }
+}
+
 }  // namespace detail
 
 /* simulateSteps<Projector, FieldSolver, Mover>(numSteps, universe) on the
@@ -298,6 +328,9 @@ Durations simulate(std::uint64_t numSteps, Universe& universe) {
                 *opt.trace << i << "\t" << q.total_momentum << "\t" << q.e_energy << "\t" << q.b_energy << "\t"
                            << q.kinetic_energy << "\n";
             }
+            if (opt.density_every > 0 && (i == 0 || (i + 1) % (std::uint64_t)opt.density_every == 0))
+                detail::write_density(c.ctx, universe.properties, (int)((i + 1) / (std::uint64_t)opt.density_every),
+                                      opt.density_prefix);
             detail::check(ipic3d_gpu_step(c.ctx, 1), "ipic3d_gpu_step");
             if (i == 0) {
                 detail::check(ipic3d_gpu_synchronize(c.ctx), "ipic3d_gpu_synchronize");

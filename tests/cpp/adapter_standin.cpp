@@ -136,9 +136,11 @@ int main(int argc, char** argv) {
     }
     dump((prefix + "_in.bin").c_str(), u);
     std::ofstream trace;
-    if (argc > 5) {  // the debug-build trace of the conserved quantities
+    if (argc > 5) {  // the debug-build trace of the conserved quantities and the density files
         trace.open(argv[5]);
         ipic3d_gpu::options().trace = &trace;
+        ipic3d_gpu::options().density_prefix = std::string(argv[5]) + ".csv.";
+        ipic3d_gpu::options().density_every = 2;
     }
     try {
         if (policy == 0)

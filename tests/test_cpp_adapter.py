@@ -115,6 +115,14 @@ def test_adapter_standin_matches_c_abi(tmp_path, policy, fp32):
     if policy == 0:  # the trace the drop-in wrote equals the C ABI's, in the reference's format
         from allscale_ipic3d_gb300 import trace_text
         assert open(trace).read() == trace_text(rows)
+    # density files before cycle 0 (t = 0) and cycles 1 and 3 (t = 1, 2): t,x,y,z,density per cell
+    lines = open(trace + ".csv.000000").read().splitlines()
+    assert lines[0] == "t,x,y,z,density" and len(lines) == 1 + props.ncells
+    assert [int(l.split(",")[4]) for l in lines[1:]] == counts.astype(int).tolist()
+    w = props.cell_width[0]
+    assert lines[2] == "0,0,0,%g,%d" % (w, counts[1])
+    for t in (1, 2):
+        assert os.path.exists(trace + ".csv.%06d" % t)
     np.testing.assert_array_equal(out_counts, c2)
     a, b = sorted_by_cell(out, out_counts), sorted_by_cell(p2, c2)
     if policy == 0:  # no floating-point atomics on the particles' data path
