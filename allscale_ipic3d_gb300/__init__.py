@@ -20,7 +20,7 @@ from .abi import (BC_OPEN, BC_PERIODIC, BC_REFLECT, FP32, FP64, MOVER_DIPOLE, MO
                   Props, Stats)
 
 __all__ = ["Simulation", "Batch", "Props", "Config", "Conserved", "Stats", "PARTICLE_DTYPE", "GpuPathError",
-           "library", "library_path", "boris", "EXPORTED_SYMBOLS"]
+           "library", "library_path", "boris", "trace", "trace_device", "trace_frames", "EXPORTED_SYMBOLS"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -65,6 +65,8 @@ _SIGNATURES = [
     ("ipic3d_gpu_get_push_shape", C.c_int, [_vp, _vp]),
     ("ipic3d_gpu_set_push_shape", C.c_int, [_vp, _vp]),
     ("ipic3d_gpu_project_noalloc", C.c_int, [_vp, C.c_uint32, _vp, _vp, _vp, _vp, _vp]),
+    ("ipic3d_gpu_trace", C.c_int, [_vp, _vp, C.c_uint64, C.c_int32, C.c_int32, C.c_int32, _vp]),
+    ("ipic3d_gpu_trace_device", C.c_int, [_vp, _vp, C.c_uint64, C.c_int32, C.c_int32, C.c_int32, _vp, _vp]),
     ("ipic3d_gpu_boris", C.c_int, [_vp, C.c_uint64, _vp, _vp, C.c_double, C.c_uint64, C.c_int]),
     ("ipic3d_gpu_batch_create", C.c_int, [C.c_uint32, _vp, _vp, C.POINTER(_vp)]),
     ("ipic3d_gpu_batch_destroy", C.c_int, [_vp]),
@@ -137,6 +139,35 @@ def project_noalloc(props, flags, d_particles, d_cell_offsets, d_J, d_rho=None, 
     device addresses): the current projection without any allocation."""
     _check(library().ipic3d_gpu_project_noalloc(C.byref(props), int(flags), d_particles, d_cell_offsets, d_J,
                                                 d_rho, stream))
+
+
+def trace_frames(steps, frame_interval):
+    """Frames of a trace of `steps` steps: (steps - 1) // frame_interval + 1
+    (pic_tracer's main traces T + 1 steps into T // S + 1 frames)."""
+    return (int(steps) - 1) // int(frame_interval) + 1 if steps > 0 else 0
+
+
+def trace(props, particles, steps, frame_interval, num_frames=None, counts=None):
+    """traceParticle (pic_tracer.cxx:77-148) for every particle of a
+    PARTICLE_DTYPE array on the GPU. Returns the ParticleCount histogram,
+    uint32 of shape (num_frames, *props.shape); `counts`, if given, is added
+    to in place (pic_tracer.cxx:282)."""
+    p = np.ascontiguousarray(particles, dtype=PARTICLE_DTYPE)
+    frames = trace_frames(steps, frame_interval) if num_frames is None else int(num_frames)
+    if counts is None:
+        counts = np.zeros((frames,) + props.shape, np.uint32)
+    if counts.dtype != np.uint32 or not counts.flags.c_contiguous or counts.size != frames * props.ncells:
+        raise ValueError("counts must be a C-contiguous uint32 array of num_frames x cells entries")
+    _check(library().ipic3d_gpu_trace(C.byref(props), abi.vptr(p), len(p), int(steps), int(frame_interval), frames,
+                                      abi.vptr(counts)))
+    return counts
+
+
+def trace_device(props, d_particles, n, steps, frame_interval, num_frames, d_counts, stream=None):
+    """ipic3d_gpu_trace_device on caller-owned device buffers (integer device
+    addresses): enqueued on `stream`, not synchronised."""
+    _check(library().ipic3d_gpu_trace_device(C.byref(props), d_particles, int(n), int(steps), int(frame_interval),
+                                             int(num_frames), d_counts, stream))
 
 
 class Simulation:

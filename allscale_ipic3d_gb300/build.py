@@ -29,6 +29,7 @@ SOURCES = {
     "upload.cu": ["-fmad=false"],
     "init.cu": ["-fmad=false"],
     "noalloc.cu": ["-fmad=false"],
+    "tracer.cu": ["-fmad=false"],
 }
 
 

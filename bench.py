@@ -615,6 +615,100 @@ def run_config(name, warmup, local):
     return res
 
 
+# ---- the standalone tracer (optional row: --only tracer) --------------------------
+TRACER_T, TRACER_S, TRACER_R = 150, 10, 64
+TRACER_N = 16 * 1000 * 1000
+
+
+def run_tracer(warmup, steps, local, n=TRACER_N, e2e_steps=2, cpu_budget=15.0, cpu=True):
+    """pic_tracer's default run (pic_tracer.cxx:153-158): N = 16M protons
+    traced for T + 1 = 151 steps through the dipole on a 64^3 grid, a frame
+    every S = 10 steps. Its metric is the one pic_tracer prints: (T + 1) N /
+    seconds (pic_tracer.cxx:290). Particles are seeded synthetic draws of its
+    distributions (uniform in the middle 3/4 of the box, normal speeds of
+    width v_mod). One step = one trace of all N particles into the histogram
+    (repetitions accumulate, as pic_tracer's M repetitions do); inputs (1 GB)
+    exceed L2."""
+    import torch
+    import allscale_ipic3d_gb300 as g
+    from allscale_ipic3d_gb300 import abi, tracer
+    props = tracer.tracer_props(TRACER_R)
+    steps1, frames = TRACER_T + 1, TRACER_T // TRACER_S + 1
+    cells = props.ncells
+    rng = np.random.default_rng(2024)
+    low, hig = tracer.particle_box(props)
+    parts = np.zeros(n, abi.PARTICLE_DTYPE)
+    parts["position"] = rng.uniform(low, hig, (n, 3))
+    parts["velocity"] = rng.standard_normal((n, 3)) * tracer.speed_scale(props)
+    parts["q"] = tracer.ELEMENTARY_CHARGE
+    parts["qom"] = tracer.ELEMENTARY_CHARGE / tracer.PROTON_MASS
+    host = torch.from_numpy(parts.view(np.uint8)).pin_memory()
+    dev = host.cuda()
+    d_counts = torch.zeros(frames * cells, dtype=torch.int32, device="cuda")
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def once():
+        g.trace_device(props, dev.data_ptr(), n, steps1, TRACER_S, frames, d_counts.data_ptr(), st.cuda_stream)
+
+    for _ in range(warmup):
+        once()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    with sampler:
+        e0.record(st)
+        for _ in range(steps):
+            once()
+        e1.record(st)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    res = {"workload": "pic_tracer default run: N = 16,000,000 protons (10 MeV normal speeds), T = 150 (151 traced "
+                       "steps), a frame every S = 10 steps, R = 64 (64^3 cells), dt 0.01, Earth dipole 3.07e-5 T"
+                       if n == TRACER_N else "pic_tracer run with N = %d, T = 150, S = 10, R = 64" % n,
+           "particles": n, "traced_steps": steps1, "frames": frames, "steps": steps, "warmup": warmup,
+           "value": steps1 * n * steps / (ms * 1e-3), "unit": "particles/s", "ms_per_step": ms / steps,
+           "gpu_launches": steps, "dtype": "f64", "clocks": sampler.summary(),
+           "l2": "inputs larger than L2 (1 GB of particles)"}
+    # end to end through ipic3d_gpu_trace: pinned host particles and histogram
+    lib = g.library()
+    h_counts = torch.zeros(frames * cells, dtype=torch.int32).pin_memory()
+    rc = lib.ipic3d_gpu_trace(C.byref(props), host.data_ptr(), n, steps1, TRACER_S, frames, h_counts.data_ptr())
+    assert rc == 0, rc
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        rc = lib.ipic3d_gpu_trace(C.byref(props), host.data_ptr(), n, steps1, TRACER_S, frames, h_counts.data_ptr())
+        assert rc == 0, rc
+    secs = time.perf_counter() - t0
+    res["e2e"] = {"value": steps1 * n * e2e_steps / secs, "unit": "particles/s",
+                  "h2d_bytes_per_step": n * 64 + frames * cells * 4, "d2h_bytes_per_step": frames * cells * 4}
+    # every repetition adds the same histogram: the timed device runs did the work
+    reps_dev, reps_host = warmup + steps, 1 + e2e_steps
+    a = d_counts.cpu().numpy().astype(np.int64)
+    b = h_counts.numpy().astype(np.int64)
+    assert (a * reps_host == b * reps_dev).all(), "device and host-entry histograms disagree"
+    res["frame_totals"] = (b.reshape(frames, cells).sum(axis=1) // reps_host).tolist()
+    if cpu:  # the oracle's restatement of traceParticle on the host cores
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle
+        olib = oracle.load()
+        threads = os.cpu_count() or 1
+        olib.oracle_set_threads(threads)
+        m = min(n, 20000)
+        cnt = np.zeros(frames * cells, np.uint32)
+        t0 = time.perf_counter()
+        olib.oracle_trace(C.byref(props), abi.vptr(parts[:m]), m, steps1, TRACER_S, frames, abi.vptr(cnt))
+        probe = time.perf_counter() - t0
+        m2 = int(min(n, max(m, m * cpu_budget / max(probe, 1e-3))))
+        cnt[:] = 0
+        t0 = time.perf_counter()
+        olib.oracle_trace(C.byref(props), abi.vptr(parts[:m2]), m2, steps1, TRACER_S, frames, abi.vptr(cnt))
+        secs = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": steps1 * m2 / secs, "unit": "particles/s", "cores": threads, "kind": "port",
+                               "sample": "the first %d particles of the same set, all %d steps (%.1f s)" %
+                                         (m2, steps1, secs)}
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -624,9 +718,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", default="all", choices=["all", "fp32", "ensemble", "c1", "c3", "c5", "udist"],
+    ap.add_argument("--only", default="all", choices=["all", "fp32", "ensemble", "c1", "c3", "c5", "udist", "tracer"],
                     help="fp32: only the FP32 timed run and its roofline (small profiling runs); "
                          "ensemble: only the batched ensemble; c1/c3/c5: that configuration alone")
+    ap.add_argument("--tracer-particles", type=int, default=TRACER_N)
     ap.add_argument("--universes", type=int, default=256, help="universes of the batched ensemble")
     ap.add_argument("--ensemble-steps", type=int, default=100)
     ap.add_argument("--no-ensemble", action="store_true")
@@ -666,6 +761,14 @@ def main():
         res = run_config(args.only, args.warmup, local)
         if rank == 0:
             print(json.dumps({"metric": METRIC, "unit": UNIT, args.only: res}))
+        return 0
+
+    if args.only == "tracer":
+        res = run_tracer(3, min(args.steps, 5), local, n=args.tracer_particles,
+                         cpu=not args.no_cpu_baseline)
+        if rank == 0:
+            print(json.dumps({"metric": "particles/s (pic_tracer throughput: traced steps x particles / s)",
+                              "tracer": res}))
         return 0
 
     if args.only == "ensemble":

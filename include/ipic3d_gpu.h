@@ -313,6 +313,39 @@ int ipic3d_gpu_batch_get_push_shape(ipic3d_batch* batch, ipic3d_push_shape* out)
 int ipic3d_gpu_project_noalloc(const ipic3d_props* props, uint32_t flags, const ipic3d_particle* d_particles,
                                const uint64_t* d_cell_offsets, double* d_J, double* d_rho, void* stream);
 
+/* ---- the standalone particle tracer (pic_tracer.cxx) -------------------- */
+/* traceParticle (pic_tracer.cxx:77-148) for n independent particles, the
+ * loop body of pic_tracer's map operator (pic_tracer.cxx:242-249). Each
+ * particle is shifted by objectCenter, skipped if it starts inside the
+ * planet (r^2 < planetRadius^2) or outside the universe box [origin,
+ * origin + cellWidth * size], then moved `steps` times (pic_tracer's main
+ * passes T + 1) through the analytic dipole B = -Bext.z R^3 / r^5 (3xz, 3yz,
+ * 2z^2 - x^2 - y^2), E = 0, with the adaptive sub-cycling and Boris rotation
+ * of the reference, wrapped periodically, and stopped once r^2 <=
+ * planetRadius^2. On every step t with t % frame_interval == 0 that it
+ * survives, the cell it was in before the move (getCellCoordinates,
+ * cell.h:64-67) gains one count in frame t / frame_interval.
+ *
+ * counts is the ParticleCount vector (pic_tracer.cxx:26-71): num_frames x
+ * size[0] x size[1] x size[2] uint32, row-major, frame slowest; the calls
+ * ADD to it, as `res += ...` does (pic_tracer.cxx:282). A cell coordinate
+ * on the upper face (a particle exactly at origin + cellWidth * size) lands
+ * where the reference's flat index puts it; an index outside the vector,
+ * undefined behaviour in the reference, is not counted. Arithmetic is FP64
+ * in the reference's order: trajectories and counts equal those of its host
+ * build. num_frames must exceed (steps - 1) / frame_interval (pic_tracer
+ * uses T / S + 1); frame_interval > 0.
+ *
+ * ipic3d_gpu_trace takes host pointers (particles are copied in, counts in
+ * and out; returns when done). ipic3d_gpu_trace_device takes device pointers
+ * (particles 16-byte aligned) and enqueues the work on `stream` (a
+ * cudaStream_t, NULL = default stream) without synchronising. */
+int ipic3d_gpu_trace(const ipic3d_props* props, const ipic3d_particle* particles, uint64_t n, int32_t steps,
+                     int32_t frame_interval, int32_t num_frames, uint32_t* counts);
+int ipic3d_gpu_trace_device(const ipic3d_props* props, const ipic3d_particle* d_particles, uint64_t n,
+                            int32_t steps, int32_t frame_interval, int32_t num_frames, uint32_t* d_counts,
+                            void* stream);
+
 /* ---- errors -------------------------------------------------------------- */
 /* Copies the message of the last failure on this thread into buf. Returns
  * the last status. */

@@ -18,7 +18,8 @@ REFERENCE_ROOT = os.environ.get("IPIC3D_REFERENCE_ROOT", "/root/reference")
 
 
 def build(force=False):
-    srcs = [os.path.join(HERE, "ipic3d_oracle.cpp"), os.path.join(HERE, "ipic3d_oracle_init.cpp")]
+    srcs = [os.path.join(HERE, "ipic3d_oracle.cpp"), os.path.join(HERE, "ipic3d_oracle_init.cpp"),
+            os.path.join(HERE, "ipic3d_oracle_tracer.cpp")]
     hdrs = [os.path.join(HERE, "ipic3d_oracle.h"), os.path.join(HERE, "..", "include", "ipic3d_gpu.h"),
             os.path.join(HERE, "..", "include", "ipic3d_types.h")]
     newest = max(os.path.getmtime(p) for p in srcs + hdrs)
@@ -70,6 +71,9 @@ def load():
         lib.oracle_trilinear.restype = C.c_double
         lib.oracle_init_uniform_pos_normal_speed.argtypes = [vp, C.c_uint64, vp, vp, vp, vp, vp, vp, vp]
         lib.oracle_init_uniform_bench.argtypes = [vp, C.c_uint64, vp, vp]
+        lib.oracle_tracer_config.argtypes = [C.c_int32, vp]
+        lib.oracle_tracer_particles.argtypes = [vp, C.c_uint64, C.c_uint32, vp]
+        lib.oracle_trace.argtypes = [vp, vp, C.c_uint64, C.c_int32, C.c_int32, C.c_int32, vp]
         _oracle = lib
     return _oracle
 

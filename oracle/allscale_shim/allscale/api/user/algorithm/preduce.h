@@ -35,6 +35,24 @@ auto preduce(const Container& c, const Map& map, const Reduce&, const Init& init
     return {res};
 }
 
+// The result of a range reduction, handed out by reference (pic_tracer's
+// ParticleCount is move-only).
+template <typename R>
+struct ready_range {
+    R value;
+    const R& get() const { return value; }
+    void wait() const {}
+};
+
+// preduce(a, b, map, reduce) over the integer range [a, b) with a range map
+// operator map(a, b) -> R, as pic_tracer.cxx:282 uses it: the range is
+// evaluated as one piece, so map runs once on [a, b) and reduce is not
+// needed.
+template <typename Map, typename Reduce>
+auto preduce(int a, int b, const Map& map, const Reduce&) -> ready_range<decltype(map(a, b))> {
+    return ready_range<decltype(map(a, b))>{map(a, b)};
+}
+
 }  // namespace algorithm
 }  // namespace user
 }  // namespace api

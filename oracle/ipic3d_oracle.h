@@ -48,6 +48,15 @@ int oracle_init_uniform_pos_normal_speed(const ipic3d_props* props, uint64_t num
                                          ipic3d_particle* out, uint64_t* counts, uint64_t* n_out);
 int oracle_init_uniform_bench(const ipic3d_props* props, uint64_t numParticles, ipic3d_particle* out,
                               uint64_t* counts);
+void oracle_generate_uniform_pos_normal_speed(const double low[3], const double hig[3], const double mean[3],
+                                              const double stddev[3], uint32_t seed, uint64_t n,
+                                              ipic3d_particle* out);
+
+/* the standalone tracer (ipic3d_oracle_tracer.cpp, pic_tracer.cxx) */
+int oracle_tracer_config(int32_t R, ipic3d_props* out);
+int oracle_tracer_particles(const ipic3d_props* props, uint64_t n, uint32_t seed, ipic3d_particle* out);
+int oracle_trace(const ipic3d_props* props, const ipic3d_particle* particles, uint64_t n, int32_t steps,
+                 int32_t frame_interval, int32_t num_frames, uint32_t* counts);
 
 int oracle_boris(ipic3d_particle* p, uint64_t n, const double E[3], const double B[3], double dt, uint64_t nsteps,
                  int push_position);

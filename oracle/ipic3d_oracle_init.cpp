@@ -212,6 +212,24 @@ int oracle_init_uniform_pos_normal_speed(const ipic3d_props* props, uint64_t num
     return IPIC3D_OK;
 }
 
+// n draws of uniform_pos_normal_speed<>(low, hig, mean, stddev, seed)
+// (cell.h:371-403): positions from the uniform stream seeded seed + 1,
+// velocities from the ziggurat seeded seed + 2, species electron (q = -1,
+// qom = -25; callers overwrite them where the reference does).
+void oracle_generate_uniform_pos_normal_speed(const double low[3], const double hig[3], const double mean[3],
+                                              const double stddev[3], uint32_t seed, uint64_t n,
+                                              ipic3d_particle* out) {
+    UniformVec pos(low, hig, seed + 1);
+    NormalVec vel(mean, stddev, seed + 2);
+    for (uint64_t i = 0; i < n; ++i) {
+        ipic3d_particle& q = out[i];
+        q.q = -1.0;
+        q.qom = -25.0;
+        pos.draw(q.position);
+        vel.draw(q.velocity);
+    }
+}
+
 // initCells(props, numParticles, uniform<>) (cell.h:638-697): the ":U:N"
 // benchmark's universe. Velocities U(-0.2, 0.2) per component, electrons
 // (q = -1, qom = -25, cell.h:107-118).

@@ -20,12 +20,21 @@ Fixtures (all small):
   project_small.npz  projectToDensityField over all nodes.
   fields_small.npz   updateFieldsOnBoundaries, two-phase leapfrog, forward
                      solver at single nodes.
+  tracer_runs.json   the standalone tracer (src/pic_tracer.cxx, built as
+                     oracle/_ref/pic_tracer_ref) run as `pic_tracer N T S R`:
+                     the per-frame histograms it writes (result_*.csv.NNNNNN),
+                     in full for the small cases, as sha256 of the uint32
+                     counts plus per-frame totals for the larger one, and the
+                     sha256 of each frame file's text.
 """
 import ctypes as C
+import glob
 import hashlib
 import json
 import os
+import subprocess
 import sys
+import tempfile
 
 import numpy as np
 
@@ -125,6 +134,31 @@ def inp_runs():
         print(name, N, "->", int(oc.sum()))
     with open(os.path.join(HERE, "inp_runs.json"), "w") as f:
         json.dump(res, f, indent=1)
+
+
+def tracer_runs():
+    exe = os.path.join(oracle.REF_DIR, "pic_tracer_ref")
+    res = []
+    for N, T, S, R, full in ((4000, 40, 10, 8, True), (3000, 23, 7, 12, True), (5000, 150, 10, 32, False)):
+        frames = T // S + 1
+        with tempfile.TemporaryDirectory() as d:
+            subprocess.check_call([exe, str(N), str(T), str(S), str(R)], cwd=d, stdout=subprocess.DEVNULL)
+            counts = np.zeros((frames, R, R, R), np.uint32)
+            texts = []
+            for t in range(frames):
+                (path,) = glob.glob(os.path.join(d, "result_*.csv.%06d" % t))
+                text = open(path, "rb").read()
+                texts.append(hashlib.sha256(text).hexdigest())
+                rows = [l.split(b",") for l in text.splitlines()[1:]]
+                counts[t] = np.array([int(r[4]) for r in rows], np.uint32).reshape(R, R, R)
+        case = {"N": N, "T": T, "S": S, "R": R, "frames": frames, "frame_totals": counts.sum(axis=(1, 2, 3)).tolist(),
+                "counts_sha256": sha(counts), "file_sha256": texts}
+        if full:
+            case["counts"] = counts.ravel().tolist()
+        res.append(case)
+        print("tracer", N, T, S, R, case["frame_totals"])
+    with open(os.path.join(HERE, "tracer_runs.json"), "w") as f:
+        json.dump(res, f)
 
 
 def scatter_into_cells(props, pos, rng_order=None):
@@ -252,3 +286,4 @@ if __name__ == "__main__":
     project_small()
     fields_small()
     inp_runs()
+    tracer_runs()
