@@ -25,25 +25,39 @@ namespace ipg {
 // The reference evaluates pow(|x|^2, 2.5) with the host libm (cell.h:940),
 // whose result is the correctly rounded one in all but rare cases. CUDA's pow
 // is not correctly rounded, so the FP64 path evaluates a^2.5 = a^2 * sqrt(a)
-// in double-double arithmetic (Dekker's exact products via fma, one Newton
-// correction of the correctly rounded sqrt) and rounds once at the end: the
-// result is the correctly rounded one unless a^2.5 lies within ~2^-100
-// relative of a rounding boundary. Valid for 0 <= a < 1e150 (a^2 finite).
-__device__ __forceinline__ double pow25_rn(double a) {
-    if (!(a > 0.0) || a >= 1e150) {
-        if (a == 0.0) return 0.0;
-        if (a != a) return a;
-        return a >= 1e150 ? __longlong_as_double(0x7ff0000000000000LL) : __longlong_as_double(0x7ff8000000000000LL);
-    }
-    double s = __dsqrt_rn(a);          // correctly rounded square root
-    double e = __fma_rn(-s, s, a);     // a - s*s, exact
-    double ds = __ddiv_rn(e, __dmul_rn(2.0, s));  // sqrt(a) = s + ds + O(2^-105)
-    double p = __dmul_rn(a, a);
-    double pe = __fma_rn(a, a, -p);    // a*a = p + pe exactly
-    double h = __dmul_rn(p, s);
-    double l = __fma_rn(p, s, -h);     // p*s = h + l exactly
+// in double-double arithmetic and rounds once at the end. sqrt(a) = s + ds
+// to ~2^-100 relative comes from the reciprocal square root y (error <= 1
+// ulp): s0 = a y, then s = s0 + (a - s0^2) y / 2, the correctly rounded root
+// (exact when a is a square), and ds = (a - s^2) y / 2, with the residuals
+// exact through fma; a^2 = p + pe and p s = h + l are Dekker's exact
+// products. The result is the correctly rounded one unless a^2.5 lies within
+// ~2^-100 relative of a rounding boundary (exact midpoints, from squares,
+// round to even). Inputs in [2^400, 2^410) are scaled by 2^-400 (exactly)
+// and the result by 2^1000; from 2^410 on a^2.5 overflows. Below 2^-400 the
+// result is subnormal or zero and is rounded twice.
+__device__ __forceinline__ double pow25_core(double a) {
+    const double y = rsqrt(a);
+    double s = __dmul_rn(a, y);
+    double e = __fma_rn(-s, s, a);
+    s = __dadd_rn(s, __dmul_rn(__dmul_rn(e, y), 0.5));
+    e = __fma_rn(-s, s, a);
+    const double ds = __dmul_rn(__dmul_rn(e, y), 0.5);
+    const double p = __dmul_rn(a, a);
+    const double pe = __fma_rn(a, a, -p);  // a*a = p + pe exactly
+    const double h = __dmul_rn(p, s);
+    double l = __fma_rn(p, s, -h);         // p*s = h + l exactly
     l = __dadd_rn(l, __dadd_rn(__dmul_rn(p, ds), __dmul_rn(pe, s)));
     return __dadd_rn(h, l);
+}
+
+__device__ __forceinline__ double pow25_rn(double a) {
+    if (a >= 0x1p-400 && a < 0x1p400) return pow25_core(a);
+    if (a != a) return a;
+    if (a < 0.0) return __longlong_as_double(0x7ff8000000000000LL);
+    if (a < 0x1p-800) return 0.0;  // a^2.5 < 2^-2000 (and a == 0)
+    if (a < 0x1p-400) return __dmul_rn(pow25_core(__dmul_rn(a, 0x1p400)), 0x1p-1000);
+    if (a < 0x1p410) return __dmul_rn(pow25_core(__dmul_rn(a, 0x1p-400)), 0x1p1000);
+    return __longlong_as_double(0x7ff0000000000000LL);  // +inf
 }
 
 // ---- the Boris rotation (Particle::updateVelocity, particle.h:31-49) -------

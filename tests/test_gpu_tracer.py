@@ -79,9 +79,8 @@ def test_trace_matches_oracle(seed, size, center, bz, n, steps, interval):
 
 def test_trace_upper_face_aliasing_and_extra_frames():
     """Particles resting on the box's upper faces are counted at the
-    reference's flat index (the next row, or the next frame); on the last
-    frame past the vector's end they are not counted. Extra frames stay
-    zero."""
+    reference's flat index (the next row, or the next frame); past the
+    vector's end they are not counted."""
     props = unit_universe(5, (4, 4, 4), bz=0.0)
     extent = np.array(props.cell_width) * 4
     p = np.zeros(3, abi.PARTICLE_DTYPE)
@@ -89,11 +88,17 @@ def test_trace_upper_face_aliasing_and_extra_frames():
     p["position"][0, 0] = props.origin[0] + extent[0]  # x on the upper face
     p["position"][1, 2] = props.origin[2] + extent[2]  # z on the upper face
     p["qom"] = 1.0
+    totals = {}
     for frames in (3, 5):
         want = oracle_trace(props, p, 21, 10, frames)
         got = ipg.trace(props, p, 21, 10, frames)
         np.testing.assert_array_equal(got, want)
-    assert got[3:].sum() == 0
+        totals[frames] = got.reshape(frames, -1).sum(axis=1).tolist()
+    # steps 0, 10, 20 recorded: the x-face particle lands one frame later
+    # (its frame-2 count falls off the 3-frame vector), the z-face particle
+    # one row later in its own frame
+    assert totals[3] == [2, 3, 3]
+    assert totals[5] == [2, 3, 3, 1, 0]
 
 
 def test_trace_device_entry_and_accumulation():
