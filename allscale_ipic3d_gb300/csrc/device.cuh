@@ -35,6 +35,7 @@ struct Geom {
     double object_center[3];
     double L[3];            // domain length per axis
     double dt, c;
+    double inv_pic;         // 1 / (pi c): the sub-cycle estimate
     double planet_r2;       // planetRadius * planetRadius (cell.h:1126)
     double mft;             // -Bext.z * pow(R, 3), host glibc pow (cell.h:923)
     double vol;             // w.x * w.y * w.z

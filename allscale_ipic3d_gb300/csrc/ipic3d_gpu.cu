@@ -855,6 +855,7 @@ void refresh_geom(ipic3d_ctx* ctx) {
     }
     g.dt = p.dt;
     g.c = p.speed_of_light;
+    g.inv_pic = 1.0 / (3.14159265358979323846 * p.speed_of_light);
     g.planet_r2 = p.planet_radius * p.planet_radius;
     g.mft = -p.external_b[2] * std::pow(p.planet_radius, 3);  // host libm, as cell.h:923
     g.vol = p.cell_width[0] * p.cell_width[1] * p.cell_width[2];

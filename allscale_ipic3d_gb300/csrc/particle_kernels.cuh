@@ -83,6 +83,38 @@ __device__ __forceinline__ void boris(T& u, T& v, T& w, T ex, T ey, T ez, T bx, 
     w = qz + kez;
 }
 
+// x + z for z = k * 0 = +-0 (k finite, z negative when k is): x itself,
+// except -0 + +0 = +0. Integer work in place of the FP64 addition.
+__device__ __forceinline__ double add_zero(double x, bool z_negative) {
+    return (!z_negative && __double_as_longlong(x) == (long long)0x8000000000000000ULL) ? 0.0 : x;
+}
+
+// Particle::updateVelocity (particle.h:31-49) in FP64 for E = 0 (the dipole
+// mover, the tracer): boris<double> with the k E terms (+-0 for finite k)
+// applied as add_zero, bit for bit the same velocities.
+__device__ __forceinline__ void boris_e0(double& u, double& v, double& w, double bx, double by, double bz,
+                                         double qom, double dt) {
+    const double k = qom * 0.5 * dt;
+    if (!isfinite(k)) {  // k E is NaN: the general routine
+        boris<double>(u, v, w, 0.0, 0.0, 0.0, bx, by, bz, qom, dt);
+        return;
+    }
+    const bool kneg = signbit(k);
+    const double tx = k * bx, ty = k * by, tz = k * bz;
+    double t_mag2 = tx * tx;
+    t_mag2 += ty * ty;
+    t_mag2 += tz * tz;
+    const double den = 1.0 + t_mag2;
+    const double sx = (2.0 * tx) / den, sy = (2.0 * ty) / den, sz = (2.0 * tz) / den;
+    const double mx = add_zero(u, kneg), my = add_zero(v, kneg), mz = add_zero(w, kneg);  // v_minus
+    const double px = mx + (my * tz - mz * ty);  // v_prime = v_minus + v_minus x t
+    const double py = my + (mz * tx - mx * tz);
+    const double pz = mz + (mx * ty - my * tx);
+    u = add_zero(mx + (py * sz - pz * sy), kneg);  // v_plus + k E
+    v = add_zero(my + (pz * sx - px * sz), kneg);
+    w = add_zero(mz + (px * sy - py * sx), kneg);
+}
+
 // Sub-cycle count of moveParticles (cell.h:947-952): min(int(dt/dt_sub)+1,
 // 100) with dt_sub = pi c / (4 |qom| |B|^2). Quotients outside the int range
 // (and NaN) convert to INT_MIN on the reference's x86 build, which leaves the
@@ -94,6 +126,23 @@ __device__ __forceinline__ int sub_cycles(T dt, T c, T qom, T bmag) {
     if (!(ratio >= T(-2147483648.0) && ratio < T(2147483647.0))) return 0;
     int n = (int)ratio + 1;
     return n < 100 ? n : 100;
+}
+
+// The FP64 sub-cycle count and step together: dt / dt_sub is first
+// estimated from its product form dt (4 |qom| |B|^2) / (pi c), with inv_pic
+// = 1 / (pi c) rounded any way; below 1/2 the reference's two roundings of
+// the quotient cannot reach 1, so the count is 1 and the step dt (dt / 1.0
+// == dt), without a division. Otherwise sub_cycles and dt / n.
+__device__ __forceinline__ int sub_cycles_dt(double dt, double c, double inv_pic, double qom, double bmag,
+                                             double& dts) {
+    const double est = (dt * ((4.0 * fabs(qom)) * bmag)) * inv_pic;
+    if (fabs(est) < 0.5) {
+        dts = dt;
+        return 1;
+    }
+    const int ns = sub_cycles<double>(dt, c, qom, bmag);
+    dts = dt / double(ns);
+    return ns;
 }
 
 // Outcome of one particle's mover + export step.
@@ -181,10 +230,13 @@ __device__ __forceinline__ int step_particle(const Geom& g, int cx, int cy, int 
     double bmag = bx * bx;
     bmag += by * by;
     bmag += bz * bz;
-    int ns = sub_cycles<double>(g.dt, g.c, qom, bmag);
-    double dts = g.dt / double(ns);
+    double dts;
+    const int ns = sub_cycles_dt(g.dt, g.c, g.inv_pic, qom, bmag, dts);
     for (int s = 0; s < ns; ++s) {
-        boris<double>(p.u, p.v, p.w, ex, ey, ez, bx, by, bz, qom, dts);
+        if (field_mover)
+            boris<double>(p.u, p.v, p.w, ex, ey, ez, bx, by, bz, qom, dts);
+        else
+            boris_e0(p.u, p.v, p.w, bx, by, bz, qom, dts);
         p.x = p.x + p.u * dts;  // updatePosition (particle.h:24-26)
         p.y = p.y + p.v * dts;
         p.z = p.z + p.w * dts;

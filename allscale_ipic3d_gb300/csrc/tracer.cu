@@ -40,38 +40,6 @@ struct TraceArgs {
     uint32_t* counts;
 };
 
-// x + z for z = k * 0 = +-0 (k finite, z negative when k is): x itself,
-// except -0 + +0 = +0. Integer work in place of the FP64 addition.
-__device__ __forceinline__ double add_zero(double x, bool z_negative) {
-    return (!z_negative && __double_as_longlong(x) == (long long)0x8000000000000000ULL) ? 0.0 : x;
-}
-
-// Particle::updateVelocity (particle.h:31-49) for E = 0: the Boris rotation
-// of the shared FP64 routine with the k E terms (+-0 for finite k) applied
-// as add_zero, bit for bit the same velocities.
-__device__ __forceinline__ void boris_e0(double& u, double& v, double& w, double bx, double by, double bz,
-                                         double qom, double dt) {
-    const double k = qom * 0.5 * dt;
-    if (!isfinite(k)) {  // k E is NaN: the general routine
-        boris<double>(u, v, w, 0.0, 0.0, 0.0, bx, by, bz, qom, dt);
-        return;
-    }
-    const bool kneg = signbit(k);
-    const double tx = k * bx, ty = k * by, tz = k * bz;
-    double t_mag2 = tx * tx;
-    t_mag2 += ty * ty;
-    t_mag2 += tz * tz;
-    const double den = 1.0 + t_mag2;
-    const double sx = (2.0 * tx) / den, sy = (2.0 * ty) / den, sz = (2.0 * tz) / den;
-    const double mx = add_zero(u, kneg), my = add_zero(v, kneg), mz = add_zero(w, kneg);  // v_minus
-    const double px = mx + (my * tz - mz * ty);  // v_prime = v_minus + v_minus x t
-    const double py = my + (mz * tx - mx * tz);
-    const double pz = mz + (mx * ty - my * tx);
-    u = add_zero(mx + (py * sz - pz * sy), kneg);  // v_plus + k E
-    v = add_zero(my + (pz * sx - px * sz), kneg);
-    w = add_zero(mz + (px * sy - py * sx), kneg);
-}
-
 __device__ __forceinline__ double sum_sq(double a, double b, double c) {
     double r = a * a;  // allscale::utils::sumOfSquares: 0 + a^2 + b^2 + c^2 (0 + a^2 == a^2)
     r += b * b;
@@ -109,17 +77,9 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const TraceArgs A) {
         const double bx = 3.0 * x * z * fac1;
         const double by = 3.0 * y * z * fac1;
         const double bz = (2.0 * (z * z) - (x * x) - (y * y)) * fac1;
-        // adaptive sub-cycling (pic_tracer.cxx:113-118). dt / dt_sub is
-        // first estimated from its product form; below 1/2 the reference's
-        // two roundings cannot reach 1, so one cycle of dt (dt / 1.0 == dt)
-        const double bmag = sum_sq(bx, by, bz);
-        const double est = (A.dt * ((4.0 * fabs(qom)) * bmag)) * A.inv_pic;
-        int ns = 1;
-        double dts = A.dt;
-        if (!(fabs(est) < 0.5)) {
-            ns = sub_cycles<double>(A.dt, A.c, qom, bmag);
-            dts = A.dt / double(ns);
-        }
+        // adaptive sub-cycling (pic_tracer.cxx:113-118)
+        double dts;
+        const int ns = sub_cycles_dt(A.dt, A.c, A.inv_pic, qom, sum_sq(bx, by, bz), dts);
         for (int s = 0; s < ns; ++s) {
             boris_e0(u, v, w, bx, by, bz, qom, dts);  // updateVelocity (particle.h:31-49)
             P[0] = P[0] + u * dts;                    // updatePosition (particle.h:24-26)
