@@ -206,7 +206,7 @@ class _Null:
         pass
 
 
-def push_roofline(sim, precision, nsteps, props, pops):
+def push_roofline(sim, precision, nsteps, props, pops, headline=True):
     """Live CUDA-event times of the push phase over `nsteps` eager steps; the
     push kernel's algorithmic bytes per launch over its average launch
     duration. The FP32 push is one launch per step for all `pops` species
@@ -215,7 +215,8 @@ def push_roofline(sim, precision, nsteps, props, pops):
     and written once (12 x 4 B FP32, 12 x 8 B FP64), the per-cell field
     coefficients read once (FP32: 48 floats per cell) or the node E, B read
     once (FP64: 48 B per node), and the 4 FP64 node moments written once
-    (32 B per node)."""
+    (32 B per node). The ncu DRAM traffic in `profiles/` is the headline
+    workload's: other workloads report traffic null."""
     sim.profile(True)
     sim.step(nsteps)
     prof = sim.profile_read(reset=True)
@@ -235,8 +236,9 @@ def push_roofline(sim, precision, nsteps, props, pops):
     achieved = bytes_per / (ms_per * 1e-3) / 1e9
     phases = {k: round(v["ms"] / max(v["launches"], 1), 5) for k, v in prof.items() if v["launches"]}
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": profiled_traffic(precision),
-            "kernel": "ipg::k_push32_pipe<3, 2, 15>" if elem == 4 else "ipg::k_push<double>",
+            "traffic": profiled_traffic(precision) if headline else None,
+            "kernel": ("ipg::k_push32_pipe<3, 2, 15>" if headline else "ipg::k_push32_pipe") if elem == 4
+            else "ipg::k_push<double>",
             "bytes_per_launch": bytes_per, "ms_per_launch": ms_per, "launches_per_step": launches_per_step,
             "peak_source": src + ", burst copy", "phase_ms_per_step": phases}
 
@@ -586,7 +588,7 @@ def run_config(name, warmup, local):
             res["push_shape"] = sim.push_shape()
             res["autotune_steps"] = pre
         cons[pname] = sim.conserved()
-        res[pname]["roofline"] = push_roofline(sim, pname, 5, props, len(species))
+        res[pname]["roofline"] = push_roofline(sim, pname, 5, props, len(species), headline=False)
         sim.close()
     tot = lambda c: c["kinetic_energy"] + c["e_energy"] + c["b_energy"]
     res["error_fp32_vs_fp64"] = {"steps": pre + warmup + steps + 5,
