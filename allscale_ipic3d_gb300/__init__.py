@@ -20,7 +20,7 @@ from .abi import (BC_OPEN, BC_PERIODIC, BC_REFLECT, FP32, FP64, MOVER_DIPOLE, MO
                   Props, Stats)
 
 __all__ = ["Simulation", "Batch", "Props", "Config", "Conserved", "Stats", "PARTICLE_DTYPE", "GpuPathError",
-           "library", "library_path", "boris", "trace", "trace_device", "trace_frames", "EXPORTED_SYMBOLS"]
+           "library", "library_path", "boris", "aggregate_contributions", "trace", "trace_device", "trace_frames", "EXPORTED_SYMBOLS"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -65,6 +65,7 @@ _SIGNATURES = [
     ("ipic3d_gpu_get_push_shape", C.c_int, [_vp, _vp]),
     ("ipic3d_gpu_set_push_shape", C.c_int, [_vp, _vp]),
     ("ipic3d_gpu_project_noalloc", C.c_int, [_vp, C.c_uint32, _vp, _vp, _vp, _vp, _vp]),
+    ("ipic3d_gpu_aggregate_contributions", C.c_int, [_vp, _vp, _vp, _vp]),
     ("ipic3d_gpu_trace", C.c_int, [_vp, _vp, C.c_uint64, C.c_int32, C.c_int32, C.c_int32, _vp]),
     ("ipic3d_gpu_trace_device", C.c_int, [_vp, _vp, C.c_uint64, C.c_int32, C.c_int32, C.c_int32, _vp, _vp]),
     ("ipic3d_gpu_boris", C.c_int, [_vp, C.c_uint64, _vp, _vp, C.c_double, C.c_uint64, C.c_int]),
@@ -139,6 +140,13 @@ def project_noalloc(props, flags, d_particles, d_cell_offsets, d_J, d_rho=None, 
     device addresses): the current projection without any allocation."""
     _check(library().ipic3d_gpu_project_noalloc(C.byref(props), int(flags), d_particles, d_cell_offsets, d_J,
                                                 d_rho, stream))
+
+
+def aggregate_contributions(props, d_contributions, d_J, stream=None):
+    """aggregateDensityContributions (cell.h:835-855) over all nodes on
+    caller-owned device buffers (integer device addresses): the (2 size)^3 x 3
+    contribution grid into the (size+1)^3 x 3 J grid, in place."""
+    _check(library().ipic3d_gpu_aggregate_contributions(C.byref(props), d_contributions, d_J, stream))
 
 
 def trace_frames(steps, frame_interval):

@@ -30,6 +30,7 @@ SOURCES = {
     "init.cu": ["-fmad=false"],
     "noalloc.cu": ["-fmad=false"],
     "tracer.cu": ["-fmad=false"],
+    "contrib.cu": ["-fmad=false"],
 }
 
 

@@ -313,6 +313,19 @@ int ipic3d_gpu_batch_get_push_shape(ipic3d_batch* batch, ipic3d_push_shape* out)
 int ipic3d_gpu_project_noalloc(const ipic3d_props* props, uint32_t flags, const ipic3d_particle* d_particles,
                                const uint64_t* d_cell_offsets, double* d_J, double* d_rho, void* stream);
 
+/* ---- density contributions ---------------------------------------------- */
+/* aggregateDensityContributions (cell.h:835-855) at every node of the
+ * (size+1)^3 current-density grid: J(pos) += the contributions at 2 pos +
+ * {-1, 0}^3 that lie inside the (2 size)^3 contribution grid (the buffer of
+ * simulator.h:156, 3 doubles per entry, row-major), then J /= vol, J /= 8.
+ * J is read and written in place (3 doubles per node), as the reference adds
+ * into the node's current J. Device pointers; the work is enqueued on
+ * `stream` (a cudaStream_t, NULL = default stream) without synchronising.
+ * The reference allocates the contribution grid but no phase of its loop
+ * fills it; this is the aggregation step for callers that do. */
+int ipic3d_gpu_aggregate_contributions(const ipic3d_props* props, const double* d_contributions, double* d_J,
+                                       void* stream);
+
 /* ---- the standalone particle tracer (pic_tracer.cxx) -------------------- */
 /* traceParticle (pic_tracer.cxx:77-148) for n independent particles, the
  * loop body of pic_tracer's map operator (pic_tracer.cxx:242-249). Each

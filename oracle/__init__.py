@@ -71,6 +71,7 @@ def load():
         lib.oracle_trilinear.restype = C.c_double
         lib.oracle_init_uniform_pos_normal_speed.argtypes = [vp, C.c_uint64, vp, vp, vp, vp, vp, vp, vp]
         lib.oracle_init_uniform_bench.argtypes = [vp, C.c_uint64, vp, vp]
+        lib.oracle_aggregate_contributions.argtypes = [vp, vp, vp]
         lib.oracle_tracer_config.argtypes = [C.c_int32, vp]
         lib.oracle_tracer_particles.argtypes = [vp, C.c_uint64, C.c_uint32, vp]
         lib.oracle_trace.argtypes = [vp, vp, C.c_uint64, C.c_int32, C.c_int32, C.c_int32, vp]
@@ -99,6 +100,7 @@ def load_reference():
         lib.ref_move_particles.argtypes = [vp, vp, vp, C.c_uint64]
         lib.ref_boris.argtypes = [vp, vp, vp, C.c_double, C.c_uint64, C.c_int]
         lib.ref_project_current.argtypes = [vp, vp, vp, vp]
+        lib.ref_aggregate_contributions.argtypes = [vp, vp, vp]
         lib.ref_update_boundaries.argtypes = [vp, vp, vp]
         lib.ref_leapfrog_two_phase.argtypes = [vp, vp, vp, vp]
         lib.ref_solve_forward_at.argtypes = [vp, vp, vp, vp, vp]

@@ -743,6 +743,36 @@ int oracle_boris(ipic3d_particle* ps, uint64_t n, const double E[3], const doubl
     return IPIC3D_OK;
 }
 
+// aggregateDensityContributions (cell.h:835-855) for every node of the
+// (size+1)^3 J grid from a (2 size)^3 contribution grid: J += the up to 8
+// contributions at 2 pos + {-1, 0}^3 inside that grid (in i, j, k order),
+// then J / vol / 8. J is updated in place.
+int oracle_aggregate_contributions(const ipic3d_props* props, const double* contrib, double* J) {
+    const int64_t cs[3] = {2 * props->size[0], 2 * props->size[1], 2 * props->size[2]};
+    const int64_t ns[3] = {props->size[0] + 1, props->size[1] + 1, props->size[2] + 1};
+    const double vol = props->cell_width[0] * props->cell_width[1] * props->cell_width[2];
+    for (int64_t x = 0; x < ns[0]; ++x)
+        for (int64_t y = 0; y < ns[1]; ++y)
+            for (int64_t z = 0; z < ns[2]; ++z) {
+                double* j = J + 3 * ((x * ns[1] + y) * ns[2] + z);
+                V3 acc = {j[0], j[1], j[2]};
+                for (int i = 0; i < 2; ++i)
+                    for (int jj = 0; jj < 2; ++jj)
+                        for (int k = 0; k < 2; ++k) {
+                            const int64_t c[3] = {2 * x + i - 1, 2 * y + jj - 1, 2 * z + k - 1};
+                            bool in = true;
+                            for (int a = 0; a < 3; ++a) in = in && c[a] >= 0 && c[a] < cs[a];
+                            if (!in) continue;
+                            const double* q = contrib + 3 * ((c[0] * cs[1] + c[1]) * cs[2] + c[2]);
+                            acc = add(acc, V3{q[0], q[1], q[2]});
+                        }
+                j[0] = acc.x / vol / 8.0;
+                j[1] = acc.y / vol / 8.0;
+                j[2] = acc.z / vol / 8.0;
+            }
+    return IPIC3D_OK;
+}
+
 double oracle_trilinear(const double corners[8], const double pos[3], double vol) {
     V3 c[2][2][2];
     for (int i = 0; i < 8; ++i) c[i / 4][(i / 2) % 2][i % 2] = {corners[i], 0.0, 0.0};

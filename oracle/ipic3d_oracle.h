@@ -61,6 +61,7 @@ int oracle_trace(const ipic3d_props* props, const ipic3d_particle* particles, ui
 int oracle_boris(ipic3d_particle* p, uint64_t n, const double E[3], const double B[3], double dt, uint64_t nsteps,
                  int push_position);
 double oracle_trilinear(const double corners[8], const double pos[3], double vol);
+int oracle_aggregate_contributions(const ipic3d_props* props, const double* contrib, double* J);
 
 #ifdef __cplusplus
 }

@@ -178,6 +178,24 @@ int ref_project_current(const ipic3d_props* props, const ipic3d_particle* in, co
     return 0;
 }
 
+// aggregateDensityContributions (cell.h:835-855) for every node of the
+// (size+1)^3 CurrentDensity grid from a (2 size)^3 contribution grid (the
+// buffer of simulator.h:156); J (3 doubles per node) is read and updated in
+// place, as the reference adds into the node's J.
+int ref_aggregate_contributions(const ipic3d_props* props, const double* contrib, double* J) {
+    Universe u(to_props(props));
+    CurrentDensity c(u.properties.size * 2);
+    grid_in(c, contrib, 3);
+    grid_in(u.currentDensity, J, 3);
+    auto sz = u.currentDensity.size();
+    for (int64_t x = 0; x < sz.x; ++x)
+        for (int64_t y = 0; y < sz.y; ++y)
+            for (int64_t z = 0; z < sz.z; ++z)
+                aggregateDensityContributions(u.properties, c, {x, y, z}, u.currentDensity[{x, y, z}]);
+    grid_out(u.currentDensity, J, 3);
+    return 0;
+}
+
 // updateFieldsOnBoundaries (field.h:407-440) on a (size+3)^3 Field and a
 // (size+2)^3 BcField.
 int ref_update_boundaries(const ipic3d_props* props, double* field, double* bcfield) {

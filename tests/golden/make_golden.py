@@ -20,6 +20,8 @@ Fixtures (all small):
   project_small.npz  projectToDensityField over all nodes.
   fields_small.npz   updateFieldsOnBoundaries, two-phase leapfrog, forward
                      solver at single nodes.
+  aggregate_small.npz  aggregateDensityContributions over all nodes of two
+                     grids from seeded contribution grids and starting J.
   tracer_runs.json   the standalone tracer (src/pic_tracer.cxx, built as
                      oracle/_ref/pic_tracer_ref) run as `pic_tracer N T S R`:
                      the per-frame histograms it writes (result_*.csv.NNNNNN),
@@ -255,6 +257,22 @@ def project_small():
     np.savez_compressed(os.path.join(HERE, "project_small.npz"), **out)
 
 
+def aggregate_small():
+    out = {}
+    for name, seed, size, width in (("a3", 21, (3, 3, 3), (0.5, 0.5, 0.5)), ("a425", 22, (4, 2, 5), (1.0, 2.0, 0.75))):
+        props = abi.Props.make(size=size, cell_width=width, dt=0.1)
+        rng = np.random.default_rng(seed)
+        contrib = rng.normal(0.0, 1.0, tuple(2 * v for v in size) + (3,))
+        J0 = rng.normal(0.0, 1.0, abi.density_shape(props))
+        J = J0.copy()
+        ref.ref_aggregate_contributions(C.byref(props), abi.vptr(contrib), abi.vptr(J))
+        out[name + "_props"] = props_vec(props)
+        out[name + "_contrib"] = contrib
+        out[name + "_J0"] = J0
+        out[name + "_J"] = J
+    np.savez_compressed(os.path.join(HERE, "aggregate_small.npz"), **out)
+
+
 def fields_small():
     rng = np.random.default_rng(21)
     out = {}
@@ -287,3 +305,4 @@ if __name__ == "__main__":
     fields_small()
     inp_runs()
     tracer_runs()
+    aggregate_small()

@@ -143,3 +143,18 @@ def test_inp_conserved_trace():
             assert abs(c[k] - row[col]) <= 1e-12 * abs(row[col]), (row[0], k, c[k], row[col])
             assert "%g" % c[k] == "%g" % row[col], (row[0], k)
         sim.step(1)
+
+
+@pytest.mark.parametrize("name", ["a3", "a425"])
+def test_aggregate_contributions_bit_exact(name):
+    """aggregateDensityContributions (cell.h:835-855) over all nodes: the
+    restatement against the reference's own function (fixture)."""
+    import ctypes as C
+
+    import oracle
+    g = golden_npz("aggregate_small.npz")
+    props = props_from_vec(g[name + "_props"])
+    J = np.ascontiguousarray(g[name + "_J0"]).copy()
+    contrib = np.ascontiguousarray(g[name + "_contrib"])
+    assert oracle.load().oracle_aggregate_contributions(C.byref(props), abi.vptr(contrib), abi.vptr(J)) == 0
+    np.testing.assert_array_equal(J, g[name + "_J"])
