@@ -155,6 +155,20 @@ def profiled_traffic(precision):
     return None
 
 
+def combine_ranks(ms, psteps, dist, device):
+    """Whole-job figures over the ranks of a replica run: the slowest rank's
+    time and the particle-steps of all ranks (every rank advances its own
+    universe; nothing is exchanged on the data path)."""
+    if dist is None:
+        return ms, psteps
+    import torch
+    t = torch.tensor([ms, psteps], device=device, dtype=torch.float64)
+    tmax = t.clone()
+    dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(tmax[0]), float(t[1])
+
+
 def autotune(sim, limit=100):
     """The push-shape autotuner's trial steps (FP32 contexts): ordinary steps
     of the simulation, run before the warm-up and outside any timing, until
@@ -792,11 +806,7 @@ def main():
     shape32 = sim32.push_shape()
     if dist:
         dist.barrier()
-        t = torch.tensor([ms32, psteps32], device="cuda", dtype=torch.float64)
-        tmax = t.clone()
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        ms32, psteps32 = float(tmax[0]), float(t[1])
+    ms32, psteps32 = combine_ranks(ms32, psteps32, dist, "cuda")
     value32 = psteps32 / (ms32 * 1e-3)
     stats32 = sim32.stats()
 
@@ -852,11 +862,8 @@ def main():
         phase["counts"] += td - tc
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    e2e_value = len(parts) * args.e2e_steps / e2e_s
-    if dist:
-        t = torch.tensor([e2e_value], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        e2e_value = float(t[0])
+    e2e_ms, e2e_psteps = combine_ranks(1e3 * e2e_s, float(len(parts) * args.e2e_steps), dist, "cuda")
+    e2e_value = e2e_psteps / (e2e_ms * 1e-3)
     e2e.close()
 
     ens = None
