@@ -350,7 +350,9 @@ int ipic3d_gpu_aggregate_contributions(const ipic3d_props* props, const double* 
  * uses T / S + 1); frame_interval > 0.
  *
  * ipic3d_gpu_trace takes host pointers (particles are copied in, counts in
- * and out; returns when done). ipic3d_gpu_trace_device takes device pointers
+ * and out; returns when done; calls are serialised, and the device buffers
+ * and stream it uses are kept, grown on demand, until the process exits).
+ * ipic3d_gpu_trace_device takes device pointers
  * (particles 16-byte aligned) and enqueues the work on `stream` (a
  * cudaStream_t, NULL = default stream) without synchronising. */
 int ipic3d_gpu_trace(const ipic3d_props* props, const ipic3d_particle* particles, uint64_t n, int32_t steps,
