@@ -358,6 +358,35 @@ Durations simulate(std::uint64_t numSteps, Universe& universe) {
             std::chrono::duration<double>(end - end_first).count()};
 }
 
+/* traceParticle (pic_tracer.cxx:77-148) on the GPU for every particle of a
+ * range of the reference's Particle objects (anything with position,
+ * velocity, q and qom members), `steps` steps each (pic_tracer's main passes
+ * T + 1), counting into `counts`, the ParticleCount vector (num_frames x
+ * cells uint32, row-major, frame slowest), which is added to as traceParticle
+ * increments it. `config` is the UniverseProperties the tracer runs with.
+ * Throws Error on failure. */
+template <class Props, class Particles>
+void trace_particles(const Props& config, const Particles& particles, int steps, int frame_interval, int num_frames,
+                     std::uint32_t* counts) {
+    std::vector<ipic3d_particle> buf;
+    buf.reserve(particles.size());
+    for (const auto& p : particles) {
+        ipic3d_particle q;
+        q.position[0] = p.position.x;
+        q.position[1] = p.position.y;
+        q.position[2] = p.position.z;
+        q.velocity[0] = p.velocity.x;
+        q.velocity[1] = p.velocity.y;
+        q.velocity[2] = p.velocity.z;
+        q.q = p.q;
+        q.qom = p.qom;
+        buf.push_back(q);
+    }
+    const ipic3d_props props = detail::props_of(config);
+    detail::check(ipic3d_gpu_trace(&props, buf.data(), buf.size(), steps, frame_interval, num_frames, counts),
+                  "ipic3d_gpu_trace");
+}
+
 }  // namespace ipic3d_gpu
 
 #endif /* IPIC3D_GPU_SIMULATOR_HPP */

@@ -108,6 +108,23 @@ int main(int argc, char** argv) {
     } catch (const ipic3d_gpu::Error& e) {
         std::printf("status %d\n", e.status());
     }
+    // the tracer helper over the reference's Particle and UniverseProperties
+    std::vector<Particle> tracer_particles;
+    for (const auto& q : parts) {
+        Particle p;
+        p.position = {q.position[0], q.position[1], q.position[2]};
+        p.velocity = {q.velocity[0], q.velocity[1], q.velocity[2]};
+        p.q = q.q;
+        p.qom = q.qom;
+        tracer_particles.push_back(p);
+    }
+    std::vector<std::uint32_t> frames(3 * n * n * n, 0);
+    try {
+        ipic3d_gpu::trace_particles(props, tracer_particles, 21, 10, 3, frames.data());
+        std::printf("traced\n");
+    } catch (const ipic3d_gpu::Error& e) {
+        std::printf("trace status %d\n", e.status());
+    }
     (void)argc;
     (void)argv;
     return bad ? 1 : 0;

@@ -49,6 +49,7 @@ def test_adapter_over_reference_universe(tmp_path):
     assert r.returncode == 0
     if not gpu_present():
         assert "status %d" % abi.E_NODEVICE in r.stdout
+        assert "trace status %d" % abi.E_NODEVICE in r.stdout
 
 
 def test_adapter_standin_builds_and_fails_loudly_without_gpu(tmp_path):
@@ -132,3 +133,29 @@ def test_adapter_standin_matches_c_abi(tmp_path, policy, fp32):
         rtol, atol = (1e-5, 1e-7) if fp32 else (1e-9, 1e-12)
         for k in ("position", "velocity"):
             np.testing.assert_allclose(a[k], b[k], rtol=rtol, atol=atol)
+
+
+@pytest.mark.gpu
+def test_tracer_standin_matches_c_abi(tmp_path):
+    """ipic3d_gpu::trace_particles over stand-in Particle / properties types
+    equals the Python binding's trace on the same particles."""
+    import allscale_ipic3d_gb300 as ipg
+    from allscale_ipic3d_gb300 import library, tracer
+    library(build_if_missing=True)
+    exe = compile_cpp("tracer_standin.cpp", str(tmp_path / "tracer_standin"))
+    R, steps, S = 16, 31, 10
+    props = tracer.tracer_props(R)
+    rng = np.random.default_rng(5)
+    low, hig = tracer.particle_box(props)
+    parts = np.zeros(20000, abi.PARTICLE_DTYPE)
+    parts["position"] = rng.uniform(low, hig, (len(parts), 3))
+    parts["velocity"] = rng.normal(0.0, tracer.speed_scale(props), (len(parts), 3))
+    parts["q"] = tracer.ELEMENTARY_CHARGE
+    parts["qom"] = tracer.ELEMENTARY_CHARGE / tracer.PROTON_MASS
+    src, dst = str(tmp_path / "p.bin"), str(tmp_path / "c.bin")
+    parts.tofile(src)
+    frames = ipg.trace_frames(steps, S)
+    r = subprocess.run([exe, str(R), str(steps), str(S), str(frames), src, dst], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    got = np.fromfile(dst, np.uint32).reshape((frames,) + props.shape)
+    np.testing.assert_array_equal(got, ipg.trace(props, parts, steps, S))
