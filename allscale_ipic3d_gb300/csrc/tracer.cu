@@ -28,6 +28,7 @@ struct TraceArgs {
     double extent[3];        // width * size (the wrap distance)
     double w[3];             // cell width (getCellCoordinates)
     double center[3];        // objectCenter
+    int center_zero;         // objectCenter == 0: the planet test's r^2 is the next step's field r^2
     double r2max;            // planetRadius^2
     double mft;              // -Bext.z * pow(planetRadius, 3), host libm
     double dt, c;
@@ -63,6 +64,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const TraceArgs A) {
         if (P[a] > A.high[a] || P[a] < A.low[a]) return;
 
     int64_t next_record = 0, frame = 0;
+    double rf2 = sum_sq(P[0], P[1], P[2]);  // |position|^2 of the field
     for (int t = 0; t < A.steps; ++t) {
         const bool record = t == next_record;  // t % frame_interval == 0
         int64_t cx = 0, cy = 0, cz = 0;
@@ -73,7 +75,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const TraceArgs A) {
         }
         // dipole B at the absolute position, E = 0 (pic_tracer.cxx:104-111)
         const double x = P[0], y = P[1], z = P[2];
-        const double fac1 = A.mft / pow25_rn(sum_sq(x, y, z));
+        const double fac1 = A.mft / pow25_rn(rf2);
         const double bx = 3.0 * x * z * fac1;
         const double by = 3.0 * y * z * fac1;
         const double bz = (2.0 * (z * z) - (x * x) - (y * y)) * fac1;
@@ -92,8 +94,13 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const TraceArgs A) {
             if (P[a] > A.high[a]) P[a] = P[a] - A.extent[a];
             if (P[a] < A.low[a]) P[a] = P[a] + A.extent[a];
         }
-        // tracing stops inside the planet (pic_tracer.cxx:135-141)
-        if (sum_sq(P[0] - A.center[0], P[1] - A.center[1], P[2] - A.center[2]) <= A.r2max) break;
+        // tracing stops inside the planet (pic_tracer.cxx:135-141); with the
+        // object at the origin, p - center is p itself, so the test's r^2 is
+        // the one the next step's field needs
+        rf2 = sum_sq(P[0], P[1], P[2]);
+        const double rp2 =
+            A.center_zero ? rf2 : sum_sq(P[0] - A.center[0], P[1] - A.center[1], P[2] - A.center[2]);
+        if (rp2 <= A.r2max) break;
         if (record) {
             // ParticleCount::increment(t / frame_interval, pos): the flat
             // index of its row-major vector, coordinates cast to int
@@ -131,6 +138,7 @@ int trace_args(const ipic3d_props* props, uint64_t n, int32_t steps, int32_t fra
         A.center[a] = props->object_center[a];
         A.size[a] = props->size[a];
     }
+    A.center_zero = props->object_center[0] == 0.0 && props->object_center[1] == 0.0 && props->object_center[2] == 0.0;
     A.r2max = props->planet_radius * props->planet_radius;
     A.mft = -props->external_b[2] * std::pow(props->planet_radius, 3);
     A.dt = props->dt;
