@@ -136,7 +136,9 @@ __device__ __forceinline__ int sub_cycles(T dt, T c, T qom, T bmag) {
 __device__ __forceinline__ int sub_cycles_dt(double dt, double c, double inv_pic, double qom, double bmag,
                                              double& dts) {
     const double est = (dt * ((4.0 * fabs(qom)) * bmag)) * inv_pic;
-    if (fabs(est) < 0.5) {
+    // |est| < 0.5 on the bit pattern (NaN compares above): integer work in
+    // place of an FP64 comparison
+    if ((__double_as_longlong(est) & 0x7fffffffffffffffLL) < 0x3fe0000000000000LL) {
         dts = dt;
         return 1;
     }

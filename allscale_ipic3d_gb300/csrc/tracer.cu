@@ -12,6 +12,7 @@
 // the sub-cycle rule, the Boris rotation and the periodic wrap are those of
 // the reference, so trajectories and counts match its host build.
 #include <cmath>
+#include <cstring>
 #include <mutex>
 
 #include "../../include/ipic3d_gpu.h"
@@ -29,6 +30,8 @@ struct TraceArgs {
     double w[3];             // cell width (getCellCoordinates)
     double center[3];        // objectCenter
     int center_zero;         // objectCenter == 0: the planet test's r^2 is the next step's field r^2
+    int int_cmp;             // box and planet radius finite: comparisons on bit patterns
+    long long key_low[3], key_high[3];  // order_key of low, high
     double r2max;            // planetRadius^2
     double mft;              // -Bext.z * pow(planetRadius, 3), host libm
     double dt, c;
@@ -40,6 +43,18 @@ struct TraceArgs {
     uint64_t n;
     uint32_t* counts;
 };
+
+// An integer that orders finite and infinite doubles as their values do
+// (+0 and -0 both map to 0); NaN is tested apart. The comparisons of the
+// step loop run on these keys, in the integer pipe, which the FP64-bound
+// loop leaves idle.
+__device__ __forceinline__ long long order_key(double x) {
+    const long long b = __double_as_longlong(x);
+    return b >= 0 ? b : -(b & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool is_nan_bits(double x) {
+    return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
 
 __device__ __forceinline__ double sum_sq(double a, double b, double c) {
     double r = a * a;  // allscale::utils::sumOfSquares: 0 + a^2 + b^2 + c^2 (0 + a^2 == a^2)
@@ -89,10 +104,23 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const TraceArgs A) {
             P[2] = P[2] + w * dts;
         }
         // periodic wrap (pic_tracer.cxx:129-133)
+        if (A.int_cmp) {
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            if (P[a] > A.high[a]) P[a] = P[a] - A.extent[a];
-            if (P[a] < A.low[a]) P[a] = P[a] + A.extent[a];
+            for (int a = 0; a < 3; ++a) {
+                const bool nan = is_nan_bits(P[a]);  // NaN compares false both ways
+                long long k = order_key(P[a]);
+                if (!nan && k > A.key_high[a]) {
+                    P[a] = P[a] - A.extent[a];
+                    k = order_key(P[a]);
+                }
+                if (!nan && k < A.key_low[a]) P[a] = P[a] + A.extent[a];
+            }
+        } else {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                if (P[a] > A.high[a]) P[a] = P[a] - A.extent[a];
+                if (P[a] < A.low[a]) P[a] = P[a] + A.extent[a];
+            }
         }
         // tracing stops inside the planet (pic_tracer.cxx:135-141); with the
         // object at the origin, p - center is p itself, so the test's r^2 is
@@ -100,7 +128,12 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const TraceArgs A) {
         rf2 = sum_sq(P[0], P[1], P[2]);
         const double rp2 =
             A.center_zero ? rf2 : sum_sq(P[0] - A.center[0], P[1] - A.center[1], P[2] - A.center[2]);
-        if (rp2 <= A.r2max) break;
+        // rp2 is >= 0 or NaN and r2max finite >= 0: their bit patterns
+        // without the sign order as the values (a NaN of either sign lies
+        // above everything, so "<=" fails as in FP64)
+        if (A.int_cmp ? (__double_as_longlong(rp2) & 0x7fffffffffffffffLL) <= __double_as_longlong(A.r2max)
+                      : rp2 <= A.r2max)
+            break;
         if (record) {
             // ParticleCount::increment(t / frame_interval, pos): the flat
             // index of its row-major vector, coordinates cast to int
@@ -140,6 +173,16 @@ int trace_args(const ipic3d_props* props, uint64_t n, int32_t steps, int32_t fra
     }
     A.center_zero = props->object_center[0] == 0.0 && props->object_center[1] == 0.0 && props->object_center[2] == 0.0;
     A.r2max = props->planet_radius * props->planet_radius;
+    A.int_cmp = std::isfinite(A.r2max) && A.r2max >= 0.0;
+    for (int a = 0; a < 3; ++a) {
+        A.int_cmp = A.int_cmp && std::isfinite(A.low[a]) && std::isfinite(A.high[a]);
+        // order_key on the host: the same mapping
+        long long bl, bh;
+        std::memcpy(&bl, &A.low[a], 8);
+        std::memcpy(&bh, &A.high[a], 8);
+        A.key_low[a] = bl >= 0 ? bl : -(bl & 0x7fffffffffffffffLL);
+        A.key_high[a] = bh >= 0 ? bh : -(bh & 0x7fffffffffffffffLL);
+    }
     A.mft = -props->external_b[2] * std::pow(props->planet_radius, 3);
     A.dt = props->dt;
     A.c = props->speed_of_light;
