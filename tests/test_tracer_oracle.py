@@ -95,3 +95,23 @@ def test_oracle_trace_accumulates_and_checks_arguments():
     c = np.zeros(8 ** 3 * 2, np.uint32)
     assert lib.oracle_trace(C.byref(props), abi.vptr(parts), 500, 21, 10, 2, abi.vptr(c)) != 0  # frames too few
     assert lib.oracle_trace(C.byref(props), abi.vptr(parts), 500, 21, 0, 3, abi.vptr(c)) != 0   # interval 0
+
+
+def test_oracle_trace_upper_face_semantics():
+    """A particle resting exactly on the box's upper x face has cell
+    coordinate `size`: the reference's flat index puts its count into the
+    next frame's x = 0 row, and past the vector's end (last frame) it is not
+    counted; on the upper z face it lands in the next row of its own frame."""
+    props = abi.Props.make(size=(4, 4, 4), cell_width=(1.0, 0.75, 1.25), dt=0.05, speed_of_light=1.0,
+                           planet_radius=1.0, origin=(-2.0, -1.5, -2.5))
+    extent = np.array(props.cell_width) * 4
+    p = np.zeros(3, abi.PARTICLE_DTYPE)
+    p["position"] = np.array(props.origin) + 0.3 * extent
+    p["position"][0, 0] = props.origin[0] + extent[0]
+    p["position"][1, 2] = props.origin[2] + extent[2]
+    p["qom"] = 1.0  # no field (Bz = 0): the particles rest
+    three = oracle_trace(props, p, 21, 10, 3)
+    five = oracle_trace(props, p, 21, 10, 5)
+    assert three.reshape(3, -1).sum(axis=1).tolist() == [2, 3, 3]
+    assert five.reshape(5, -1).sum(axis=1).tolist() == [2, 3, 3, 1, 0]
+    assert five[1, 0].sum() == 1 and five[3, 0].sum() == 1   # x = size -> next frame, x = 0
