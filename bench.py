@@ -741,6 +741,7 @@ def main():
     ap.add_argument("--universes", type=int, default=256, help="universes of the batched ensemble")
     ap.add_argument("--ensemble-steps", type=int, default=100)
     ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--no-tracer", action="store_true", help="skip the standalone tracer's row in the full run")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -866,6 +867,15 @@ def main():
     e2e_value = e2e_psteps / (e2e_ms * 1e-3)
     e2e.close()
 
+    tracer_row = None
+    if not args.no_tracer and world == 1:  # pic_tracer's default run (its own metric), beside the headline
+        try:
+            tracer_row = run_tracer(3, 5, local, cpu_budget=8.0,
+                                    cpu=rank == 0 and world == 1 and not args.no_cpu_baseline)
+        except Exception as e:  # the headline line is printed regardless
+            tracer_row = {"error": "%s: %s" % (type(e).__name__, e)}
+        torch.cuda.empty_cache()
+
     ens = None
     if not args.no_ensemble:
         ens = run_ensemble(args.universes, args.warmup, args.ensemble_steps, local)
@@ -893,6 +903,7 @@ def main():
         "stats": stats32,
         "cpu_baseline": cpu,
         "ensemble": ens,
+        "tracer": tracer_row,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(parts.nbytes + counts.nbytes),
                 "ms_per_phase": {k: round(1e3 * v / args.e2e_steps, 3) for k, v in phase.items()},
                 "d2h_bytes_per_step": int(res.nbytes)},
