@@ -253,6 +253,15 @@ int ipic3d_gpu_trace(const ipic3d_props* props, const ipic3d_particle* particles
     if ((rc = check_device(dev)) != IPIC3D_OK) return rc;
     std::lock_guard<std::mutex> lock(g_tb.mu);
     if (g_tb.dev != dev) {  // first call, or another current device: start over
+        if (g_tb.dev >= 0) {  // release the other device's buffers and stream on that device
+            if (cudaSetDevice(g_tb.dev) == cudaSuccess) {
+                if (g_tb.particles) cudaFree(g_tb.particles);
+                if (g_tb.counts) cudaFree(g_tb.counts);
+                if (g_tb.st) cudaStreamDestroy(g_tb.st);
+            }
+            TR_CU(cudaSetDevice(dev));
+            g_tb.dev = -1;
+        }
         g_tb.particles = nullptr;
         g_tb.particles_cap = 0;
         g_tb.counts = nullptr;
