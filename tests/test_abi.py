@@ -85,3 +85,33 @@ def test_batch_create_without_gpu_fails_loudly():
     assert lib.ipic3d_gpu_batch_create(2, props, C.byref(cfg), C.byref(b)) == abi.E_NODEVICE
     assert lib.ipic3d_gpu_batch_create(0, props, C.byref(cfg), C.byref(b)) == abi.E_INVALID
     assert not b.value
+
+
+def test_tracer_arguments_and_no_gpu():
+    """ipic3d_gpu_trace checks its arguments before any device work, does
+    nothing for an empty set, and refuses without an sm_103 GPU."""
+    import numpy as np
+    import pytest
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    from allscale_ipic3d_gb300 import tracer
+    props = tracer.tracer_props(8)
+    parts = np.zeros(4, abi.PARTICLE_DTYPE)
+    with pytest.raises(pkg.GpuPathError) as e:
+        pkg.trace(props, parts, 21, 10, num_frames=2)   # frame 2 does not fit
+    assert e.value.status == abi.E_INVALID
+    with pytest.raises(pkg.GpuPathError) as e:
+        pkg.trace(props, parts, 21, 0, num_frames=3)    # frame interval 0
+    assert e.value.status == abi.E_INVALID
+    assert pkg.trace(props, parts[:0], 21, 10).sum() == 0   # nothing to trace
+    assert pkg.trace(props, parts, 0, 10, num_frames=0).size == 0
+    with pytest.raises(pkg.GpuPathError) as e:
+        pkg.trace(props, parts, 21, 10)
+    assert e.value.status == abi.E_NODEVICE
+    with pytest.raises(pkg.GpuPathError) as e:
+        pkg.aggregate_contributions(props, None, None)
+    assert e.value.status == abi.E_INVALID
