@@ -115,3 +115,26 @@ def test_tracer_arguments_and_no_gpu():
     with pytest.raises(pkg.GpuPathError) as e:
         pkg.aggregate_contributions(props, None, None)
     assert e.value.status == abi.E_INVALID
+
+
+def test_plain_c_consumer(tmp_path):
+    """The header is C99 and the library links from C (the form cgo, JNI or
+    N-API bindings use)."""
+    import subprocess
+    import pytest
+    lib = os.path.dirname(pkg.library_path())
+    pkg.library(build_if_missing=True)
+    exe = str(tmp_path / "c_consumer")
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I" + os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "cpp", "c_consumer.c"), "-L" + lib, "-lipic3d_gb300",
+                        "-Wl,-rpath," + lib, "-o", exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=120).stdout
+    assert "defaults 0 0 0 0" in out
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    assert "create %d " % abi.E_NODEVICE in out
