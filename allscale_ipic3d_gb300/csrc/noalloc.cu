@@ -5,6 +5,8 @@
 // its own pool, or a per-step loop that must not synchronise the device.
 // The caller passes the particles and the output grids; the FP64 node sums
 // in between live in a file-scope device array, so no call here allocates.
+#include <cuda.h>
+
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -22,10 +24,40 @@ namespace {
 constexpr int64_t kNoAllocMaxNodes = 33LL * 33 * 33;
 __device__ __align__(256) double g_noalloc_scratch[4 * kNoAllocMaxNodes];
 
-// device address of g_noalloc_scratch per device, resolved on first use
+// Device address of g_noalloc_scratch per device, resolved on the first
+// call in each context. The address belongs to the context the module was
+// loaded into: after cudaDeviceReset (a new primary context, the module
+// loaded again) the next call looks it up again, keyed on the context's
+// unique id (cuCtxGetId), so no call writes through a stale address.
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 double* g_scratch_ptr[kMaxDevices] = {};
+unsigned long long g_scratch_ctx[kMaxDevices] = {};
+
+// The unique id of the calling thread's current context (driver entry
+// points resolved through the runtime: the library links no libcuda).
+cudaError_t current_context_id(unsigned long long* id) {
+    using GetCurrent = CUresult (*)(CUcontext*);
+    using GetId = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    if (!get_current || !get_id) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+        if (e == cudaSuccess) e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+        if (e != cudaSuccess) return e;
+        if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return cudaErrorSymbolNotFound;
+        get_current = reinterpret_cast<GetCurrent>(f1);
+        get_id = reinterpret_cast<GetId>(f2);
+    }
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return cudaErrorDeviceUninitialized;
+    if (get_id(ctx, id) != CUDA_SUCCESS) return cudaErrorContextIsDestroyed;
+    return cudaSuccess;
+}
 
 struct NAGeom {
     int sx, sy, sz;
@@ -126,6 +158,11 @@ int ipic3d_gpu_project_noalloc(const ipic3d_props* props, uint32_t flags, const 
     if (!props || !d_cell_offsets || !d_J) return na_fail(IPIC3D_E_INVALID, "NULL argument");
     for (int a = 0; a < 3; ++a)
         if (props->size[a] <= 0 || !(props->cell_width[a] > 0)) return na_fail(IPIC3D_E_INVALID, "bad grid");
+    // each axis on its own first, so the node count below cannot overflow
+    for (int a = 0; a < 3; ++a)
+        if (props->size[a] >= kNoAllocMaxNodes)
+            return na_fail(IPIC3D_E_CAPACITY,
+                           "ipic3d_gpu_project_noalloc: grid too large for its fixed scratch (at most (32+1)^3 nodes)");
     const int64_t nodes = (props->size[0] + 1) * (props->size[1] + 1) * (props->size[2] + 1);
     if (nodes > kNoAllocMaxNodes)
         return na_fail(IPIC3D_E_CAPACITY,
@@ -133,15 +170,21 @@ int ipic3d_gpu_project_noalloc(const ipic3d_props* props, uint32_t flags, const 
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
         return na_fail(IPIC3D_E_NODEVICE, "no current CUDA device");
+    unsigned long long ctx_id = 0;
+    {
+        const cudaError_t e = current_context_id(&ctx_id);
+        if (e != cudaSuccess) return na_fail(IPIC3D_E_NODEVICE, cudaGetErrorString(e));
+    }
     double* scratch = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_mu);
-        if (!g_scratch_ptr[dev]) {
-            // first call on this device: the device address of the static array
+        if (!g_scratch_ptr[dev] || g_scratch_ctx[dev] != ctx_id) {
+            // first call in this context: the device address of the static array
             void* p = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
             if (e != cudaSuccess) return na_fail(IPIC3D_E_CUDA, cudaGetErrorString(e));
             g_scratch_ptr[dev] = static_cast<double*>(p);
+            g_scratch_ctx[dev] = ctx_id;
         }
         scratch = g_scratch_ptr[dev];
     }

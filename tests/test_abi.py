@@ -117,6 +117,35 @@ def test_tracer_arguments_and_no_gpu():
     assert e.value.status == abi.E_INVALID
 
 
+def test_project_noalloc_rejects_sizes_before_any_device_work():
+    """The allocation-free projection checks the grid against its fixed
+    scratch axis by axis before it multiplies (no overflow for huge sizes)
+    and before it touches a device; the pointers are never dereferenced."""
+    import pytest
+    lib = pkg.library(build_if_missing=True)
+    fake = C.c_void_p(256)
+    buf = C.create_string_buffer(256)
+    for size in ((1 << 21,) * 3, (1 << 62, 1, 1), (40000, 1, 1), (33, 32, 32), (2, 2, 1 << 40)):
+        props = abi.Props.make(size=(1, 1, 1))
+        props.size[0], props.size[1], props.size[2] = size
+        rc = lib.ipic3d_gpu_project_noalloc(C.byref(props), 0, fake, fake, fake, None, None)
+        assert rc == abi.E_CAPACITY, size
+        lib.ipic3d_gpu_last_error(buf, 256)
+        assert b"too large" in buf.value
+    props = abi.Props.make(size=(1, 1, 1))
+    props.size[1] = 0
+    assert lib.ipic3d_gpu_project_noalloc(C.byref(props), 0, fake, fake, fake, None, None) == abi.E_INVALID
+    assert lib.ipic3d_gpu_project_noalloc(None, 0, fake, fake, fake, None, None) == abi.E_INVALID
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    props = abi.Props.make(size=(32, 32, 32))  # fits: refused only for want of a device
+    assert lib.ipic3d_gpu_project_noalloc(C.byref(props), 0, fake, fake, fake, None, None) == abi.E_NODEVICE
+
+
 def test_plain_c_consumer(tmp_path):
     """The header is C99 and the library links from C (the form cgo, JNI or
     N-API bindings use)."""
