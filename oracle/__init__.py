@@ -14,7 +14,19 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_LIB = os.path.join(REF_DIR, "libipic3d_ref.so")
-REFERENCE_ROOT = os.environ.get("IPIC3D_REFERENCE_ROOT", "/root/reference")
+ROOT_RECORD = os.path.join(REF_DIR, "reference_root.txt")
+
+
+def reference_root():
+    """The reference source tree to compile: $IPIC3D_REFERENCE_ROOT, else the
+    tree the last build_reference() used (recorded in oracle/_ref/), else
+    None (no reference sources: the reference-based tests skip)."""
+    root = os.environ.get("IPIC3D_REFERENCE_ROOT")
+    if not root and os.path.exists(ROOT_RECORD):
+        root = open(ROOT_RECORD).read().strip()
+    if root and os.path.isdir(os.path.join(root, "code", "app", "include")):
+        return root
+    return None
 
 
 def build(force=False):
@@ -32,11 +44,15 @@ def build(force=False):
     return LIB
 
 
-def build_reference():
-    """Compiles the reference's sources in place (only where they exist)."""
-    if not os.path.isdir(os.path.join(REFERENCE_ROOT, "code", "app", "include")):
+def build_reference(root=None):
+    """Compiles the reference's sources in place from `root` (default:
+    reference_root()), only where they exist, and records the tree used."""
+    root = root or reference_root()
+    if not root or not os.path.isdir(os.path.join(root, "code", "app", "include")):
         return None
-    subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"), "-j8", "REF=" + REFERENCE_ROOT])
+    subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"), "-j8", "REF=" + root])
+    with open(ROOT_RECORD, "w") as f:
+        f.write(root + "\n")
     return REF_LIB
 
 

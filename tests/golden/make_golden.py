@@ -90,7 +90,7 @@ def trace_line(row):
 def inp_runs():
     res = {}
     for name in ("test", "tiny"):
-        path = os.path.join(oracle.REFERENCE_ROOT, "inputs", name + ".inp").encode()
+        path = os.path.join(oracle.reference_root(), "inputs", name + ".inp").encode()
         props = abi.Props()
         ncyc = C.c_uint64()
         n = C.c_uint64()
@@ -116,7 +116,7 @@ def inp_runs():
             ref.ref_conserved(C.byref(props), abi.vptr(cur), abi.vptr(cur_counts), abi.vptr(field), C.byref(cq))
             trace.append([i, cq.total_momentum, cq.e_energy, cq.b_energy, cq.kinetic_energy])
             cur, cur_counts, _ = ref_simulate(props, cur, cur_counts, 1)
-        ref_lines = open(os.path.join(oracle.REFERENCE_ROOT, "outputs", name + "ConservedQuantities.out")).read()
+        ref_lines = open(os.path.join(oracle.reference_root(), "outputs", name + "ConservedQuantities.out")).read()
         ref_cols = {int(c[0]): c for c in (l.split("\t") for l in ref_lines.strip().splitlines()[1:])}
         for row in trace:  # the file's cycles (its own output cycle): E energy, B energy
             line = trace_line(row).split("\t")

@@ -5,6 +5,7 @@ with the same members (compiled and run on the GPU, compared with the C ABI
 path)."""
 import os
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -13,7 +14,10 @@ from allscale_ipic3d_gb300 import abi, library_path
 
 ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
 CPP = os.path.join(ROOT, "tests", "cpp")
-REFERENCE = os.environ.get("REFERENCE_ROOT", "/root/reference")
+sys.path.insert(0, ROOT)
+import oracle  # noqa: E402  (test infrastructure: where the reference sources are, if anywhere)
+
+REFERENCE = oracle.reference_root() or ""
 
 
 def compile_cpp(src, out, std="c++14", extra=()):

@@ -8,13 +8,14 @@ import pytest
 
 import oracle
 
-HAVE_REF = os.path.isdir(os.path.join(oracle.REFERENCE_ROOT, "code", "app", "include"))
+REFERENCE = oracle.reference_root()
+HAVE_REF = REFERENCE is not None
 
 
 @pytest.mark.reference
 @pytest.mark.skipif(not HAVE_REF, reason="reference sources not present on this machine")
 def test_reference_unit_tests_pass_against_shim():
-    r = subprocess.run(["make", "-s", "-C", os.path.join(oracle.HERE, "ref"), "check", "REF=" + oracle.REFERENCE_ROOT],
+    r = subprocess.run(["make", "-s", "-C", os.path.join(oracle.HERE, "ref"), "check", "REF=" + REFERENCE],
                        capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stderr
     lines = [l for l in r.stdout.splitlines() if l.startswith(("PASS", "FAIL"))]
