@@ -64,6 +64,7 @@ _SIGNATURES = [
     ("ipic3d_gpu_profile_read", C.c_int, [_vp, _vp, C.c_int]),
     ("ipic3d_gpu_get_push_shape", C.c_int, [_vp, _vp]),
     ("ipic3d_gpu_set_push_shape", C.c_int, [_vp, _vp]),
+    ("ipic3d_gpu_set_wait_limit", C.c_int, [_vp, C.c_int64]),
     ("ipic3d_gpu_project_noalloc", C.c_int, [_vp, C.c_uint32, _vp, _vp, _vp, _vp, _vp]),
     ("ipic3d_gpu_aggregate_contributions", C.c_int, [_vp, _vp, _vp, _vp]),
     ("ipic3d_gpu_trace", C.c_int, [_vp, _vp, C.c_uint64, C.c_int32, C.c_int32, C.c_int32, _vp]),
@@ -241,13 +242,22 @@ class Simulation:
         _check(library().ipic3d_gpu_particle_count(self._ctx, C.byref(n)))
         return n.value
 
-    def download_particles(self):
+    def download_particles(self, out=None, ids=True):
         """(particles, cell_counts, ids) grouped by cell; order inside a cell
-        is unspecified."""
+        is unspecified. `out` = (particles, cell_counts): caller-owned host
+        arrays to fill (for example pinned memory); the result is then views
+        of them (particles[:n]) and ids is None unless `ids` is an array."""
+        if out is not None:
+            p, c = out
+            i = ids if isinstance(ids, np.ndarray) else None
+            _check(library().ipic3d_gpu_download_particles(self._ctx, abi.vptr(p), len(p), abi.vptr(c),
+                                                           abi.vptr(i)))
+            n = int(c.sum())
+            return p[:n], c, (i[:n] if i is not None else None)
         n = self.particle_count()
         p = np.zeros(n, PARTICLE_DTYPE)
         c = np.zeros(self.ncells, np.uint64)
-        i = np.zeros(n, np.uint32)
+        i = np.zeros(n, np.uint32) if ids else None
         _check(library().ipic3d_gpu_download_particles(self._ctx, abi.vptr(p), n, abi.vptr(c), abi.vptr(i)))
         return p, c, i
 
@@ -351,6 +361,13 @@ class Simulation:
                           item_cells=cur["item_cells"] if item_cells is None else int(item_cells),
                           blocks_per_sm=cur["blocks_per_sm"] if blocks_per_sm is None else int(blocks_per_sm))
         _check(library().ipic3d_gpu_set_push_shape(self._ctx, C.byref(s)))
+
+    def set_wait_limit(self, polls=None):
+        """Bound of the FP32 push's waits on its shared-memory barriers, in
+        polls of about 20 us (None: the default, about 1 s; 0: every wait
+        gives up at once). A wait that gives up makes the step raise
+        GpuPathError with status E_TIMEOUT."""
+        _check(library().ipic3d_gpu_set_wait_limit(self._ctx, -1 if polls is None else int(polls)))
 
     @property
     def stream(self):

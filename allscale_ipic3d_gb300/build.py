@@ -57,7 +57,9 @@ def build(force=False, verbose=False):
     objdir = os.path.join(LIBDIR, "obj")
     os.makedirs(objdir, exist_ok=True)
     cc = nvcc()
-    common = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-strict-aliasing"] + ARCH
+    # host code: no fused multiply-add either (x86 and Arm hosts round alike)
+    common = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-strict-aliasing",
+              "-Xcompiler", "-ffp-contract=off"] + ARCH
 
     def compile_one(item):
         src, extra = item

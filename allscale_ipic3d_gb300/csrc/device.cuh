@@ -115,6 +115,9 @@ struct PushShape {
     int32_t item;        // a power of two, 32..1024
     int32_t item_cells;  // 0..32 (0: every tile slot by slot)
     int32_t per_sm;      // 1..the blocks that fit on an SM
+    // polls (of ~20 us each) after which a wait on a shared-memory barrier
+    // gives up; < 0: the default bound (about 1 s)
+    int32_t wait_polls = -1;
 };
 constexpr PushShape kDefaultPushShape{256, 32, 2};
 
@@ -131,6 +134,8 @@ struct Push32Const {
     float origin[3];  // domain origin relative to the dipole centre (0,0,0)
     float center[3];  // object centre (planet)
     float inv_sy, inv_sz;  // 1 / cells along y and z (cell index -> coordinates)
+    float k1;         // qom * 0.5 * dt: the Boris factor of a single sub-cycle
+    float a1[3];      // dt / w: the position step of a single sub-cycle (cell widths per velocity unit)
 };
 
 // The push constants of the populations of a PopSet.

@@ -190,7 +190,9 @@ struct ipic3d_ctx {
     int32_t* st_cnt = nullptr;
     int* st_unknown = nullptr;
     int* st_flags = nullptr;            // fused upload: unknown species, cell overflow
-    cudaStream_t copy_stream = nullptr; // host-to-device copies of the chunked upload
+    int64_t* st_dst = nullptr;          // download: output index of each (population, cell)
+    size_t st_dst_cap = 0;
+    cudaStream_t copy_stream = nullptr; // copies of the chunked upload and download
     cudaEvent_t copy_ev = nullptr;
     // second stream of a step: kernels that run beside the push / placement
     cudaStream_t aux_stream = nullptr;
@@ -206,6 +208,7 @@ struct ipic3d_ctx {
     // fixed by ipic3d_gpu_set_push_shape
     PushTuner tuner;
     bool shape_fixed = false;
+    int32_t wait_polls = -1;       // bounded-wait polls of the FP32 push (< 0: default)
     uint64_t tuned_particles = 0;  // particle count the shape was tuned for
     bool tune_timing = false;      // this step is a trial: time the push
     cudaEvent_t tune_ev[2] = {nullptr, nullptr};
@@ -722,67 +725,150 @@ int init_uniform_impl(ipic3d_ctx* ctx, uint64_t n) {
 }
 
 // Downloads every population, adding the pending particles to their cells.
+// The reference's record of a particle of population P in cell c from its
+// GPU state (cell-relative FP32 positions made absolute in FP64 with the
+// pack kernel's formula).
 template <typename T>
-int download_pop(ipic3d_ctx* ctx, const PopStore<T>& P, std::vector<std::vector<ipic3d_particle>>& cells,
-                 std::vector<std::vector<uint32_t>>& cell_ids) {
-    const int64_t nc = ctx->ncells();
-    const size_t cap = (size_t)P.capacity;
-    std::vector<T> hx(cap), hy(cap), hz(cap), hu(cap), hv(cap), hw(cap);
-    std::vector<uint32_t> hid(P.id ? cap : 0);
-    std::vector<int32_t> hcount(nc);
-    uint32_t npend = 0;
-    cudaStream_t st = ctx->stream;
-    CU(cudaMemcpyAsync(hx.data(), P.x, cap * sizeof(T), cudaMemcpyDeviceToHost, st));
-    CU(cudaMemcpyAsync(hy.data(), P.y, cap * sizeof(T), cudaMemcpyDeviceToHost, st));
-    CU(cudaMemcpyAsync(hz.data(), P.z, cap * sizeof(T), cudaMemcpyDeviceToHost, st));
-    CU(cudaMemcpyAsync(hu.data(), P.u, cap * sizeof(T), cudaMemcpyDeviceToHost, st));
-    CU(cudaMemcpyAsync(hv.data(), P.v, cap * sizeof(T), cudaMemcpyDeviceToHost, st));
-    CU(cudaMemcpyAsync(hw.data(), P.w, cap * sizeof(T), cudaMemcpyDeviceToHost, st));
-    if (P.id) CU(cudaMemcpyAsync(hid.data(), P.id, cap * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    CU(cudaMemcpyAsync(hcount.data(), P.count, nc * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-    CU(cudaMemcpyAsync(&npend, P.pending_in_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    CU(cudaStreamSynchronize(st));
-    std::vector<Mover<T>> pend(npend);
-    if (npend) CU(cudaMemcpy(pend.data(), P.pending_in, npend * sizeof(Mover<T>), cudaMemcpyDeviceToHost));
+ipic3d_particle host_record(const ipic3d_ctx* ctx, const PopStore<T>& P, int64_t c, const Mover<T>& m) {
     const ipic3d_props& pr = ctx->props;
-    auto emit = [&](int64_t c, T x, T y, T z, T u, T v, T w, uint32_t id) {
-        ipic3d_particle p;
-        if (std::is_same<T, float>::value) {
-            int64_t cx = c / (pr.size[1] * pr.size[2]), cy = (c / pr.size[2]) % pr.size[1], cz = c % pr.size[2];
-            p.position[0] = (pr.origin[0] + (double)cx * pr.cell_width[0]) + (double)x * pr.cell_width[0];
-            p.position[1] = (pr.origin[1] + (double)cy * pr.cell_width[1]) + (double)y * pr.cell_width[1];
-            p.position[2] = (pr.origin[2] + (double)cz * pr.cell_width[2]) + (double)z * pr.cell_width[2];
-        } else {
-            p.position[0] = (double)x;
-            p.position[1] = (double)y;
-            p.position[2] = (double)z;
-        }
-        p.velocity[0] = (double)u;
-        p.velocity[1] = (double)v;
-        p.velocity[2] = (double)w;
-        p.q = P.q;
-        p.qom = P.qom;
-        cells[c].push_back(p);
-        cell_ids[c].push_back(id);
-    };
-    for (int64_t c = 0; c < nc; ++c)
-        for (int32_t i = 0; i < hcount[c]; ++i) {
-            size_t s = (size_t)(P.h_start[c] + i);
-            emit(c, hx[s], hy[s], hz[s], hu[s], hv[s], hw[s], P.id ? hid[s] : 0u);
-        }
-    for (const auto& m : pend) emit(m.cell, m.x, m.y, m.z, m.u, m.v, m.w, m.id);
-    return IPIC3D_OK;
+    ipic3d_particle p;
+    if (std::is_same<T, float>::value) {
+        const int64_t cx = c / (pr.size[1] * pr.size[2]), cy = (c / pr.size[2]) % pr.size[1], cz = c % pr.size[2];
+        p.position[0] = (pr.origin[0] + (double)cx * pr.cell_width[0]) + (double)m.x * pr.cell_width[0];
+        p.position[1] = (pr.origin[1] + (double)cy * pr.cell_width[1]) + (double)m.y * pr.cell_width[1];
+        p.position[2] = (pr.origin[2] + (double)cz * pr.cell_width[2]) + (double)m.z * pr.cell_width[2];
+    } else {
+        p.position[0] = (double)m.x;
+        p.position[1] = (double)m.y;
+        p.position[2] = (double)m.z;
+    }
+    p.velocity[0] = (double)m.u;
+    p.velocity[1] = (double)m.v;
+    p.velocity[2] = (double)m.w;
+    p.q = P.q;
+    p.qom = P.qom;
+    return p;
 }
 
-int gather_host(ipic3d_ctx* ctx, std::vector<std::vector<ipic3d_particle>>& cells,
-                std::vector<std::vector<uint32_t>>& ids) {
-    cells.assign(ctx->ncells(), {});
-    ids.assign(ctx->ncells(), {});
+// Download through the device. The per-cell output offsets come from the
+// counts and the cells of the particles waiting for a slot (host, small);
+// the AoS records are packed on the device in chunks of cells and each
+// chunk is copied to the host on the copy stream while the next is packed
+// (one cudaMemcpyAsync per chunk and array); the waiting particles (few)
+// are filled in on the host. Order per cell: population 0's particles in
+// slot order, then its waiting particles in list order, then population
+// 1's, and so on. `particles` / `ids` may be NULL (counts only).
+template <typename T>
+int download_device(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, ipic3d_particle* particles, uint64_t capacity,
+                    uint64_t* cell_counts, uint32_t* ids) {
+    const int64_t nc = ctx->ncells();
+    const int npop = (int)pops.size();
+    if (npop > kUploadMaxPops) return fail(IPIC3D_E_CAPACITY, "%d populations: at most %d", npop, kUploadMaxPops);
+    cudaStream_t st = ctx->stream;
+    std::vector<int32_t> cnt((size_t)npop * nc);
+    std::vector<uint32_t> npend(npop, 0);
+    for (int k = 0; k < npop; ++k) {
+        CU(cudaMemcpyAsync(cnt.data() + (size_t)k * nc, pops[k].count, nc * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                           st));
+        CU(cudaMemcpyAsync(&npend[k], pops[k].pending_in_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    }
+    CU(cudaStreamSynchronize(st));
+    std::vector<std::vector<Mover<T>>> pend(npop);
+    std::vector<int32_t> pcell;  // waiting particles per (population, cell), if any
+    for (int k = 0; k < npop; ++k) {
+        if (!npend[k]) continue;
+        pend[k].resize(npend[k]);
+        CU(cudaMemcpyAsync(pend[k].data(), pops[k].pending_in, npend[k] * sizeof(Mover<T>), cudaMemcpyDeviceToHost,
+                           st));
+    }
+    CU(cudaStreamSynchronize(st));
+    for (int k = 0; k < npop; ++k)
+        for (const auto& m : pend[k]) {
+            if (m.cell < 0 || m.cell >= nc) return fail(IPIC3D_E_STATE, "waiting particle in cell %d", m.cell);
+            if (pcell.empty()) pcell.assign((size_t)npop * nc, 0);
+            ++pcell[(size_t)k * nc + m.cell];
+        }
+    std::vector<int64_t> dst((size_t)npop * nc);
+    int64_t n = 0;
+    for (int64_t c = 0; c < nc; ++c) {
+        const int64_t first = n;
+        for (int k = 0; k < npop; ++k) {
+            const size_t i = (size_t)k * nc + c;
+            dst[i] = n;
+            n += cnt[i] + (pcell.empty() ? 0 : pcell[i]);
+        }
+        if (cell_counts) cell_counts[c] = (uint64_t)(n - first);
+    }
+    if ((!particles && !ids) || n == 0) return IPIC3D_OK;
+    if ((uint64_t)n > capacity)
+        return fail(IPIC3D_E_CAPACITY, "output capacity %llu too small", (unsigned long long)capacity);
     int rc;
-    for (auto& P : ctx->p32)
-        if ((rc = download_pop(ctx, P, cells, ids))) return rc;
-    for (auto& P : ctx->p64)
-        if ((rc = download_pop(ctx, P, cells, ids))) return rc;
+    if ((rc = grow(reinterpret_cast<char*&>(ctx->st_parts), ctx->st_parts_cap, (size_t)n * sizeof(ipic3d_particle))))
+        return rc;
+    if (ids && (rc = grow(ctx->st_ids, ctx->st_ids_cap, (size_t)n))) return rc;
+    if ((rc = grow(ctx->st_dst, ctx->st_dst_cap, dst.size()))) return rc;
+    if (!ctx->copy_stream) CU(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    if (!ctx->copy_ev) CU(cudaEventCreateWithFlags(&ctx->copy_ev, cudaEventDisableTiming));
+    CU(cudaMemcpyAsync(ctx->st_dst, dst.data(), dst.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    PackPops<T> P{};
+    P.npop = npop;
+    P.relative = std::is_same<T, float>::value ? 1 : 0;
+    for (int k = 0; k < npop; ++k) {
+        const auto& S = pops[k];
+        P.x[k] = S.x; P.y[k] = S.y; P.z[k] = S.z; P.u[k] = S.u; P.v[k] = S.v; P.w[k] = S.w;
+        P.id[k] = S.id;
+        P.start[k] = S.start;
+        P.count[k] = S.count;
+        P.q[k] = S.q;
+        P.qom[k] = S.qom;
+    }
+    P.dst = ctx->st_dst;
+    UploadGeom g;
+    g.ncells = (int)nc;
+    g.sx = (int)ctx->props.size[0];
+    g.sy = (int)ctx->props.size[1];
+    g.sz = (int)ctx->props.size[2];
+    for (int a = 0; a < 3; ++a) {
+        g.origin[a] = ctx->props.origin[a];
+        g.w[a] = ctx->props.cell_width[a];
+    }
+    // chunks of about 16 MB of records, cut at cell boundaries
+    const int64_t chunk = std::max<int64_t>(1, (int64_t)(16u << 20) / (int64_t)sizeof(ipic3d_particle));
+    cudaStream_t cs = ctx->copy_stream;
+    auto* stage = static_cast<ipic3d_particle*>(ctx->st_parts);
+    int nl = 0;
+    for (int64_t c0 = 0; c0 < nc;) {
+        const int64_t o0 = dst[(size_t)c0];
+        int64_t c1 = c0 + 1;
+        while (c1 < nc && dst[(size_t)c1] - o0 < chunk) ++c1;
+        const int64_t o1 = c1 < nc ? dst[(size_t)c1] : n;
+        nl += launch_pack_cells<T>(P, g, (int)c0, (int)c1, stage, ids ? ctx->st_ids : nullptr, st);
+        if (o1 > o0) {
+            CU(cudaEventRecord(ctx->copy_ev, st));
+            CU(cudaStreamWaitEvent(cs, ctx->copy_ev, 0));
+            if (particles)
+                CU(cudaMemcpyAsync(particles + o0, stage + o0, (size_t)(o1 - o0) * sizeof(ipic3d_particle),
+                                   cudaMemcpyDeviceToHost, cs));
+            if (ids)
+                CU(cudaMemcpyAsync(ids + o0, ctx->st_ids + o0, (size_t)(o1 - o0) * sizeof(uint32_t),
+                                   cudaMemcpyDeviceToHost, cs));
+        }
+        c0 = c1;
+    }
+    if ((rc = check_launch(ctx, nl))) return rc;
+    CU(cudaStreamSynchronize(cs));
+    CU(cudaStreamSynchronize(st));
+    // the waiting particles, into the gaps after each cell's slots
+    for (int k = 0; k < npop; ++k) {
+        if (pend[k].empty()) continue;
+        std::vector<int32_t> rank(nc, 0);
+        for (const auto& m : pend[k]) {
+            const size_t i = (size_t)k * nc + m.cell;
+            const int64_t o = dst[i] + cnt[i] + rank[m.cell]++;
+            if (particles) particles[o] = host_record(ctx, pops[k], m.cell, m);
+            if (ids) ids[o] = m.id;
+        }
+    }
     return IPIC3D_OK;
 }
 
@@ -988,7 +1074,8 @@ int move_impl(ipic3d_ctx* ctx, bool deposit, bool next_solve = false, bool clear
     }
     const auto s32 = pop_sets(ctx->p32);
     const auto s64 = pop_sets(ctx->p64);
-    const PushShape shp = ctx->tuner.next();
+    PushShape shp = ctx->tuner.next();
+    shp.wait_polls = ctx->wait_polls;
     ph_begin(ctx, IPIC3D_PHASE_PUSH);
     if (ctx->tune_timing) CU(cudaEventRecord(ctx->tune_ev[0], st));
     for (auto& S : s32) n += launch_push<float>(g, S, 0, shp, st);
@@ -1251,6 +1338,7 @@ int destroy_impl(ipic3d_ctx* ctx) {
     dfree(ctx->st_cnt);
     dfree(ctx->st_unknown);
     dfree(ctx->st_flags);
+    dfree(ctx->st_dst);
     if (ctx->copy_ev) cudaEventDestroy(ctx->copy_ev);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     for (auto& e : ctx->aux_ev)
@@ -1463,23 +1551,8 @@ int ipic3d_gpu_download_particles(ipic3d_ctx* ctx, ipic3d_particle* particles, u
                                   uint64_t* cell_counts, uint32_t* ids) {
     int rc = check_ctx(ctx);
     if (rc) return rc;
-    std::vector<std::vector<ipic3d_particle>> cells;
-    std::vector<std::vector<uint32_t>> cid;
-    if ((rc = gather_host(ctx, cells, cid))) return rc;
-    uint64_t k = 0;
-    for (int64_t c = 0; c < ctx->ncells(); ++c) {
-        if (cell_counts) cell_counts[c] = cells[c].size();
-        for (size_t i = 0; i < cells[c].size(); ++i, ++k) {
-            if (k >= capacity) {
-                if (particles || ids) return fail(IPIC3D_E_CAPACITY, "output capacity %llu too small",
-                                                  (unsigned long long)capacity);
-                continue;
-            }
-            if (particles) particles[k] = cells[c][i];
-            if (ids) ids[k] = cid[c][i];
-        }
-    }
-    return IPIC3D_OK;
+    if (ctx->fp32) return download_device(ctx, ctx->p32, particles, capacity, cell_counts, ids);
+    return download_device(ctx, ctx->p64, particles, capacity, cell_counts, ids);
 }
 
 int ipic3d_gpu_upload_fields(ipic3d_ctx* ctx, const double* field, const double* bcfield, const double* density) {
@@ -1734,6 +1807,14 @@ int ipic3d_gpu_set_push_shape(ipic3d_ctx* ctx, const ipic3d_push_shape* shape) {
     } else {
         ctx->tuner.fix(kDefaultPushShape);
     }
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_set_wait_limit(ipic3d_ctx* ctx, int64_t polls) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    drop_graph(ctx);  // captured with the previous bound
+    ctx->wait_polls = polls < 0 ? -1 : (int32_t)std::min<int64_t>(polls, INT32_MAX);
     return IPIC3D_OK;
 }
 

@@ -161,6 +161,10 @@ Push32Const push32_const(const Geom& g, const Pop<float>& P) {
     }
     pc.inv_sy = 1.0f / (float)g.sy;
     pc.inv_sz = 1.0f / (float)g.sz;
+    // the one-sub-cycle constants, rounded as the kernel's general path
+    // rounds them for ns = 1 (dts = dt): qom * 0.5f * dt and dt * inv_w
+    pc.k1 = pc.qom * 0.5f * pc.dt;
+    for (int a = 0; a < 3; ++a) pc.a1[a] = pc.dt * pc.inv_w[a];
     return pc;
 }
 

@@ -1,7 +1,8 @@
-// FP32 particle physics shared by the FP32 kernels, and the kernels that use
-// it one particle at a time: particles waiting for a slot (k_push_pending32)
-// and the per-cell field polynomial (k_cell_coef / k_cell_coef32). The bulk
-// push is push32_pipe.cuh.
+// FP32 particle physics shared by the FP32 kernels -- the bulk push
+// (push32_pipe.cuh) and the particles waiting for a slot (k_push_pending32)
+// run the same functions, so a particle's arithmetic does not depend on the
+// path it takes -- and the per-cell field polynomial (k_cell_coef /
+// k_cell_coef32).
 //   * fields: per-cell trilinear polynomial f = c0 + c1 x + c2 y + c3 z +
 //     c4 xy + c5 xz + c6 yz + c7 xyz of every E and B component (the
 //     expansion of trilinearInterpolationF2P, cell.h:867-885, with node
@@ -15,116 +16,253 @@
 
 namespace ipg {
 
-// E (and B) at cell-relative r from the cell's coefficients: component q
-// (Ex, Ey, Ez, Bx, By, Bz) owns coef[q * 8 + m], m = 1, x, y, z, xy, xz, yz,
-// xyz: two float4 per component, evaluated one component at a time.
-__device__ __forceinline__ void eval_fields(const float* __restrict__ coef, float x, float y, float z, float (&f)[6]) {
+// What the push needs to know about a particle's cell (four registers).
+struct CellInfo {
+    float ox, oy, oz;  // cell origin, relative to the dipole centre (0, 0, 0)
+    int flags;         // kCell* bits
+};
+enum : int {
+    kCellNear = 1,    // the planet test can remove a particle that stays in the cell
+    kCellEdge = 2,    // a face of the cell lies on a reflecting or open domain face
+    kCellLoX = 4,     // bits 2..4: the cell is the first along x, y, z; bits 5..7: the last
+    kCellHiX = 32,
+};
+
+// Cell coordinates of a cell index (no 64-bit division for the sizes the
+// push handles).
+__device__ __forceinline__ int3 cell_xyz(const Geom& g, const Push32Const& pc, int cell) {
+    int3 c;
+    if (g.ncells < (1 << 24) && g.sy < 4096 && g.sz < 4096) {
+        const int t = fast_div(cell, g.sz, pc.inv_sz);
+        c.z = cell - t * g.sz;
+        c.x = fast_div(t, g.sy, pc.inv_sy);
+        c.y = t - c.x * g.sy;
+    } else {
+        cell_coords(g, cell, c.x, c.y, c.z);
+    }
+    return c;
+}
+
+__device__ __forceinline__ CellInfo cell_info(const Geom& g, const Push32Const& pc, int cell) {
+    const int3 x = cell_xyz(g, pc, cell);
+    CellInfo c;
+    c.ox = fmaf((float)x.x, pc.w[0], pc.origin[0]);
+    c.oy = fmaf((float)x.y, pc.w[1], pc.origin[1]);
+    c.oz = fmaf((float)x.z, pc.w[2], pc.origin[2]);
+    const int pos[3] = {x.x, x.y, x.z};
+    const int size[3] = {g.sx, g.sy, g.sz};
+    int f = 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (pos[a] == 0 && g.bc_lo[a] != 1) f |= kCellLoX << a;
+        if (pos[a] == size[a] - 1 && g.bc_hi[a] != 1) f |= kCellHiX << a;
+    }
+    if (f) f |= kCellEdge;
+    // squared distance of the closed cell box from the planet centre against
+    // the planet radius plus 1/64 of the widest cell side: a particle that
+    // stays in a cell that is not near lies outside the planet whatever the
+    // rounding of the test (cell.h:1123-1128)
+    const float lo[3] = {c.ox - pc.center[0], c.oy - pc.center[1], c.oz - pc.center[2]};
+    float d2 = 0.f, wmax = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float hi = lo[a] + pc.w[a];
+        const float t = lo[a] > 0.f ? lo[a] : (hi < 0.f ? -hi : 0.f);
+        d2 = fmaf(t, t, d2);
+        wmax = fmaxf(wmax, pc.w[a]);
+    }
+    const float r = sqrtf(pc.planet_r2) + wmax * (1.f / 64.f);
+    if (d2 <= r * r) f |= kCellNear;
+    c.flags = f;
+    return c;
+}
+
+// The CellInfo of lane `src` (warp-wide).
+__device__ __forceinline__ CellInfo shfl_cell_info(const CellInfo& c, int src) {
+    CellInfo r;
+    r.ox = __shfl_sync(0xffffffffu, c.ox, src);
+    r.oy = __shfl_sync(0xffffffffu, c.oy, src);
+    r.oz = __shfl_sync(0xffffffffu, c.oz, src);
+    r.flags = __shfl_sync(0xffffffffu, c.flags, src);
+    return r;
+}
+
+// One component of the cell's trilinear field polynomial at (x, y, z):
+// lo = (c0, cx, cy, cz), hi = (cxy, cxz, cyz, cxyz), seven FMAs.
+__device__ __forceinline__ float poly32(const float4& lo, const float4& hi, float x, float y, float z) {
+    const float a = fmaf(y, hi.w, hi.y);  // x z terms
+    float b = fmaf(y, hi.x, lo.y);        // x terms
+    b = fmaf(z, a, b);
+    const float gz = fmaf(z, hi.z, lo.z);  // y terms
+    float r = fmaf(y, gz, lo.x);
+    r = fmaf(z, lo.w, r);
+    return fmaf(x, b, r);
+}
+
+// E and B of kN particles of one cell from the cell's polynomial
+// coefficients (kSmem: staged in shared memory; else read from global
+// memory): each 16-byte coefficient load serves all kN particles.
+template <bool kSmem, int kN>
+__device__ __forceinline__ void fields_n(const float* __restrict__ coef, const PState<float> (&p)[kN],
+                                         float (&E)[kN][6]) {
     const float4* c4 = reinterpret_cast<const float4*>(coef);
 #pragma unroll
     for (int q = 0; q < 6; ++q) {
-        const float4 lo = __ldg(c4 + 2 * q), hi = __ldg(c4 + 2 * q + 1);
-        // lo = (c0, cx, cy, cz), hi = (cxy, cxz, cyz, cxyz)
-        const float a = fmaf(y, hi.w, hi.y);     // x z terms
-        float b = fmaf(y, hi.x, lo.y);           // x terms
-        b = fmaf(z, a, b);
-        const float gz = fmaf(z, hi.z, lo.z);    // y terms
-        float r = fmaf(y, gz, lo.x);
-        r = fmaf(z, lo.w, r);
-        f[q] = fmaf(x, b, r);
+        const float4 lo = kSmem ? c4[2 * q] : __ldg(c4 + 2 * q);
+        const float4 hi = kSmem ? c4[2 * q + 1] : __ldg(c4 + 2 * q + 1);
+#pragma unroll
+        for (int i = 0; i < kN; ++i) E[i][q] = poly32(lo, hi, p[i].x, p[i].y, p[i].z);
+    }
+}
+template <bool kSmem>
+__device__ __forceinline__ void fields_one(const float* __restrict__ coef, const PState<float>& a, float (&E)[6]) {
+    const float4* c4 = reinterpret_cast<const float4*>(coef);
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        const float4 lo = kSmem ? c4[2 * q] : __ldg(c4 + 2 * q);
+        const float4 hi = kSmem ? c4[2 * q + 1] : __ldg(c4 + 2 * q + 1);
+        E[q] = poly32(lo, hi, a.x, a.y, a.z);
     }
 }
 
-// mover + export of one particle (FP32, cell-relative); same outcomes as
-// step_particle(..., PState<float>&, ...).
-__device__ __forceinline__ int step32(const Geom& g, const Push32Const& pc, const float* __restrict__ coef, int cx,
-                                      int cy, int cz, float ox, float oy, float oz, PState<float>& p, int& dest) {
+// The analytic dipole (cell.h:939-945) added to B: B += (3xz, 3yz,
+// 2z^2 - x^2 - y^2) mft / |r|^5, |r|^-5 from one reciprocal square root.
+__device__ __forceinline__ void add_dipole(const Push32Const& pc, const CellInfo& ci, const PState<float>& p,
+                                           float (&E)[6]) {
+    const float X = fmaf(p.x, pc.w[0], ci.ox), Y = fmaf(p.y, pc.w[1], ci.oy), Z = fmaf(p.z, pc.w[2], ci.oz);
+    const float r2 = fmaf(X, X, fmaf(Y, Y, Z * Z));
+    const float ir = rsqrtf(r2), ir2 = ir * ir;
+    const float fac1 = pc.mft * (ir2 * ir2 * ir);
+    E[3] = fmaf(3.f * X * Z, fac1, E[3]);
+    E[4] = fmaf(3.f * Y * Z, fac1, E[4]);
+    E[5] = fmaf(fmaf(2.f * Z, Z, -fmaf(X, X, Y * Y)), fac1, E[5]);
+}
+
+// dt / dt_sub of cell.h:947-952: K |B|^2 with K = k_sub of the species
+__device__ __forceinline__ float sub_ratio(float k_sub, const float (&E)[6]) {
+    return k_sub * fmaf(E[3], E[3], fmaf(E[4], E[4], E[5] * E[5]));
+}
+
+// `ns` Boris sub-cycles (particle.h:24-49) with k = q/m dts / 2 and
+// a = dts / w (positions in cell widths): t = k B, s = 2 t / (1 + |t|^2),
+// v- = v + k E, v' = v- + v- x t, v+ = v- + v' x s, v = v+ + k E,
+// x += v dts. The cross products are fused multiply-adds; the rotation
+// factor 2 / (1 + |t|^2) is the hardware reciprocal (relative error ~2^-22:
+// |v| changes by that times |t|^2 per rotation, far below the FP32 path's
+// stated error).
+template <int kFixedNs>
+__device__ __forceinline__ void boris32(float k, float ax, float ay, float az, const float (&E)[6], PState<float>& p,
+                                        int ns = kFixedNs) {
+    const float tx = k * E[3], ty = k * E[4], tz = k * E[5];
+    const float den = fmaf(tx, tx, fmaf(ty, ty, fmaf(tz, tz, 1.f)));
+    const float f = __fdividef(2.f, den);
+    const float sx = tx * f, sy = ty * f, sz = tz * f;
+    // k E as separate roundings: the adds below must not fuse with them in
+    // one kernel and not in another (the batched and single-universe
+    // kernels give the same particles bit for bit)
+    const float kex = __fmul_rn(k, E[0]), key = __fmul_rn(k, E[1]), kez = __fmul_rn(k, E[2]);
+    int s = 0;
+    do {
+        const float mx = p.u + kex, my = p.v + key, mz = p.w + kez;
+        const float qx = fmaf(my, tz, fmaf(-mz, ty, mx));
+        const float qy = fmaf(mz, tx, fmaf(-mx, tz, my));
+        const float qz = fmaf(mx, ty, fmaf(-my, tx, mz));
+        p.u = fmaf(qy, sz, fmaf(-qz, sy, mx)) + kex;
+        p.v = fmaf(qz, sx, fmaf(-qx, sz, my)) + key;
+        p.w = fmaf(qx, sy, fmaf(-qy, sx, mz)) + kez;
+        p.x = fmaf(p.u, ax, p.x);
+        p.y = fmaf(p.v, ay, p.y);
+        p.z = fmaf(p.w, az, p.z);
+    } while (kFixedNs == 0 && ++s < ns);
+}
+
+// The reference's sub-cycling rule (cell.h:947-952): ns = min(int(ratio) +
+// 1, 100) Boris steps of dt / ns; a quotient beyond the int range (or NaN)
+// leaves the particle unmoved, as the reference's x86 conversion does. For
+// ns = 1 the constants equal the species' one-step constants (k1, a1) bit
+// for bit, whichever path a particle takes.
+__device__ __forceinline__ void boris_sub(const Push32Const& pc, const Push32Const& sp, float ratio,
+                                          const float (&E)[6], PState<float>& p) {
+    if (!(ratio < 2147483647.f)) return;
+    int ns = (int)ratio + 1;
+    ns = ns < 100 ? ns : 100;
+    const float dts = ns == 1 ? pc.dt : __fdividef(pc.dt, (float)ns);
+    boris32<0>(sp.qom * 0.5f * dts, dts * pc.inv_w[0], dts * pc.inv_w[1], dts * pc.inv_w[2], E, p, ns);
+}
+
+// Export of one moved particle (cell.h:1093-1146) in cell-relative
+// coordinates: the walls of reflecting / open domain faces (cells on such a
+// face only), the planet (cells near it, and every particle that left its
+// cell), then the move to a neighbour: kStay, kDrop, or kMove with the move
+// in `dir` as (dx + 1) | (dy + 1) << 2 | (dz + 1) << 4 and the position made
+// relative to the destination cell. NaN coordinates stay (no axis moves).
+__device__ __forceinline__ int export32(const Geom& g, const Push32Const& pc, const CellInfo& ci, PState<float>& p,
+                                        int& dir) {
+    if (ci.flags & kCellEdge) {
+        float* R[3] = {&p.x, &p.y, &p.z};
+        bool invert = false, drop = false;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            if ((ci.flags & (kCellLoX << a)) && *R[a] < 0.f) {  // a reflecting / open low face
+                if (g.bc_lo[a] == 0) { invert = true; *R[a] += 0.5f; }
+                else if (g.bc_lo[a] == 2) drop = true;
+            } else if ((ci.flags & (kCellHiX << a)) && *R[a] > 1.f) {
+                if (g.bc_hi[a] == 0) { invert = true; *R[a] -= 0.5f; }
+                else if (g.bc_hi[a] == 2) drop = true;
+            }
+        }
+        if (invert) { p.u = -p.u; p.v = -p.v; p.w = -p.w; }
+        if (drop) return kDrop;
+    }
+    const bool in = p.x >= 0.f && p.x <= 1.f && p.y >= 0.f && p.y <= 1.f && p.z >= 0.f && p.z <= 1.f;
+    if ((ci.flags & kCellNear) || !in) {
+        const float dx = fmaf(p.x, pc.w[0], ci.ox - pc.center[0]);
+        const float dy = fmaf(p.y, pc.w[1], ci.oy - pc.center[1]);
+        const float dz = fmaf(p.z, pc.w[2], ci.oz - pc.center[2]);
+        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= pc.planet_r2) return kDrop;  // cell.h:1123-1128
+    }
+    if (in) return kStay;
+    const float fx = p.x < 0.f ? -1.f : (p.x > 1.f ? 1.f : 0.f);
+    const float fy = p.y < 0.f ? -1.f : (p.y > 1.f ? 1.f : 0.f);
+    const float fz = p.z < 0.f ? -1.f : (p.z > 1.f ? 1.f : 0.f);
+    p.x -= fx;
+    p.y -= fy;
+    p.z -= fz;
+    if (fx == 0.f && fy == 0.f && fz == 0.f) return kStay;
+    dir = ((int)fx + 1) | (((int)fy + 1) << 2) | (((int)fz + 1) << 4);
+    return kMove;
+}
+
+// Mover + export of one particle: fields, sub-cycled Boris, export.
+template <bool kSmemCoef, bool kGather, bool kDipole>
+__device__ __forceinline__ int step32f(const Geom& g, const Push32Const& pc, const Push32Const& sp,
+                                       const float* __restrict__ coef, const CellInfo& ci, PState<float>& p,
+                                       int& dir) {
     float E[6];
-    if (g.mover == 1) {
-        eval_fields(coef, p.x, p.y, p.z, E);
+    if (kGather) {
+        fields_one<kSmemCoef>(coef, p, E);
     } else {
 #pragma unroll
         for (int q = 0; q < 6; ++q) E[q] = 0.f;
     }
-    if (g.mover != 1 || (g.flags & 4u)) {
-        const float X = fmaf(p.x, pc.w[0], ox), Y = fmaf(p.y, pc.w[1], oy), Z = fmaf(p.z, pc.w[2], oz);
-        const float r2 = fmaf(X, X, fmaf(Y, Y, Z * Z));
-        const float ir = rsqrtf(r2), ir2 = ir * ir;
-        const float fac1 = pc.mft * (ir2 * ir2 * ir);
-        E[3] = fmaf(3.f * X * Z, fac1, E[3]);
-        E[4] = fmaf(3.f * Y * Z, fac1, E[4]);
-        E[5] = fmaf(fmaf(2.f * Z, Z, -fmaf(X, X, Y * Y)), fac1, E[5]);
+    if (kDipole) add_dipole(pc, ci, p, E);
+    const float ratio = sub_ratio(sp.k_sub, E);
+    if (ratio < 1.f)
+        boris32<1>(sp.k1, pc.a1[0], pc.a1[1], pc.a1[2], E, p);
+    else
+        boris_sub(pc, sp, ratio, E, p);
+    return export32(g, pc, ci, p, dir);
+}
+
+// Mover + export of one particle with the policy read at run time (the
+// particles that waited for a slot): the same arithmetic as the bulk push.
+__device__ __forceinline__ int step32_any(const Geom& g, const Push32Const& pc, const float* __restrict__ coef,
+                                          const CellInfo& ci, PState<float>& p, int& dir) {
+    if (g.mover == 1) {
+        if (g.flags & 4u) return step32f<false, true, true>(g, pc, pc, coef, ci, p, dir);
+        return step32f<false, true, false>(g, pc, pc, coef, ci, p, dir);
     }
-    const float bmag = fmaf(E[3], E[3], fmaf(E[4], E[4], E[5] * E[5]));
-    const float ratio = pc.k_sub * bmag;
-    int ns = 0;
-    if (ratio >= 0.f && ratio < 2147483647.f) {
-        ns = (int)ratio + 1;
-        ns = ns < 100 ? ns : 100;
-    }
-    if (ns > 0) {
-        const float dts = __fdividef(pc.dt, (float)ns);
-        const float k = pc.qom * 0.5f * dts;
-        const float tx = k * E[3], ty = k * E[4], tz = k * E[5];
-        // the rotation factor 2 / (1 + |t|^2) keeps |v| through the rotation:
-        // correctly rounded reciprocal here
-        const float inv = __frcp_rn(fmaf(tx, tx, fmaf(ty, ty, fmaf(tz, tz, 1.f))));
-        const float sx = 2.f * tx * inv, sy = 2.f * ty * inv, sz = 2.f * tz * inv;
-        const float kex = k * E[0], key = k * E[1], kez = k * E[2];
-        const float ax = dts * pc.inv_w[0], ay = dts * pc.inv_w[1], az = dts * pc.inv_w[2];
-        for (int s = 0; s < ns; ++s) {
-            const float mx = p.u + kex, my = p.v + key, mz = p.w + kez;
-            const float px = mx + (my * tz - mz * ty);
-            const float py = my + (mz * tx - mx * tz);
-            const float pz = mz + (mx * ty - my * tx);
-            p.u = mx + (py * sz - pz * sy) + kex;
-            p.v = my + (pz * sx - px * sz) + key;
-            p.w = mz + (px * sy - py * sx) + kez;
-            p.x = fmaf(p.u, ax, p.x);
-            p.y = fmaf(p.v, ay, p.y);
-            p.z = fmaf(p.w, az, p.z);
-        }
-    }
-    // export (cell.h:1093-1146) in cell-relative coordinates
-    const int pos[3] = {cx, cy, cz};
-    const int size[3] = {g.sx, g.sy, g.sz};
-    float R[3] = {p.x, p.y, p.z};
-    bool invert = false, drop = false;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        if (pos[a] == 0 && R[a] < 0.f) {
-            if (g.bc_lo[a] == 0) { invert = true; R[a] += 0.5f; }
-            else if (g.bc_lo[a] == 2) drop = true;
-        } else if (pos[a] == size[a] - 1 && R[a] > 1.f) {
-            if (g.bc_hi[a] == 0) { invert = true; R[a] -= 0.5f; }
-            else if (g.bc_hi[a] == 2) drop = true;
-        }
-    }
-    if (invert) { p.u = -p.u; p.v = -p.v; p.w = -p.w; }
-    if (drop) return kDrop;
-    {
-        const float dx = fmaf(R[0], pc.w[0], ox - pc.center[0]);
-        const float dy = fmaf(R[1], pc.w[1], oy - pc.center[1]);
-        const float dz = fmaf(R[2], pc.w[2], oz - pc.center[2]);
-        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= pc.planet_r2) return kDrop;  // cell.h:1123-1128
-    }
-    int d[3];
-    bool out = false;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        d[a] = R[a] < 0.f ? -1 : (R[a] > 1.f ? 1 : 0);
-        out |= d[a] != 0;
-        R[a] -= (float)d[a];
-    }
-    p.x = R[0]; p.y = R[1]; p.z = R[2];
-    if (!out) return kStay;
-    int n[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        int t = pos[a] + d[a];
-        n[a] = t < 0 ? t + size[a] : (t >= size[a] ? t - size[a] : t);
-    }
-    dest = cell_id(g, n[0], n[1], n[2]);
-    return kMove;
+    return step32f<false, false, true>(g, pc, pc, coef, ci, p, dir);
 }
 
 // Pending particles (no slot last step) with the same physics; threads
@@ -135,13 +273,18 @@ __device__ __forceinline__ void push_pending32_body(const Geom& g, const Pop<flo
     for (uint32_t i = t0; i < n; i += stride) {
         Mover<float> m = P.pending_in[i];
         PState<float> p = {m.x, m.y, m.z, m.u, m.v, m.w};
-        int cx, cy, cz;
-        cell_coords(g, m.cell, cx, cy, cz);
-        const float ox = fmaf((float)cx, pc.w[0], pc.origin[0]);
-        const float oy = fmaf((float)cy, pc.w[1], pc.origin[1]);
-        const float oz = fmaf((float)cz, pc.w[2], pc.origin[2]);
+        const CellInfo ci = cell_info(g, pc, m.cell);
+        int dir = 0;
+        const int outcome = step32_any(g, pc, g.cellcoef + (size_t)m.cell * 48, ci, p, dir);
         int dest = m.cell;
-        const int outcome = step32(g, pc, g.cellcoef + (size_t)m.cell * 48, cx, cy, cz, ox, oy, oz, p, dest);
+        if (outcome == kMove) {
+            const int3 c = cell_xyz(g, pc, m.cell);
+            int n[3] = {c.x + (dir & 3) - 1, c.y + ((dir >> 2) & 3) - 1, c.z + ((dir >> 4) & 3) - 1};
+            const int size[3] = {g.sx, g.sy, g.sz};
+#pragma unroll
+            for (int a = 0; a < 3; ++a) n[a] = n[a] < 0 ? n[a] + size[a] : (n[a] >= size[a] ? n[a] - size[a] : n[a]);
+            dest = cell_id(g, n[0], n[1], n[2]);
+        }
         if (outcome == kDrop) {
             atomicAdd(&P.ctr->removed, 1u);
             continue;

@@ -36,9 +36,11 @@
 // moments keep the FP32 sums small, so the butterflies' cancellation loses
 // no more than the sums' own rounding.
 //
-// Every wait on an mbarrier is bounded (kMaxPolls): on expiry the CTA
-// records a timeout in the population's counters, drains its own copies and
-// returns; the host turns the count into IPIC3D_E_TIMEOUT.
+// Every wait on an mbarrier is bounded (PushShape::wait_polls polls, by
+// default kMaxPolls: about 1 s): on expiry the CTA records a timeout in the
+// population's counters, drains its own copies in flight (with the default
+// bound: those copies are real and complete) and returns; the host turns the
+// count into IPIC3D_E_TIMEOUT.
 #pragma once
 
 #include <cstddef>
@@ -75,11 +77,12 @@ __device__ __forceinline__ uint32_t mbar_try_wait(uint64_t* bar, uint32_t parity
         : "memory");
     return ok;
 }
-// Polls until the phase completes: false after kMaxPolls polls (about 1 s)
-// or as soon as *abort is set.
+// Polls until the phase completes: false after `polls` polls (the default
+// kMaxPolls: about 1 s) or as soon as *abort is set.
 constexpr uint32_t kMaxPolls = 1000000000u / kPollNs;
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const volatile int* abort) {
-    for (uint32_t it = 0; it < kMaxPolls; ++it) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const volatile int* abort,
+                                          uint32_t polls = kMaxPolls) {
+    for (uint32_t it = 0; it < polls; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
         if (*abort) break;
     }
@@ -120,6 +123,8 @@ constexpr int kSlotWarps = kTileSlots / 128;        // slot mode: 128-slot slice
 // item mode (tiles of at most PushShape::item_cells cells, work items of
 // PushShape::item particles): the cells' field coefficients are staged
 constexpr int kItemMaxCells = 32;
+// particles per lane and warp step of the item mode's move pass
+constexpr int kItemPer = 1;
 
 // Every member is a bulk-copy destination: 16-byte aligned offsets.
 struct __align__(16) PipeStage {
@@ -197,29 +202,7 @@ __device__ __forceinline__ void issue_tile(const Pop<float>& P, const float* coe
     if (coef_bytes) bulk_load(st.coef, coef + (size_t)desc.x * 48, coef_bytes, bar);
 }
 
-// 16-byte load from shared memory (p is a generic address of shared memory).
-__device__ __forceinline__ float4 ld_shared_f4(const float* p) {
-    float4 v;
-    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
-                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
-                 : "r"(smem_u32(p)));
-    return v;
-}
-
-// eval_fields (push32.cuh) with the coefficients in shared memory.
-__device__ __forceinline__ void eval_fields_smem(const float* coef, float x, float y, float z, float (&f)[6]) {
-#pragma unroll
-    for (int q = 0; q < 6; ++q) {
-        const float4 lo = ld_shared_f4(coef + 8 * q), hi = ld_shared_f4(coef + 8 * q + 4);
-        const float a = fmaf(y, hi.w, hi.y);
-        float b = fmaf(y, hi.x, lo.y);
-        b = fmaf(z, a, b);
-        const float gz = fmaf(z, hi.z, lo.z);
-        float r = fmaf(y, gz, lo.x);
-        r = fmaf(z, lo.w, r);
-        f[q] = fmaf(x, b, r);
-    }
-}
+// ---- per-particle physics --------------------------------------------------------
 
 // Compile-time policy of one pipelined push launch (template bit set).
 enum : int {
@@ -229,130 +212,23 @@ enum : int {
     kPipeDeposit = 8,  // cloud-in-cell deposit of J and rho
 };
 
-struct CellInfo {
-    int cx, cy, cz;
-    float ox, oy, oz;
-    bool edge;  // a face of this cell lies on a reflecting or open domain face
-};
-
-__device__ __forceinline__ CellInfo cell_info(const Geom& g, const Push32Const& pc, int cell) {
-    CellInfo c;
-    if (g.ncells < (1 << 24) && g.sy < 4096 && g.sz < 4096) {
-        const int t = fast_div(cell, g.sz, pc.inv_sz);
-        c.cz = cell - t * g.sz;
-        c.cx = fast_div(t, g.sy, pc.inv_sy);
-        c.cy = t - c.cx * g.sy;
-    } else {
-        cell_coords(g, cell, c.cx, c.cy, c.cz);
-    }
-    c.ox = fmaf((float)c.cx, pc.w[0], pc.origin[0]);
-    c.oy = fmaf((float)c.cy, pc.w[1], pc.origin[1]);
-    c.oz = fmaf((float)c.cz, pc.w[2], pc.origin[2]);
-    c.edge = (c.cx == 0 && g.bc_lo[0] != 1) || (c.cx == g.sx - 1 && g.bc_hi[0] != 1) ||
-             (c.cy == 0 && g.bc_lo[1] != 1) || (c.cy == g.sy - 1 && g.bc_hi[1] != 1) ||
-             (c.cz == 0 && g.bc_lo[2] != 1) || (c.cz == g.sz - 1 && g.bc_hi[2] != 1);
-    return c;
+__device__ __forceinline__ PState<float> load_slot(const PipeStage& st, int sl) {
+    PState<float> p;
+    p.x = st.s[0][sl]; p.y = st.s[1][sl]; p.z = st.s[2][sl];
+    p.u = st.s[3][sl]; p.v = st.s[4][sl]; p.w = st.s[5][sl];
+    return p;
 }
-
-// Mover + export of one particle (FP32, cell-relative), the physics of
-// step32 (push32.cuh) specialised at compile time: kGather / kDipole select
-// the field terms, kSmemCoef says where the coefficients are. The wall logic
-// runs only for cells on a reflecting or open face; the rotation factor
-// 2 / (1 + |t|^2) comes from the hardware reciprocal plus one Newton-Raphson
-// step (r + r (1 - d r)). A leaver's move is returned in `dir` as
-// (dx + 1) | (dy + 1) << 2 | (dz + 1) << 4. Only qom and k_sub are read
-// from `sp` (the species' constants); the rest, which every population of
-// a launch shares, from `pc`.
-template <bool kSmemCoef, bool kGather, bool kDipole>
-__device__ __forceinline__ int step32f(const Geom& g, const Push32Const& pc, const Push32Const& sp,
-                                       const float* __restrict__ coef, const CellInfo& ci, PState<float>& p,
-                                       int& dir) {
-    float E[6];
-    if (kGather) {
-        if (kSmemCoef)
-            eval_fields_smem(coef, p.x, p.y, p.z, E);
-        else
-            eval_fields(coef, p.x, p.y, p.z, E);
-    } else {
-#pragma unroll
-        for (int q = 0; q < 6; ++q) E[q] = 0.f;
-    }
-    if (kDipole) {
-        const float X = fmaf(p.x, pc.w[0], ci.ox), Y = fmaf(p.y, pc.w[1], ci.oy), Z = fmaf(p.z, pc.w[2], ci.oz);
-        const float r2 = fmaf(X, X, fmaf(Y, Y, Z * Z));
-        const float ir = rsqrtf(r2), ir2 = ir * ir;
-        const float fac1 = pc.mft * (ir2 * ir2 * ir);
-        E[3] = fmaf(3.f * X * Z, fac1, E[3]);
-        E[4] = fmaf(3.f * Y * Z, fac1, E[4]);
-        E[5] = fmaf(fmaf(2.f * Z, Z, -fmaf(X, X, Y * Y)), fac1, E[5]);
-    }
-    const float bmag = fmaf(E[3], E[3], fmaf(E[4], E[4], E[5] * E[5]));
-    const float ratio = sp.k_sub * bmag;  // >= 0 or NaN
-    // cell.h:947-952; a quotient beyond the int range (or NaN) leaves the
-    // particle unmoved, as the reference's x86 conversion does
-    int ns = 0;
-    if (ratio < 2147483647.f) {
-        ns = (int)ratio + 1;
-        ns = ns < 100 ? ns : 100;
-    }
-    if (ns > 0) {
-        const float dts = ns == 1 ? pc.dt : __fdividef(pc.dt, (float)ns);
-        const float k = sp.qom * 0.5f * dts;
-        const float tx = k * E[3], ty = k * E[4], tz = k * E[5];
-        const float den = fmaf(tx, tx, fmaf(ty, ty, fmaf(tz, tz, 1.f)));
-        float inv = __fdividef(1.f, den);
-        inv = fmaf(inv, fmaf(-den, inv, 1.f), inv);
-        const float inv2 = 2.f * inv;
-        const float sx = tx * inv2, sy = ty * inv2, sz = tz * inv2;
-        const float kex = k * E[0], key = k * E[1], kez = k * E[2];
-        const float ax = dts * pc.inv_w[0], ay = dts * pc.inv_w[1], az = dts * pc.inv_w[2];
-        int s = 0;
-        do {
-            const float mx = p.u + kex, my = p.v + key, mz = p.w + kez;
-            const float px = mx + (my * tz - mz * ty);
-            const float py = my + (mz * tx - mx * tz);
-            const float pz = mz + (mx * ty - my * tx);
-            p.u = mx + (py * sz - pz * sy) + kex;
-            p.v = my + (pz * sx - px * sz) + key;
-            p.w = mz + (px * sy - py * sx) + kez;
-            p.x = fmaf(p.u, ax, p.x);
-            p.y = fmaf(p.v, ay, p.y);
-            p.z = fmaf(p.w, az, p.z);
-        } while (++s < ns);
-    }
-    float R[3] = {p.x, p.y, p.z};
-    if (ci.edge) {
-        const int pos[3] = {ci.cx, ci.cy, ci.cz};
-        const int size[3] = {g.sx, g.sy, g.sz};
-        bool invert = false, drop = false;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            if (pos[a] == 0 && R[a] < 0.f) {
-                if (g.bc_lo[a] == 0) { invert = true; R[a] += 0.5f; }
-                else if (g.bc_lo[a] == 2) drop = true;
-            } else if (pos[a] == size[a] - 1 && R[a] > 1.f) {
-                if (g.bc_hi[a] == 0) { invert = true; R[a] -= 0.5f; }
-                else if (g.bc_hi[a] == 2) drop = true;
-            }
-        }
-        if (invert) { p.u = -p.u; p.v = -p.v; p.w = -p.w; }
-        if (drop) return kDrop;
-    }
-    {
-        const float dx = fmaf(R[0], pc.w[0], ci.ox - pc.center[0]);
-        const float dy = fmaf(R[1], pc.w[1], ci.oy - pc.center[1]);
-        const float dz = fmaf(R[2], pc.w[2], ci.oz - pc.center[2]);
-        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= pc.planet_r2) return kDrop;  // cell.h:1123-1128
-    }
-    const float fx = R[0] < 0.f ? -1.f : (R[0] > 1.f ? 1.f : 0.f);
-    const float fy = R[1] < 0.f ? -1.f : (R[1] > 1.f ? 1.f : 0.f);
-    const float fz = R[2] < 0.f ? -1.f : (R[2] > 1.f ? 1.f : 0.f);
-    p.x = R[0] - fx;
-    p.y = R[1] - fy;
-    p.z = R[2] - fz;
-    if (fx == 0.f && fy == 0.f && fz == 0.f) return kStay;
-    dir = ((int)fx + 1) | (((int)fy + 1) << 2) | (((int)fz + 1) << 4);
-    return kMove;
+__device__ __forceinline__ void store_slot(PipeStage& st, int sl, const PState<float>& p) {
+    st.s[0][sl] = p.x; st.s[1][sl] = p.y; st.s[2][sl] = p.z;
+    st.s[3][sl] = p.u; st.s[4][sl] = p.v; st.s[5][sl] = p.w;
+}
+// A slot whose particle left (a hole now, whose contents nothing reads):
+// the cell centre at rest, so that the moment pass adds exactly zero for it
+// (every centred monomial but 1 is 0, and so is the velocity; the rho count
+// is taken apart).
+__device__ __forceinline__ void clear_slot(PipeStage& st, int sl) {
+    st.s[0][sl] = 0.5f; st.s[1][sl] = 0.5f; st.s[2][sl] = 0.5f;
+    st.s[3][sl] = 0.f; st.s[4][sl] = 0.f; st.s[5][sl] = 0.f;
 }
 
 // FP64 atomic of corner m (bits x|y<<1|z<<2) and component q (0-2 J, 3 rho)
@@ -387,10 +263,15 @@ __device__ __forceinline__ void deposit_leavers32(const Geom& g, unsigned lb, in
     }
 }
 
-// Adds the centred cloud-in-cell moments of a stayer to acc (index 8 Q + m).
+// Adds the centred cloud-in-cell moments of a particle to acc (index 8 Q +
+// m, Q in {u, v, w, 1}, m in {1, x, y, xy, z, xz, yz, xyz} of r - 1/2):
+// kCount also counts it in acc[24] (the work-item path counts its stayers
+// apart). A cleared slot (clear_slot) adds zero.
+template <bool kCount>
 __device__ __forceinline__ void add_moments(float (&acc)[32], const PState<float>& p) {
     const float x = p.x - 0.5f, y = p.y - 0.5f, z = p.z - 0.5f;
-    const float xy = x * y, xz = x * z, yz = y * z, xyz = xy * z;
+    // separate roundings (no fusion with the sums below in some kernels only)
+    const float xy = __fmul_rn(x, y), xz = __fmul_rn(x, z), yz = __fmul_rn(y, z), xyz = __fmul_rn(xy, z);
     const float Q[3] = {p.u, p.v, p.w};
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
@@ -403,7 +284,7 @@ __device__ __forceinline__ void add_moments(float (&acc)[32], const PState<float
         acc[q * 8 + 6] = fmaf(Q[q], yz, acc[q * 8 + 6]);
         acc[q * 8 + 7] = fmaf(Q[q], xyz, acc[q * 8 + 7]);
     }
-    acc[24] += 1.f;
+    if (kCount) acc[24] += 1.f;
     acc[25] += x;
     acc[26] += y;
     acc[27] += xy;
@@ -428,15 +309,15 @@ __device__ __forceinline__ void emit_corner_sums(const Geom& g, float s, int cx,
 
 // Leaver bookkeeping of one warp step: outbox (one warp-aggregated append),
 // arrival list of the destination, cooperative deposit; the old slot is
-// filed as a hole of its cell (leavers and drops). `dir` is step32f's move.
-// The round trips (the destination's arrival slot, the outbox slots, the
-// hole slots) are issued together before any result is used, and cells are
-// flagged with plain stores (k_dirty_compact lists them). kOneCell: every
-// lane's slot is in `cell` (item mode), so the warp files its holes with one
-// aggregated atomic.
+// filed as a hole of its cell (leavers and drops). `dir` is the export's
+// move. The round trips (the destination's arrival slot, the outbox slots,
+// the hole slots) are issued together before any result is used, and cells
+// are flagged with plain stores (k_dirty_compact lists them). kOneCell:
+// every lane's slot is in `cell` (item mode), so the warp files its holes
+// with one aggregated atomic.
 template <bool kOneCell>
-__device__ __forceinline__ void leave_and_hole(const Geom& g, const Pop<float>& P, int outcome, int dir,
-                                               const CellInfo& ci, const PState<float>& p, int slot, int cell,
+__device__ __forceinline__ void leave_and_hole(const Geom& g, const Pop<float>& P, const Push32Const& pc, int outcome,
+                                               int dir, const PState<float>& p, int slot, int cell,
                                                int cstart, bool deposit, uint32_t& nmig, uint32_t& nrem) {
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
@@ -453,9 +334,10 @@ __device__ __forceinline__ void leave_and_hole(const Geom& g, const Pop<float>& 
     int nx = 0, ny = 0, nz = 0;
     if (lb) {
         // destination cell (periodic wrap of the index, as the outbox expects)
-        nx = ci.cx + (dir & 3) - 1;
-        ny = ci.cy + ((dir >> 2) & 3) - 1;
-        nz = ci.cz + ((dir >> 4) & 3) - 1;
+        const int3 c = cell_xyz(g, pc, cell);
+        nx = c.x + (dir & 3) - 1;
+        ny = c.y + ((dir >> 2) & 3) - 1;
+        nz = c.z + ((dir >> 4) & 3) - 1;
         nx = nx < 0 ? nx + g.sx : (nx >= g.sx ? nx - g.sx : nx);
         ny = ny < 0 ? ny + g.sy : (ny >= g.sy ? ny - g.sy : ny);
         nz = nz < 0 ? nz + g.sz : (nz >= g.sz ? nz - g.sz : nz);
@@ -507,40 +389,81 @@ __device__ __forceinline__ void leave_and_hole(const Geom& g, const Pop<float>& 
 }
 
 // Item mode: the warp pushes particles [a, b) (tile-local slots, b - a <=
-// PushShape::item) of cell `cell`, lane l taking a + l, a + l + 32, ... A first
-// pass moves them: stayers go back to the stage (the producer writes the
-// whole tile back with bulk stores), the slots of leavers and drops are
-// marked (NaN position; their slots are holes now, whose contents nothing
-// reads). The second pass sums the stayers' cloud-in-cell moments and
-// flushes the cell once. Keeping the 32 moment sums out of the mover keeps
-// the register count low enough for 6 warps per scheduler. `coef` points at
-// the cell's 48 field coefficients (shared memory).
+// PushShape::item) of cell `cell`, kItemPer at a time per lane: lane l takes
+// a + l, a + l + 32, ... (with two per lane one coefficient load serves both
+// and their arithmetic interleaves). When no particle of the warp step needs
+// more than one Boris sub-cycle (the common case) the step is straight-line
+// code with the species' one-step constants. Stayers go back to the stage (the producer writes the whole
+// tile back with bulk stores); the slots of leavers and drops are cleared
+// (holes now). A second pass sums the stayers' cloud-in-cell moments and
+// flushes the cell once, with the stayer count from the first pass's
+// ballots. `coef` points at the cell's 48 field coefficients (shared memory).
 template <int kF>
 __device__ __forceinline__ void push_item(const Geom& g, const Pop<float>& P, const Push32Const& pc,
-                                          const Push32Const& sp, PipeStage& st, const float* coef, int base, int cell,
-                                          int cstart, int a, int b, uint32_t& nmig, uint32_t& nrem) {
+                                          const Push32Const& sp, PipeStage& st, const float* coef,
+                                          const CellInfo& ci, int base, int cell, int cstart, int a, int b,
+                                          uint32_t& nmig, uint32_t& nrem) {
     constexpr bool kStep = (kF & kPipeStep) != 0, kDep = (kF & kPipeDeposit) != 0;
+    constexpr bool kGather = (kF & kPipeGather) != 0, kDipole = (kF & kPipeDipole) != 0;
     const int lane = threadIdx.x & 31;
-    const CellInfo ci = cell_info(g, pc, cell);
+    int gone = 0;  // leavers and drops of the item (warp-uniform)
     if (kStep) {
+        const float k1 = sp.k1, ksub = sp.k_sub;
 #pragma unroll 1
-        for (int s0 = a; s0 < b; s0 += 32) {
-            const int sl = s0 + lane;
-            PState<float> p;
-            int outcome = -1, dir = 0;
-            if (sl < b) {
-                p.x = st.s[0][sl]; p.y = st.s[1][sl]; p.z = st.s[2][sl];
-                p.u = st.s[3][sl]; p.v = st.s[4][sl]; p.w = st.s[5][sl];
-                outcome =
-                    step32f<true, (kF & kPipeGather) != 0, (kF & kPipeDipole) != 0>(g, pc, sp, coef, ci, p, dir);
-                if (outcome == kStay) {
-                    st.s[0][sl] = p.x; st.s[1][sl] = p.y; st.s[2][sl] = p.z;
-                    st.s[3][sl] = p.u; st.s[4][sl] = p.v; st.s[5][sl] = p.w;
-                } else if (kDep) {
-                    st.s[0][sl] = __int_as_float(0x7fffffff);  // not deposited here
+        for (int s0 = a; s0 < b; s0 += 32 * kItemPer) {
+            PState<float> p[kItemPer];
+            int sl[kItemPer], o[kItemPer], d[kItemPer];
+            float E[kItemPer][6];
+            float r[kItemPer];
+#pragma unroll
+            for (int i = 0; i < kItemPer; ++i) {
+                sl[i] = s0 + 32 * i + lane;
+                // a lane past the item works on a copy of slot a and keeps nothing
+                p[i] = load_slot(st, sl[i] < b ? sl[i] : a);
+            }
+            if (kGather) {
+                fields_n<true, kItemPer>(coef, p, E);
+            } else {
+#pragma unroll
+                for (int i = 0; i < kItemPer; ++i)
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) E[i][q] = 0.f;
+            }
+#pragma unroll
+            for (int i = 0; i < kItemPer; ++i) {
+                if (kDipole) add_dipole(pc, ci, p[i], E[i]);
+                r[i] = sub_ratio(ksub, E[i]);
+            }
+            bool fast = true;
+#pragma unroll
+            for (int i = 0; i < kItemPer; ++i) fast = fast && r[i] < 1.f;
+            if (__all_sync(0xffffffffu, fast)) {
+#pragma unroll
+                for (int i = 0; i < kItemPer; ++i) boris32<1>(k1, pc.a1[0], pc.a1[1], pc.a1[2], E[i], p[i]);
+            } else {
+#pragma unroll
+                for (int i = 0; i < kItemPer; ++i) {
+                    if (r[i] < 1.f) boris32<1>(k1, pc.a1[0], pc.a1[1], pc.a1[2], E[i], p[i]);
+                    else boris_sub(pc, sp, r[i], E[i], p[i]);
                 }
             }
-            leave_and_hole<true>(g, P, outcome, dir, ci, p, base + sl, cell, cstart, kDep, nmig, nrem);
+            bool any = false;
+#pragma unroll
+            for (int i = 0; i < kItemPer; ++i) {
+                d[i] = 0;
+                o[i] = export32(g, pc, ci, p[i], d[i]);
+                o[i] = sl[i] < b ? o[i] : -1;
+                if (o[i] == kStay) store_slot(st, sl[i], p[i]);
+                else if (kDep && o[i] > 0) clear_slot(st, sl[i]);
+                any = any || o[i] > 0;
+            }
+            if (__any_sync(0xffffffffu, any)) {
+#pragma unroll
+                for (int i = 0; i < kItemPer; ++i) {
+                    gone += __popc(__ballot_sync(0xffffffffu, o[i] > 0));
+                    leave_and_hole<true>(g, P, pc, o[i], d[i], p[i], base + sl[i], cell, cstart, kDep, nmig, nrem);
+                }
+            }
         }
         __syncwarp();
     }
@@ -548,20 +471,26 @@ __device__ __forceinline__ void push_item(const Geom& g, const Pop<float>& P, co
     float acc[32];
 #pragma unroll
     for (int l = 0; l < 32; ++l) acc[l] = 0.f;
+    int s0 = a;
 #pragma unroll 1
-    for (int s0 = a; s0 < b; s0 += 32) {
-        const int sl = s0 + lane;
-        if (sl < b) {
-            PState<float> p;
-            p.x = st.s[0][sl];
-            if (p.x == p.x) {
-                p.y = st.s[1][sl]; p.z = st.s[2][sl];
-                p.u = st.s[3][sl]; p.v = st.s[4][sl]; p.w = st.s[5][sl];
-                add_moments(acc, p);
-            }
-        }
+    for (; s0 + 64 <= b; s0 += 64) {
+        add_moments<false>(acc, load_slot(st, s0 + lane));
+        add_moments<false>(acc, load_slot(st, s0 + 32 + lane));
     }
-    emit_corner_sums(g, warp_transpose_sum<float>(acc), ci.cx, ci.cy, ci.cz, P.q);
+#pragma unroll 1
+    for (; s0 < b; s0 += 32) {
+        const int sl = s0 + lane;
+        PState<float> p = load_slot(st, sl < b ? sl : a);
+        if (sl >= b) {  // past the item: adds zero
+            p.x = p.y = p.z = 0.5f;
+            p.u = p.v = p.w = 0.f;
+        }
+        add_moments<false>(acc, p);
+    }
+    float s = warp_transpose_sum<float>(acc);
+    if (lane == 24) s = (float)(b - a - gone);  // the stayers: sum of the rho weights' 1 term
+    const int3 c = cell_xyz(g, pc, cell);
+    emit_corner_sums(g, s, c.x, c.y, c.z, P.q);
 }
 
 // warp_transpose_sum of acc over the lanes with `mine` set (the others add
@@ -591,11 +520,12 @@ __device__ __forceinline__ float run_transpose_sum(const float (&acc)[32], bool 
 
 // Slot mode: slice w of the tile (slots [128 w, 128 w + 128)) is pushed by
 // one warp, thread t of the slice the 4 slots from 4 t (one cell:
-// capacities are multiples of 8), and flushed per run of lanes of one cell.
+// capacities are multiples of 8), in two passes as in item mode (move, then
+// moments of the stayers), and flushed per run of lanes of one cell.
 template <int kF>
 __device__ __forceinline__ void push_slots(const Geom& g, const Pop<float>& P, const Push32Const& pc,
-                                           const Push32Const& sp, PipeStage& st, int base, int2 desc, int slice, uint32_t& nmig,
-                                           uint32_t& nrem) {
+                                           const Push32Const& sp, PipeStage& st, int base, int2 desc, int slice,
+                                           uint32_t& nmig, uint32_t& nrem) {
     constexpr bool kStep = (kF & kPipeStep) != 0, kDep = (kF & kPipeDeposit) != 0;
     constexpr int kPer = 4;
     const int lane = threadIdx.x & 31, tid = slice * 32 + lane;
@@ -620,54 +550,52 @@ __device__ __forceinline__ void push_slots(const Geom& g, const Pop<float>& P, c
         nv = e <= 0 ? 0 : (e >= kPer ? kPer : e);
     }
     const CellInfo ci = cell_info(g, pc, cell);
-    const float* coef = g.cellcoef + (size_t)cell * 48;
+    const int sl0 = tid * kPer;
+    int nst = nv;  // this thread's stayers
+    if (kStep) {
+        const float* coef = g.cellcoef + (size_t)cell * 48;
+        // lane groups start at different slots of their run of 4: the words a
+        // warp reads in one step fall in 32 different banks
+        const int rot = lane >> 3;
+#pragma unroll 1
+        for (int jj = 0; jj < kPer; ++jj) {
+            const int j = (jj + rot) & (kPer - 1);
+            const int sl = sl0 + j;
+            PState<float> p;
+            int outcome = -1, dir = 0;
+            if (j < nv) {
+                p = load_slot(st, sl);
+                outcome = step32f<false, (kF & kPipeGather) != 0, (kF & kPipeDipole) != 0>(g, pc, sp, coef, ci, p,
+                                                                                           dir);
+                if (outcome == kStay) store_slot(st, sl, p);
+                else if (kDep) clear_slot(st, sl);
+            }
+            if (outcome > 0) --nst;
+            leave_and_hole<false>(g, P, pc, outcome, dir, p, base + sl, cell, cstart, kDep, nmig, nrem);
+        }
+        __syncwarp();
+    }
+    if (!kDep) return;
     float acc[32];
 #pragma unroll
     for (int l = 0; l < 32; ++l) acc[l] = 0.f;
-    bool has_acc = false;
-    // lane groups start at different slots of their run of 4: the words a
-    // warp reads in one step fall in 32 different banks
-    const int rot = lane >> 3;
-    const int sl0 = tid * kPer;
 #pragma unroll 1
-    for (int jj = 0; jj < kPer; ++jj) {
-        const int j = (jj + rot) & (kPer - 1);
-        const int sl = sl0 + j;
-        PState<float> p;
-        int outcome = -1, dir = 0;
-        if (j < nv) {
-            p.x = st.s[0][sl]; p.y = st.s[1][sl]; p.z = st.s[2][sl];
-            p.u = st.s[3][sl]; p.v = st.s[4][sl]; p.w = st.s[5][sl];
-            outcome = kStep ? step32f<false, (kF & kPipeGather) != 0, (kF & kPipeDipole) != 0>(g, pc, sp, coef, ci,
-                                                                                                 p, dir)
-                            : kStay;
-            if (outcome == kStay) {
-                if (kStep) {
-                    st.s[0][sl] = p.x; st.s[1][sl] = p.y; st.s[2][sl] = p.z;
-                    st.s[3][sl] = p.u; st.s[4][sl] = p.v; st.s[5][sl] = p.w;
-                }
-                if (kDep) {
-                    add_moments(acc, p);
-                    has_acc = true;
-                }
-            }
-        }
-        if (kStep) leave_and_hole<false>(g, P, outcome, dir, ci, p, base + sl, cell, cstart, kDep, nmig, nrem);
-    }
-    if (!kDep) return;
-    const unsigned todo = __ballot_sync(0xffffffffu, has_acc);
+    for (int j = 0; j < nv; ++j) add_moments<false>(acc, load_slot(st, sl0 + j));
+    const unsigned todo = __ballot_sync(0xffffffffu, nst > 0);
     const int prev_cell = __shfl_up_sync(0xffffffffu, cell, 1);
     unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev_cell != cell);
     while (heads) {
-        const int a = __ffs(heads) - 1;
+        const int ra = __ffs(heads) - 1;
         heads &= heads - 1;
-        const int b = heads ? __ffs(heads) - 1 : 32;  // run [a, b)
-        const unsigned run = (b < 32 ? (1u << b) : 0u) - (1u << a);
+        const int rb = heads ? __ffs(heads) - 1 : 32;  // run [ra, rb)
+        const unsigned run = (rb < 32 ? (1u << rb) : 0u) - (1u << ra);
         if (!(todo & run)) continue;
-        const float s = run_transpose_sum(acc, ((run >> lane) & 1u) != 0);
-        const int gx = __shfl_sync(0xffffffffu, ci.cx, a), gy = __shfl_sync(0xffffffffu, ci.cy, a),
-                  gz = __shfl_sync(0xffffffffu, ci.cz, a);
-        emit_corner_sums(g, s, gx, gy, gz, P.q);
+        const bool mine = ((run >> lane) & 1u) != 0;
+        float s = run_transpose_sum(acc, mine);
+        const int cnt = __reduce_add_sync(0xffffffffu, mine ? nst : 0);
+        if (lane == 24) s = (float)cnt;
+        const int3 c = cell_xyz(g, pc, __shfl_sync(0xffffffffu, cell, ra));
+        emit_corner_sums(g, s, c.x, c.y, c.z, P.q);
     }
 }
 
@@ -686,7 +614,7 @@ __device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& 
         return;
     }
     // item mode: lane i describes cell c0 + i: its occupied slots [lo, hi)
-    // within the tile, its items and their exclusive prefix
+    // within the tile, its items and their exclusive prefix, its CellInfo
     const int64_t* S = st.start + (c0 & 1);
     const int32_t* N = st.count + (c0 & 3);
     int lo = 0, hi = 0, cst = 0;
@@ -696,6 +624,7 @@ __device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& 
         lo = l < 0 ? 0 : l;
         hi = h > kTileSlots ? kTileSlots : h;
     }
+    const CellInfo mine = cell_info(g, pc, c0 + (lane < nc ? lane : 0));
     const int sh = 31 - __clz(shp.item);  // items of 2^sh particles
     const int items = hi > lo ? (hi - lo + (1 << sh) - 1) >> sh : 0;
     int incl = items;
@@ -718,7 +647,8 @@ __device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& 
         const int cstart = __shfl_sync(0xffffffffu, cst, src);
         const int a = clo + ((j - cex) << sh);
         const int b = a + (1 << sh) < chi ? a + (1 << sh) : chi;
-        push_item<kF>(g, P, pc, sp, st, st.coef + src * 48, base, c0 + src, cstart, a, b, nmig, nrem);
+        push_item<kF>(g, P, pc, sp, st, st.coef + src * 48, shfl_cell_info(mine, src), base, c0 + src, cstart, a, b,
+                      nmig, nrem);
     }
 }
 
@@ -758,6 +688,7 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int G = gridDim.x;
     const int ntiles = tm.first[tm.n];
+    const uint32_t polls = shp.wait_polls < 0 ? kMaxPolls : (uint32_t)shp.wait_polls;
     if (tid == 0) {
         for (int s = 0; s < kStages; ++s) {
             mbar_init(&sm.full[s], 1);
@@ -797,7 +728,7 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
         int k = 0;
         for (int t = blockIdx.x; t < ntiles; t += G, ++k) {
             const int s = k % kStages;
-            if (!mbar_wait(&sm.empty[s], (uint32_t)(k / kStages) & 1u, abort)) {
+            if (!mbar_wait(&sm.empty[s], (uint32_t)(k / kStages) & 1u, abort, polls)) {
                 failed = true;
                 break;
             }
@@ -839,7 +770,7 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
     for (int t = blockIdx.x; t < ntiles; t += G, ++k) {
         const int s = k % kStages;
         // warp-uniform: every lane polls the same barrier
-        if (!__all_sync(0xffffffffu, mbar_wait(&sm.full[s], (uint32_t)(k / kStages) & 1u, abort))) {
+        if (!__all_sync(0xffffffffu, mbar_wait(&sm.full[s], (uint32_t)(k / kStages) & 1u, abort, polls))) {
             if (lane == 0 && atomicExch(&sm.abort, 1) == 0) atomicAdd(&S.p[0].ctr->timeouts, 1u);
             break;
         }
@@ -872,6 +803,7 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
     PipeSmem<kStages>& sm = *reinterpret_cast<PipeSmem<kStages>*>(smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int G = gridDim.x;
+    const uint32_t polls = shp.wait_polls < 0 ? kMaxPolls : (uint32_t)shp.wait_polls;
     if (tid == 0) {
         for (int s = 0; s < kStages; ++s) {
             mbar_init(&sm.full[s], 1);
@@ -910,7 +842,7 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
         int k = 0;
         for (int t = blockIdx.x; t < ntiles; t += G, ++k) {
             const int s = k % kStages;
-            if (!mbar_wait(&sm.empty[s], (uint32_t)(k / kStages) & 1u, abort)) {
+            if (!mbar_wait(&sm.empty[s], (uint32_t)(k / kStages) & 1u, abort, polls)) {
                 failed = true;
                 break;
             }
@@ -946,7 +878,7 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
     int k = 0;
     for (int t = blockIdx.x; t < ntiles; t += G, ++k) {
         const int s = k % kStages;
-        if (!__all_sync(0xffffffffu, mbar_wait(&sm.full[s], (uint32_t)(k / kStages) & 1u, abort))) {
+        if (!__all_sync(0xffffffffu, mbar_wait(&sm.full[s], (uint32_t)(k / kStages) & 1u, abort, polls))) {
             if (lane == 0 && atomicExch(&sm.abort, 1) == 0) atomicAdd(&jobs[0].P.ctr->timeouts, 1u);
             break;
         }

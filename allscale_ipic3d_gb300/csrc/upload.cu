@@ -231,6 +231,65 @@ template int launch_upload_cells<double>(const void*, const uint32_t*, const int
                                          const UploadPops<double>&, const UploadGeom&, const UploadDeposit&, int*,
                                          cudaStream_t);
 
+namespace {
+// One warp per cell of [c0, c1): every population's particles of the cell
+// as AoS records at their output indices (consecutive lanes write
+// consecutive 64-byte records).
+template <typename T>
+__global__ void k_pack_cells(PackPops<T> P, UploadGeom g, int c0, int c1, ipic3d_particle* __restrict__ out,
+                             uint32_t* __restrict__ out_ids) {
+    const int64_t c = c0 + ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (c >= c1) return;
+    const int cz = (int)(c % g.sz), cy = (int)((c / g.sz) % g.sy), cx = (int)(c / ((int64_t)g.sy * g.sz));
+    const double ox = g.origin[0] + (double)cx * g.w[0];
+    const double oy = g.origin[1] + (double)cy * g.w[1];
+    const double oz = g.origin[2] + (double)cz * g.w[2];
+    for (int k = 0; k < P.npop; ++k) {
+        const int n = P.count[k][c];
+        const int64_t s0 = P.start[k][c], d0 = P.dst[(int64_t)k * g.ncells + c];
+        for (int i = lane; i < n; i += 32) {
+            const int64_t s = s0 + i;
+            ipic3d_particle r;
+            if (P.relative) {
+                r.position[0] = ox + (double)P.x[k][s] * g.w[0];
+                r.position[1] = oy + (double)P.y[k][s] * g.w[1];
+                r.position[2] = oz + (double)P.z[k][s] * g.w[2];
+            } else {
+                r.position[0] = (double)P.x[k][s];
+                r.position[1] = (double)P.y[k][s];
+                r.position[2] = (double)P.z[k][s];
+            }
+            r.velocity[0] = (double)P.u[k][s];
+            r.velocity[1] = (double)P.v[k][s];
+            r.velocity[2] = (double)P.w[k][s];
+            r.q = P.q[k];
+            r.qom = P.qom[k];
+            double2* o = reinterpret_cast<double2*>(out + d0 + i);
+            o[0] = make_double2(r.position[0], r.position[1]);
+            o[1] = make_double2(r.position[2], r.velocity[0]);
+            o[2] = make_double2(r.velocity[1], r.velocity[2]);
+            o[3] = make_double2(r.q, r.qom);
+            if (out_ids) out_ids[d0 + i] = P.id[k] ? P.id[k][s] : 0u;
+        }
+    }
+}
+}  // namespace
+
+template <typename T>
+int launch_pack_cells(const PackPops<T>& P, const UploadGeom& g, int c0, int c1, void* out, uint32_t* out_ids,
+                      cudaStream_t st) {
+    if (c1 <= c0) return 0;
+    const int64_t threads = (int64_t)(c1 - c0) * 32;
+    k_pack_cells<T><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(P, g, c0, c1,
+                                                                        static_cast<ipic3d_particle*>(out), out_ids);
+    return 1;
+}
+template int launch_pack_cells<float>(const PackPops<float>&, const UploadGeom&, int, int, void*, uint32_t*,
+                                      cudaStream_t);
+template int launch_pack_cells<double>(const PackPops<double>&, const UploadGeom&, int, int, void*, uint32_t*,
+                                       cudaStream_t);
+
 int launch_classify(const void* parts, int64_t n, const SpeciesTable& sp, uint8_t* sid, int* unknown,
                     cudaStream_t st) {
     if (n <= 0) return 0;

@@ -54,6 +54,32 @@ int launch_upload_cells(const void* parts, const uint32_t* ids, const int64_t* i
                         const SpeciesTable& sp, const UploadPops<T>& U, const UploadGeom& g, const UploadDeposit& dep,
                         int* flags, cudaStream_t st);
 int launch_count(const uint8_t* sid, const int64_t* in_off, int ncells, int npop, int32_t* counts, cudaStream_t st);
+
+// Download: the populations' particles as the reference's AoS records
+// (Particle, particle.h:9-60), the i-th particle of cell c of population k at
+// output index dst[k][c] + i; cell-relative FP32 positions are made absolute
+// with the host's formula (origin + cx w) + x w in FP64.
+template <typename T>
+struct PackPops {
+    int npop;
+    int relative;
+    const T* x[kUploadMaxPops];
+    const T* y[kUploadMaxPops];
+    const T* z[kUploadMaxPops];
+    const T* u[kUploadMaxPops];
+    const T* v[kUploadMaxPops];
+    const T* w[kUploadMaxPops];
+    const uint32_t* id[kUploadMaxPops];
+    const int64_t* start[kUploadMaxPops];
+    const int32_t* count[kUploadMaxPops];
+    const int64_t* dst;  // [npop][ncells]
+    double q[kUploadMaxPops], qom[kUploadMaxPops];
+};
+// Cells [c0, c1): one warp per cell; `out` (records) and `out_ids` (may be
+// null) are device buffers indexed by the output index.
+template <typename T>
+int launch_pack_cells(const PackPops<T>& P, const UploadGeom& g, int c0, int c1, void* out, uint32_t* out_ids,
+                      cudaStream_t st);
 template <typename T>
 int launch_scatter(const void* parts, const uint32_t* ids, const uint8_t* sid, const int64_t* in_off,
                    const UploadPops<T>& U, const UploadGeom& g, cudaStream_t st);

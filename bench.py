@@ -68,6 +68,18 @@ def make_workload(seed):
     return props, parts, counts
 
 
+# trial steps of the push-shape autotuner on a fresh process (one full pass
+# over its candidate shapes); the reference arm runs as many untimed steps
+AUTOTUNE_STEPS = 21
+
+
+def headline_config(steps_before_timing):
+    """The `config` object of both arms' JSON lines (identical by design)."""
+    return {"workload": WORKLOAD, "cells": CELLS ** 3, "particles": CELLS ** 3 * 2 * PPC_SPECIES,
+            "steps_before_timing": int(steps_before_timing),
+            "l2": "inputs larger than L2: particle state 201 MB (FP32) / 403 MB (FP64) > 129 MB"}
+
+
 def make_config(precision, graph=True):
     from allscale_ipic3d_gb300 import abi
     flags = abi.F_DIPOLE_IN_GATHER | abi.F_REFRESH_NODE_B | abi.F_INJECT_LOW_X
@@ -141,18 +153,12 @@ def measured_peak():
     return 6800.0, "fallback 6.8 TB/s"
 
 
-def profiled_traffic(precision):
-    """DRAM bytes per push launch from the committed ncu summary, if any."""
-    name = os.path.join(ROOT, "profiles", "k_push32_pipe_dipole32.md" if precision == "fp32" else "k_push64_dipole32.md")
-    if not os.path.exists(name):
-        return None
-    for line in open(name):
-        if line.strip().startswith("dram_bytes_per_launch:"):
-            try:
-                return int(float(line.split(":")[1].strip().split()[0]))
-            except ValueError:
-                return None
-    return None
+# DRAM bytes (read + write) per push launch on the headline workload, from
+# one ncu capture of each kernel (the committed summaries under profiles/
+# give the command); a citation of that capture, not a measurement of this
+# run. FP32: one launch for both species; FP64: one launch per species.
+PUSH_TRAFFIC = {"fp32": (437772544, "ncu capture, profiles/k_push32_pipe_dipole32.md"),
+                "fp64": (369767168, "ncu capture, profiles/k_push64_dipole32.md")}
 
 
 def combine_ranks(ms, psteps, dist, device):
@@ -250,7 +256,8 @@ def push_roofline(sim, precision, nsteps, props, pops, headline=True):
     achieved = bytes_per / (ms_per * 1e-3) / 1e9
     phases = {k: round(v["ms"] / max(v["launches"], 1), 5) for k, v in prof.items() if v["launches"]}
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": profiled_traffic(precision) if headline else None,
+            "traffic": PUSH_TRAFFIC[precision][0] if headline else None,
+            "traffic_source": PUSH_TRAFFIC[precision][1] if headline else None,
             "kernel": ("ipg::k_push32_pipe<3, 2, 15>" if headline else "ipg::k_push32_pipe") if elem == 4
             else "ipg::k_push<double>",
             "bytes_per_launch": bytes_per, "ms_per_launch": ms_per, "launches_per_step": launches_per_step,
@@ -282,6 +289,196 @@ def cpu_port_run(props, parts, counts, warmup, steps, budget_s, cfg=None):
     n1 = lib.oracle_particle_count(sim.s)
     sim.close()
     return 0.5 * (n0 + n1) * done / dt, threads, done, dt
+
+
+# ---- end to end ----------------------------------------------------------------------
+def run_e2e(props, parts, counts, steps, dist=None):
+    """The headline metric through the public API with host buffers, as the
+    drop-in simulateSteps(1, universe) runs it every step: the reference's
+    AoS particles (pinned host memory) up to the device, one step, every
+    particle and the per-cell counts back into pinned host memory. Particle-
+    steps per second of the whole round trip."""
+    import torch
+    import allscale_ipic3d_gb300 as g
+    from allscale_ipic3d_gb300 import abi
+    host_in = torch.empty(parts.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(abi.PARTICLE_DTYPE)
+    host_in[:] = parts
+    cap = int(len(parts) * 1.05) + 4096  # room for the injected particles of a step
+    host_out = torch.empty(cap * parts.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(abi.PARTICLE_DTYPE)
+    out_counts = torch.zeros(len(counts), dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+    sim = g.Simulation(props, make_config(abi.FP32))
+    sim.upload_particles(host_in, counts)
+    autotune(sim)  # the shape the timed headline used (cached: no trials here)
+    sim.upload_particles(host_in, counts)
+    sim.step(1)
+    sim.download_particles(out=(host_out, out_counts), ids=False)
+    phase = {"upload": 0.0, "step": 0.0, "download": 0.0}
+    d2h = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ta = time.perf_counter()
+        sim.upload_particles(host_in, counts)
+        tb = time.perf_counter()
+        sim.step(1)
+        sim.synchronize()
+        tc = time.perf_counter()
+        got, _, _ = sim.download_particles(out=(host_out, out_counts), ids=False)
+        td = time.perf_counter()
+        d2h += got.nbytes + out_counts.nbytes
+        phase["upload"] += tb - ta
+        phase["step"] += tc - tb
+        phase["download"] += td - tc
+    secs = time.perf_counter() - t0
+    sim.close()
+    ms, psteps = combine_ranks(1e3 * secs, float(len(parts) * steps), dist, "cuda")
+    link = {k: round(v, 1) for k, v in host_link_rates(parts.nbytes).items()}
+    return {"value": psteps / (ms * 1e-3), "unit": UNIT, "steps": steps,
+            "h2d_bytes_per_step": int(parts.nbytes + counts.nbytes), "d2h_bytes_per_step": int(d2h // max(steps, 1)),
+            "ms_per_phase": {k: round(1e3 * v / steps, 3) for k, v in phase.items()},
+            "host_link_gbs": link,
+            "note": "per step: upload of every particle (AoS, pinned host memory, chunked copies with the scatter "
+                    "kernel behind them), one step, download of every particle and the per-cell counts (device "
+                    "pack kernel, chunked copies behind it)"}
+
+
+def host_link_rates(nbytes):
+    """Pinned host<->device copy rates (GB/s) over `nbytes`, CUDA events on
+    one stream: H2D alone, D2H alone, and both directions at once on two
+    streams (the link is full duplex)."""
+    import torch
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    h2 = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    d2 = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    out = {}
+    for name in ("h2d", "d2h", "both"):
+        best = None
+        for _ in range(3):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s1)
+            s2.wait_event(e0)
+            if name in ("h2d", "both"):
+                with torch.cuda.stream(s1):
+                    d.copy_(h, non_blocking=True)
+            if name in ("d2h", "both"):
+                with torch.cuda.stream(s2 if name == "both" else s1):
+                    h2.copy_(d2, non_blocking=True)
+            s1.wait_stream(s2)
+            e1.record(s1)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        out[name] = (2 if name == "both" else 1) * nbytes / (best * 1e-3) / 1e9
+    return out
+
+
+# ---- error statements ---------------------------------------------------------------
+NO_ID = 0xFFFFFFFF  # particles made by the injection carry no id
+
+
+def array_error(a, b):
+    """Error of `a` against `b`: max |a - b| over max |b| (relative to the
+    field's peak), and the max and median of |a - b| / |b| over the entries
+    with |b| above 1e-6 of the peak."""
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    d = np.abs(a - b)
+    peak = float(np.abs(b).max()) if b.size else 0.0
+    sel = np.abs(b) > 1e-6 * peak if peak > 0 else np.zeros(b.shape, bool)
+    rel = d[sel] / np.abs(b[sel])
+    return {"max_rel_to_peak": float(d.max() / peak) if peak > 0 else float(d.max(initial=0.0)),
+            "max_rel": float(rel.max()) if rel.size else 0.0, "median_rel": float(np.median(rel)) if rel.size else 0.0,
+            "peak": peak}
+
+
+def particle_error(a, b, props):
+    """Particle states of two runs matched by id (injected particles, which
+    carry no id, are counted apart): position error in cell widths,
+    velocity error relative to |v|."""
+    (pa, ca, ia), (pb, cb, ib) = a, b
+    ka, kb = ia != NO_ID, ib != NO_ID
+    common, xa, xb = np.intersect1d(ia[ka], ib[kb], assume_unique=True, return_indices=True)
+    ra, rb = pa[ka][xa], pb[kb][xb]
+    w = np.array(props.cell_width, np.float64)
+    dx = np.abs(ra["position"] - rb["position"]) / w
+    vb = np.linalg.norm(rb["velocity"], axis=1)
+    dv = np.linalg.norm(ra["velocity"] - rb["velocity"], axis=1) / np.where(vb > 0, vb, 1.0)
+    return {"matched": int(len(common)), "only_first": int(ka.sum() - len(common)),
+            "only_second": int(kb.sum() - len(common)),
+            "injected": [int((~ka).sum()), int((~kb).sum())],
+            "position_cells": {"max": float(dx.max(initial=0.0)), "median": float(np.median(dx)) if dx.size else 0.0},
+            "velocity_rel": {"max": float(dv.max(initial=0.0)), "median": float(np.median(dv)) if dv.size else 0.0},
+            "cell_counts": {"cells_differing": int((ca != cb).sum()),
+                            "sum_abs_difference": int(np.abs(ca.astype(np.int64) - cb.astype(np.int64)).sum())}}
+
+
+def conserved_error(a, b):
+    """Relative error of every conserved quantity of `a` against `b`."""
+    tot = lambda c: c["kinetic_energy"] + c["e_energy"] + c["b_energy"]
+    out = {}
+    for k in ("kinetic_energy", "e_energy", "b_energy", "total_momentum", "total_charge"):
+        out[k] = abs(a[k] - b[k]) / abs(b[k]) if b[k] != 0 else abs(a[k] - b[k])
+    out["total_energy"] = abs(tot(a) - tot(b)) / abs(tot(b))
+    out["particles"] = [int(a["particles"]), int(b["particles"])]
+    return out
+
+
+def state_of(sim):
+    """(particles with ids, fields, conserved) of a GPU or oracle run."""
+    parts = sim.download_particles()
+    f, bc, J, rho = sim.download_fields()
+    return parts, (f, bc, J, rho), sim.conserved()
+
+
+def state_error(a, b, props):
+    """Every output of run `a` against run `b` (same steps from the same
+    particles): E (node), Bc (cell centres), J and rho (nodes), the particle
+    states matched by id, the per-cell counts and the conserved quantities."""
+    (pa, (fa, ba, ja, ra), ca), (pb, (fb, bb, jb, rb), cb) = a, b
+    return {"E": array_error(fa[..., 0:3], fb[..., 0:3]), "Bc": array_error(ba, bb), "J": array_error(ja, jb),
+            "rho": array_error(ra, rb), "particles": particle_error(pa, pb, props),
+            "conserved": conserved_error(ca, cb)}
+
+
+def headline_errors(props, parts, counts, steps, cpu_steps):
+    """The headline workload's error statement: FP32 GPU against FP64 GPU
+    after `steps` steps, and FP64 GPU against the CPU oracle (the reference's
+    double-precision algorithm) after `cpu_steps` steps, every output, from
+    the same particles (ids tracked)."""
+    import allscale_ipic3d_gb300 as g
+    from allscale_ipic3d_gb300 import abi
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle
+    from common import OracleSim
+    ids = np.arange(len(parts), dtype=np.uint32)
+    out = {}
+    sims = {}
+    for name, prec in (("fp32", abi.FP32), ("fp64", abi.FP64)):
+        cfg = make_config(prec, graph=True)
+        cfg.flags |= abi.F_TRACK_IDS
+        sim = g.Simulation(props, cfg)
+        sim.upload_particles(parts, counts, ids)
+        sims[name] = sim
+    sims["fp64"].step(cpu_steps)
+    s64_cpu = state_of(sims["fp64"])
+    lib = oracle.load()
+    lib.oracle_set_threads(os.cpu_count() or 1)
+    cfg = make_config(abi.FP64, graph=False)
+    cfg.flags |= abi.F_TRACK_IDS
+    orc = OracleSim(props, cfg)
+    orc.upload_particles(parts, counts, ids)
+    orc.step(cpu_steps)
+    orc.project()  # the oracle's J after its last move (the GPU deposits during the move)
+    out["fp64_gpu_vs_cpu_oracle"] = dict(steps=cpu_steps, **state_error(s64_cpu, state_of(orc), props))
+    orc.close()
+    sims["fp64"].step(steps - cpu_steps)
+    sims["fp32"].step(steps)
+    out["fp32_vs_fp64_gpu"] = dict(steps=steps, **state_error(state_of(sims["fp32"]), state_of(sims["fp64"]), props))
+    for s in sims.values():
+        s.close()
+    return out
 
 
 # ---- batched ensemble -----------------------------------------------------------
@@ -353,7 +550,7 @@ def timed_batch(batch, warmup, steps, sampler=None, pre_steps=None):
     import torch
     if pre_steps is None:
         pre_steps = autotune(batch)
-    else:
+    elif pre_steps:
         batch.step(pre_steps)
     batch.step(warmup)
     batch.synchronize()
@@ -413,15 +610,30 @@ def run_ensemble(count, warmup, steps, local):
             b.universe(i).upload_particles(parts, counts)
     cells = int(sum(p.ncells for p in props))
     setup_s = time.perf_counter() - t_setup
+
+    def ke_rel():
+        rel, lost = [], 0
+        for i in range(count):
+            c32, c64 = b32.universe(i).conserved(), b64.universe(i).conserved()
+            rel.append(abs(c32["kinetic_energy"] - c64["kinetic_energy"]) / abs(c64["kinetic_energy"]))
+            lost += abs(int(c32["particles"]) - int(c64["particles"]))
+        return np.array(rel), lost
+
+    # the FP32 error against FP64 over the configuration's 100 steps from the
+    # fresh start, every 20 steps (the FP32 batch's first steps are its push
+    # autotuner's trials: ordinary steps of the simulation)
+    curve = []
+    for k in range(5):
+        b32.step(20)
+        b64.step(20)
+        r, lost_k = ke_rel()
+        curve.append({"step": 20 * (k + 1), "max": float(r.max()), "median": float(np.median(r)),
+                      "particle_count_differences": lost_k})
     sampler = ClockSampler(local)
-    ms32, ps32, launches32, pre = timed_batch(b32, warmup, steps, sampler)
-    ms64, ps64, _, _ = timed_batch(b64, warmup, steps, pre_steps=pre)
-    rel, lost = [], 0
-    for i in range(count):
-        c32, c64 = b32.universe(i).conserved(), b64.universe(i).conserved()
-        rel.append(abs(c32["kinetic_energy"] - c64["kinetic_energy"]) / abs(c64["kinetic_energy"]))
-        lost += abs(int(c32["particles"]) - int(c64["particles"]))
-    rel = np.array(rel)
+    ms32, ps32, launches32, pre = timed_batch(b32, warmup, steps, sampler, pre_steps=0)
+    ms64, ps64, _, _ = timed_batch(b64, warmup, steps, pre_steps=0)
+    pre = 100
+    rel, lost = ke_rel()
     worst = [dict(zip(("universe", "n", "ppc", "B", "E", "sigma", "ke_rel"),
                       (int(i),) + tuple(universe_params(int(i))) + (float(rel[i]),)))
              for i in np.argsort(rel)[::-1][:4]]
@@ -436,14 +648,15 @@ def run_ensemble(count, warmup, steps, local):
     return {"workload": ENS_WORKLOAD, "universes": count, "cells": cells, "particles": total,
             "steps": steps, "warmup": warmup, "setup_s": round(setup_s, 1),
             "fp32_batched": {"value": v32, "ms_per_step": ms32 / steps, "gpu_launches": int(launches32),
-                             "push_shape": shape32, "autotune_steps": pre},
+                             "push_shape": shape32, "steps_before_timing": pre},
             "fp64_batched": {"value": v64, "ms_per_step": ms64 / steps},
             "fp64_plain": {"value": vp64, "ms_per_step": msp64 / steps},
             "fp32_plain": {"value": vp32, "ms_per_step": msp32 / steps},
             "fp32_batched_over_fp64_plain": v32 / vp64, "fp32_batched_over_fp64_batched": v32 / v64,
             "kinetic_energy_rel_fp32_vs_fp64": {"after_steps": pre + warmup + steps, "max": float(rel.max()),
                                                 "median": float(np.median(rel)), "worst": worst,
-                                                "particle_count_differences": lost},
+                                                "particle_count_differences": lost,
+                                                "first_100_steps": curve},
             "stats_fp32": st32, "stats_fp64": st64,
             "clocks": sampler.summary(), "unit": UNIT}
 
@@ -563,14 +776,17 @@ def config_udist():
             None, kw, 20)
 
 
-def run_config(name, warmup, local):
+def run_config(name, warmup, local, steps=None, cpu=True):
     """FP32 and FP64 on the same inputs: particle-steps/s, the FP32 push's
-    live roofline, the FP32 energy error against FP64 after the run."""
+    live roofline, the FP32 energy error against FP64 after the run, and a
+    bounded CPU-oracle sample (C5, :U:N). `steps` overrides the
+    configuration's timed steps."""
     import allscale_ipic3d_gb300 as g
     from allscale_ipic3d_gb300 import abi
     t0 = time.perf_counter()
-    desc, props, parts, counts, fields, kw, steps = {"c1": config_c1, "c3": config_c3, "c5": config_c5,
-                                                     "udist": config_udist}[name]()
+    desc, props, parts, counts, fields, kw, nsteps = {"c1": config_c1, "c3": config_c3, "c5": config_c5,
+                                                      "udist": config_udist}[name]()
+    steps = nsteps if steps is None else steps
     res = {"workload": desc, "cells": props.ncells, "particles": int(len(parts)) if parts is not None else UDIST_N,
            "steps": steps, "warmup": warmup}
     species = [(-1.0, -25.0)] if parts is None else \
@@ -613,7 +829,16 @@ def run_config(name, warmup, local):
                                  "particles_fp32": cons["fp32"]["particles"],
                                  "particles_fp64": cons["fp64"]["particles"]}
     res["fp32_over_fp64"] = res["fp32"]["value"] / res["fp64"]["value"]
-    if name == "udist":  # the reference's own CPU algorithm (the oracle port) on the same universe
+    res["value"] = res["fp32"]["value"]
+    res["roofline"] = res["fp32"]["roofline"]
+    res["configured_steps"] = nsteps
+    if name == "c5" and cpu:  # the oracle port on a bounded sample: the full universe, a few steps
+        cfg = abi.Config.make(precision=abi.FP64, **dict(kw, flags=kw["flags"] & ~abi.F_USE_GRAPH))
+        v, cores, done, secs = cpu_port_run(props, parts, counts, 1, 3, 30.0, cfg)
+        res["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": "the full universe (268,435,456 particles), %d timed steps (%.1f s) after "
+                                         "1 warm-up step, all host threads" % (done, secs)}
+    if name == "udist" and cpu:  # the reference's own CPU algorithm (the oracle port) on the same universe
         cfg = abi.Config.make(precision=abi.FP64, **{k: v for k, v in kw.items() if k != "flags"})
         sys.path.insert(0, os.path.join(ROOT, "tests"))
         import oracle
@@ -623,9 +848,9 @@ def run_config(name, warmup, local):
         oracle.load().oracle_init_uniform_bench(C.byref(props), UDIST_N, abi.vptr(parts), abi.vptr(counts))
         res.setdefault("init_ms", {})["cpu_port"] = round(1e3 * (time.perf_counter() - t_init), 2)
         v, cores, done, secs = cpu_port_run(props, parts, counts, 2, 5, 60.0, cfg)
-        res["cpu_port"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                           "sample": "the full universe, %d timed steps (%.1f s) after 2 warm-up steps, all host "
-                                     "threads (the reference's benchmark.h protocol)" % (done, secs)}
+        res["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": "the full universe, %d timed steps (%.1f s) after 2 warm-up steps, all host "
+                                         "threads (the reference's benchmark.h protocol)" % (done, secs)}
     res["species"] = species
     res["setup_and_run_s"] = round(time.perf_counter() - t0, 1)
     return res
@@ -734,14 +959,19 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", default="all", choices=["all", "fp32", "ensemble", "c1", "c3", "c5", "udist", "tracer"],
-                    help="fp32: only the FP32 timed run and its roofline (small profiling runs); "
+    ap.add_argument("--only", default="all", choices=["all", "fp32", "fp64", "ensemble", "c1", "c3", "c5", "udist", "tracer"],
+                    help="fp32 / fp64: only that precision's timed run and its push roofline (profiling runs); "
                          "ensemble: only the batched ensemble; c1/c3/c5: that configuration alone")
     ap.add_argument("--tracer-particles", type=int, default=TRACER_N)
     ap.add_argument("--universes", type=int, default=256, help="universes of the batched ensemble")
     ap.add_argument("--ensemble-steps", type=int, default=100)
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-tracer", action="store_true", help="skip the standalone tracer's row in the full run")
+    ap.add_argument("--no-error", action="store_true", help="skip the headline's error statement")
+    ap.add_argument("--error-steps", type=int, default=100, help="steps of the FP32 vs FP64 GPU error statement")
+    ap.add_argument("--error-cpu-steps", type=int, default=10, help="steps of the FP64 GPU vs CPU oracle statement")
+    ap.add_argument("--no-configs", action="store_true", help="skip the C5 and :U:N rows in the full run")
+    ap.add_argument("--c5-steps", type=int, default=20, help="timed steps of the C5 row in the full run")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -753,14 +983,17 @@ def main():
         if rank != 0:
             return 0
         props, parts, counts = make_workload(12345)
-        value, cores, done, secs = cpu_port_run(props, parts, counts, min(args.warmup, 2), args.steps, 120.0)
+        # the same simulated interval as the GPU arm: its autotuner's trial
+        # steps and its warm-up run untimed first
+        pre = AUTOTUNE_STEPS + args.warmup
+        value, cores, done, secs = cpu_port_run(props, parts, counts, pre, args.steps, 120.0)
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": done, "warmup": args.warmup,
                "ms_per_step": 1e3 * secs / max(done, 1), "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-               "config": {"workload": WORKLOAD, "cells": CELLS ** 3, "particles": int(len(parts))},
+               "config": headline_config(pre),
                "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                                "sample": "the full workload, %d timed steps (%.1f s) after 2 warm-up steps" %
-                                          (done, secs)},
+                                "sample": "the full workload, %d timed steps (%.1f s) after %d untimed steps (the GPU "
+                                          "arm's autotuner trials and warm-up)" % (done, secs, pre)},
                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(out))
         return 0
@@ -796,6 +1029,19 @@ def main():
 
     props, parts, counts = make_workload(12345 + rank)
     ncells = props.ncells
+
+    if args.only == "fp64":  # the FP64 GPU path alone (profiling runs of its push)
+        sim64 = g.Simulation(props, make_config(abi.FP64))
+        sim64.upload_particles(parts, counts)
+        ms64, psteps64, launches64, n0, _ = run_timed(sim64, args.warmup, args.steps, pre_steps=0)
+        roof64 = push_roofline(sim64, "fp64", 2, props, 2)
+        out = {"metric": METRIC, "value": psteps64 / (ms64 * 1e-3), "unit": UNIT, "n_gpus": world,
+               "steps": args.steps, "ms_per_step": ms64 / args.steps, "roofline": roof64, "stats": sim64.stats(),
+               "gpu_launches": int(launches64), "dtype": "f64"}
+        if rank == 0:
+            print(json.dumps(out))
+        sim64.close()
+        return 0
 
     # ---- FP32 headline ----
     sim32 = g.Simulation(props, make_config(abi.FP32))
@@ -840,32 +1086,7 @@ def main():
     sim64.close()
 
     # ---- end to end through the public API, host buffers ----
-    host = torch.empty(parts.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(abi.PARTICLE_DTYPE)
-    host[:] = parts
-    e2e = g.Simulation(props, make_config(abi.FP32))
-    e2e.upload_particles(host, counts)
-    e2e.step(1)
-    e2e.cell_counts()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    phase = {"upload": 0.0, "step": 0.0, "counts": 0.0}
-    for _ in range(args.e2e_steps):
-        ta = time.perf_counter()
-        e2e.upload_particles(host, counts)
-        tb = time.perf_counter()
-        e2e.step(1)
-        e2e.synchronize()
-        tc = time.perf_counter()
-        res = e2e.cell_counts()
-        td = time.perf_counter()
-        phase["upload"] += tb - ta
-        phase["step"] += tc - tb
-        phase["counts"] += td - tc
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    e2e_ms, e2e_psteps = combine_ranks(1e3 * e2e_s, float(len(parts) * args.e2e_steps), dist, "cuda")
-    e2e_value = e2e_psteps / (e2e_ms * 1e-3)
-    e2e.close()
+    e2e_res = run_e2e(props, parts, counts, args.e2e_steps, dist)
 
     tracer_row = None
     if not args.no_tracer and world == 1:  # pic_tracer's default run (its own metric), beside the headline
@@ -882,31 +1103,48 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, cores, done, secs = cpu_port_run(props, parts, counts, 1, 50, args.cpu_budget)
+        pre = tune_steps + args.warmup
+        v, cores, done, secs = cpu_port_run(props, parts, counts, pre, 50, args.cpu_budget)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": "the full workload (8,388,608 particles), %d timed steps (%.1f s) after 1 warm-up step, "
-                         "all host threads" % (done, secs)}
+               "sample": "the full workload (8,388,608 particles), %d timed steps (%.1f s) after %d untimed steps "
+                         "(the autotuner's trials and the warm-up), all host threads" % (done, secs, pre)}
+
+    # ---- error of every output at the headline size, against both oracles ----
+    errors = None
+    if rank == 0 and not args.no_error:
+        errors = headline_errors(props, parts, counts, args.error_steps, args.error_cpu_steps)
+
+    # ---- the largest single-GPU configuration and the reference's own mode ----
+    configs = {}
+    if rank == 0 and world == 1 and not args.no_configs:
+        for name, steps in (("c5", args.c5_steps), ("udist", 20)):
+            try:
+                configs[name] = run_config(name, args.warmup, local, steps=steps, cpu=not args.no_cpu_baseline)
+            except Exception as e:  # the headline line is printed regardless
+                configs[name] = {"error": "%s: %s" % (type(e).__name__, e)}
+            torch.cuda.empty_cache()
 
     out = {
         "metric": METRIC, "value": value32, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms32 / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "cells": ncells, "particles": int(n0), "precision":
-                   "fp32 push/deposit (cell-relative), fp64 node moments/fields/reductions",
-                   "l2": "inputs larger than L2: particle state %.0f MB > 129 MB" % (n0 * 24 / 1e6),
-                   "graph": True, "parallelism": "replicas" if world > 1 else "single",
-                   "push_shape": shape32, "autotune_steps": tune_steps},
+        "config": headline_config(tune_steps + args.warmup),
+        "setup": {"precision": "fp32 push/deposit (cell-relative), fp64 node moments/fields/reductions",
+                  "particles_at_timing": int(n0), "graph": True,
+                  "parallelism": "replicas" if world > 1 else "single", "push_shape": shape32,
+                  "autotune_steps": tune_steps},
         "roofline": roof,
         "fp64": {"value": value64, "ms_per_step": ms64 / args.steps, "roofline": roof64, "stats": stats64},
         "fp32_over_fp64": value32 / value64,
         "error_fp32_vs_fp64": err,
+        "error": errors,
         "stats": stats32,
         "cpu_baseline": cpu,
         "ensemble": ens,
         "tracer": tracer_row,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(parts.nbytes + counts.nbytes),
-                "ms_per_phase": {k: round(1e3 * v / args.e2e_steps, 3) for k, v in phase.items()},
-                "d2h_bytes_per_step": int(res.nbytes)},
+        "c5": configs.get("c5"),
+        "udist": configs.get("udist"),
+        "e2e": e2e_res,
         "clocks": sampler.summary(),
         "gpu_launches": int(launches32),
     }

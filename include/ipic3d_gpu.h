@@ -253,6 +253,16 @@ int ipic3d_gpu_get_push_shape(ipic3d_ctx* ctx, ipic3d_push_shape* out);
  * clamped at launch); shape == NULL restarts the autotuner: the next steps
  * are its trials. */
 int ipic3d_gpu_set_push_shape(ipic3d_ctx* ctx, const ipic3d_push_shape* shape);
+/* No counterpart in the reference (its runtime has no device waits). The
+ * FP32 push's warps wait on their own thread block's shared-memory barriers
+ * (bulk-copy completion, stage release); each wait gives up after a bounded
+ * number of polls of about 20 us, the thread block then records a timeout,
+ * lets its copies in flight land (always with the default bound) and
+ * returns, and the step returns IPIC3D_E_TIMEOUT. polls < 0 restores the
+ * default bound (about 1 s); polls >= 0 sets it (0: every wait gives up
+ * before its first poll -- the way a test makes the bound run out). Takes
+ * effect from the next step (captured step graphs are dropped). */
+int ipic3d_gpu_set_wait_limit(ipic3d_ctx* ctx, int64_t polls);
 
 /* ---- element kernels (the reference's unit-level functions) ------------- */
 /* Particle::updateVelocity + updatePosition (particle.h:24-49) applied
@@ -296,20 +306,21 @@ int ipic3d_gpu_batch_stats(ipic3d_batch* batch, ipic3d_stats* out);
 int ipic3d_gpu_batch_get_push_shape(ipic3d_batch* batch, ipic3d_push_shape* out);
 
 /* ---- projection without allocation -------------------------------------- */
-/* No counterpart in the reference. The current projection of
- * ipic3d_gpu_project (projectToDensityField over all nodes, cell.h:787-824)
- * for callers that cannot allocate device memory: hosts that hand out every
- * byte of device memory from their own pool, or loops where a cudaMalloc
- * would synchronise the device. Nothing here allocates: the caller passes
- * device pointers to the particles (grouped by cell, d_cell_offsets[c] ..
- * d_cell_offsets[c+1] for cell c, ncells + 1 entries), J ((size+1)^3 x 3
- * doubles) and rho ((size+1)^3 doubles, may be NULL); the FP64 node sums in
- * between live in one fixed device array of the library, sized for grids of
- * at most 32^3 cells (larger grids return IPIC3D_E_CAPACITY). The first call
- * on a device looks up that array's device address, so make it once before
- * any stream capture. Every call shares the array: calls that overlap on
- * the GPU (other streams, other host threads) race. flags: IPIC3D_F_J_DIV8.
- * Work is enqueued on `stream` (a cudaStream_t, NULL = default stream). */
+/* No counterpart in the reference. The same projection as
+ * ipic3d_gpu_project, for callers that cannot allocate device memory: hosts
+ * that hand out every byte of device memory from their own pool, or loops
+ * where a cudaMalloc would synchronise the device. Nothing here allocates:
+ * the caller passes device pointers to the particles (grouped by cell,
+ * d_cell_offsets[c] .. d_cell_offsets[c+1] for cell c, ncells + 1 entries),
+ * J ((size+1)^3 x 3 doubles) and rho ((size+1)^3 doubles, may be NULL); the
+ * FP64 node sums in between live in one fixed device array of the library,
+ * sized for grids of at most (32+1)^3 nodes (larger grids return
+ * IPIC3D_E_CAPACITY before any work is enqueued). The first call in each
+ * CUDA context (and the first after a cudaDeviceReset) looks up that array's
+ * device address, so make it once before any stream capture. Every call
+ * shares the array: calls that overlap on the GPU (other streams, other host
+ * threads) race. flags: IPIC3D_F_J_DIV8. Work is enqueued on `stream` (a
+ * cudaStream_t, NULL = default stream). */
 int ipic3d_gpu_project_noalloc(const ipic3d_props* props, uint32_t flags, const ipic3d_particle* d_particles,
                                const uint64_t* d_cell_offsets, double* d_J, double* d_rho, void* stream);
 
