@@ -125,6 +125,11 @@ constexpr int kSlotWarps = kTileSlots / 128;        // slot mode: 128-slot slice
 constexpr int kItemMaxCells = 32;
 // particles per lane and warp step of the item mode's move pass
 constexpr int kItemPer = 1;
+// slot mode: moments added during the move pass (one pass) or in a second
+// pass over the stage (two passes, fewer live registers)
+constexpr bool kSlotOnePass = false;
+// item mode: items assigned to warps by a fixed rotation (no counter)
+constexpr bool kStaticItems = false;
 
 // Every member is a bulk-copy destination: 16-byte aligned offsets.
 struct __align__(16) PipeStage {
@@ -552,7 +557,32 @@ __device__ __forceinline__ void push_slots(const Geom& g, const Pop<float>& P, c
     const CellInfo ci = cell_info(g, pc, cell);
     const int sl0 = tid * kPer;
     int nst = nv;  // this thread's stayers
-    if (kStep) {
+    float acc[32];
+#pragma unroll
+    for (int l = 0; l < 32; ++l) acc[l] = 0.f;
+    if (kSlotOnePass && kStep) {
+        // one pass: a stayer's moments are added as soon as it is moved
+        const float* coef = g.cellcoef + (size_t)cell * 48;
+        const int rot = lane >> 3;
+#pragma unroll 1
+        for (int jj = 0; jj < kPer; ++jj) {
+            const int j = (jj + rot) & (kPer - 1);
+            const int sl = sl0 + j;
+            PState<float> p;
+            int outcome = -1, dir = 0;
+            if (j < nv) {
+                p = load_slot(st, sl);
+                outcome = step32f<false, (kF & kPipeGather) != 0, (kF & kPipeDipole) != 0>(g, pc, sp, coef, ci, p,
+                                                                                           dir);
+                if (outcome == kStay) {
+                    store_slot(st, sl, p);
+                    if (kDep) add_moments<false>(acc, p);
+                }
+            }
+            if (outcome > 0) --nst;
+            leave_and_hole<false>(g, P, pc, outcome, dir, p, base + sl, cell, cstart, kDep, nmig, nrem);
+        }
+    } else if (kStep) {
         const float* coef = g.cellcoef + (size_t)cell * 48;
         // lane groups start at different slots of their run of 4: the words a
         // warp reads in one step fall in 32 different banks
@@ -576,11 +606,10 @@ __device__ __forceinline__ void push_slots(const Geom& g, const Pop<float>& P, c
         __syncwarp();
     }
     if (!kDep) return;
-    float acc[32];
-#pragma unroll
-    for (int l = 0; l < 32; ++l) acc[l] = 0.f;
+    if (!(kSlotOnePass && kStep)) {
 #pragma unroll 1
-    for (int j = 0; j < nv; ++j) add_moments<false>(acc, load_slot(st, sl0 + j));
+        for (int j = 0; j < nv; ++j) add_moments<false>(acc, load_slot(st, sl0 + j));
+    }
     const unsigned todo = __ballot_sync(0xffffffffu, nst > 0);
     const int prev_cell = __shfl_up_sync(0xffffffffu, cell, 1);
     unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev_cell != cell);
@@ -635,10 +664,17 @@ __device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& 
     }
     const int excl = incl - items;
     const int total = __shfl_sync(0xffffffffu, incl, 31);
-    for (;;) {
+    // kStaticItems: warp w takes items w + r, w + r + 11, ... (mod 11) with
+    // r turning from tile to tile; else items come from the stage's counter
+    const int wrot = (int)(((threadIdx.x >> 5) + 5u * (unsigned)tile) % (unsigned)kComputeWarps);
+    for (int jj = 0;; ++jj) {
         int j = 0;
-        if (lane == 0) j = atomicAdd(next_item, 1);
-        j = __shfl_sync(0xffffffffu, j, 0);
+        if (kStaticItems) {
+            j = wrot + jj * kComputeWarps;
+        } else {
+            if (lane == 0) j = atomicAdd(next_item, 1);
+            j = __shfl_sync(0xffffffffu, j, 0);
+        }
         if (j >= total) break;
         const unsigned owners = __ballot_sync(0xffffffffu, items > 0 && excl <= j);
         const int src = 31 - __clz(owners);

@@ -619,9 +619,23 @@ def run_ensemble(count, warmup, steps, local):
             lost += abs(int(c32["particles"]) - int(c64["particles"]))
         return np.array(rel), lost
 
-    # the FP32 error against FP64 over the configuration's 100 steps from the
+    sampler = ClockSampler(local)
+    ms32, ps32, launches32, pre = timed_batch(b32, warmup, steps, sampler)
+    ms64, ps64, _, _ = timed_batch(b64, warmup, steps, pre_steps=pre)
+    rel, lost = ke_rel()
+    st32, st64 = b32.stats(), b64.stats()
+    b32.close()
+    b64.close()
+    # the FP32 error against FP64 over the configuration's 100 steps from a
     # fresh start, every 20 steps (the FP32 batch's first steps are its push
     # autotuner's trials: ordinary steps of the simulation)
+    b32 = g.Batch(props, ensemble_config(abi.FP32))
+    b64 = g.Batch(props, ensemble_config(abi.FP64))
+    for i in range(count):
+        _, parts, counts, f, bc = make_universe(i)
+        for b in (b32, b64):
+            b.universe(i).upload_fields(f, bc, None)
+            b.universe(i).upload_particles(parts, counts)
     curve = []
     for k in range(5):
         b32.step(20)
@@ -629,15 +643,9 @@ def run_ensemble(count, warmup, steps, local):
         r, lost_k = ke_rel()
         curve.append({"step": 20 * (k + 1), "max": float(r.max()), "median": float(np.median(r)),
                       "particle_count_differences": lost_k})
-    sampler = ClockSampler(local)
-    ms32, ps32, launches32, pre = timed_batch(b32, warmup, steps, sampler, pre_steps=0)
-    ms64, ps64, _, _ = timed_batch(b64, warmup, steps, pre_steps=0)
-    pre = 100
-    rel, lost = ke_rel()
     worst = [dict(zip(("universe", "n", "ppc", "B", "E", "sigma", "ke_rel"),
                       (int(i),) + tuple(universe_params(int(i))) + (float(rel[i]),)))
              for i in np.argsort(rel)[::-1][:4]]
-    st32, st64 = b32.stats(), b64.stats()
     msp64, psp64 = timed_plain(b64, count, steps)
     msp32, psp32 = timed_plain(b32, count, steps)
     v32, v64 = ps32 / (ms32 * 1e-3), ps64 / (ms64 * 1e-3)
@@ -648,7 +656,7 @@ def run_ensemble(count, warmup, steps, local):
     return {"workload": ENS_WORKLOAD, "universes": count, "cells": cells, "particles": total,
             "steps": steps, "warmup": warmup, "setup_s": round(setup_s, 1),
             "fp32_batched": {"value": v32, "ms_per_step": ms32 / steps, "gpu_launches": int(launches32),
-                             "push_shape": shape32, "steps_before_timing": pre},
+                             "push_shape": shape32, "autotune_steps": pre},
             "fp64_batched": {"value": v64, "ms_per_step": ms64 / steps},
             "fp64_plain": {"value": vp64, "ms_per_step": msp64 / steps},
             "fp32_plain": {"value": vp32, "ms_per_step": msp32 / steps},
