@@ -46,6 +46,7 @@ _SIGNATURES = [
     ("ipic3d_gpu_upload_particles", C.c_int, [_vp, _vp, _vp, _vp]),
     ("ipic3d_gpu_reserve", C.c_int, [_vp, C.c_uint64]),
     ("ipic3d_gpu_init_uniform", C.c_int, [_vp, C.c_uint64]),
+    ("ipic3d_gpu_init_uniform_pos_normal_speed", C.c_int, [_vp, C.c_uint64, _vp, _vp, _vp, _vp]),
     ("ipic3d_gpu_particle_count", C.c_int, [_vp, C.POINTER(C.c_uint64)]),
     ("ipic3d_gpu_download_particles", C.c_int, [_vp, _vp, C.c_uint64, _vp, _vp]),
     ("ipic3d_gpu_cell_counts", C.c_int, [_vp, _vp]),
@@ -236,6 +237,15 @@ class Simulation:
         """initCells(uniform) of the reference's :U:N benchmark mode, made on
         the device with the reference's random streams (cell.h:638-697)."""
         _check(library().ipic3d_gpu_init_uniform(self._ctx, int(num_particles)))
+
+    def init_uniform_pos_normal_speed(self, num_particles, low, hig, mean, stddev):
+        """initCells with the .inp driver's distribution (cell.h:492-636):
+        per-cell counts on the host, the particles made on the device with
+        the reference's random streams (src/ipic3d.cxx:69-82 builds low, hig
+        as the middle 3/4 of the box, mean 0 and stddev v_mod)."""
+        arr = [np.ascontiguousarray(v, np.float64).reshape(3) for v in (low, hig, mean, stddev)]
+        _check(library().ipic3d_gpu_init_uniform_pos_normal_speed(self._ctx, int(num_particles),
+                                                                  *[abi.vptr(a) for a in arr]))
 
     def particle_count(self):
         n = C.c_uint64()

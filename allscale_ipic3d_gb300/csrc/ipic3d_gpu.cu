@@ -724,6 +724,89 @@ int init_uniform_impl(ipic3d_ctx* ctx, uint64_t n) {
     return IPIC3D_OK;
 }
 
+// initCells<uniform_pos_normal_speed> of the .inp driver (cell.h:492-636):
+// the per-cell counts on the host (phase 1: one sequential stream), every
+// particle on the device (phase 2: per-cell streams), stored like an
+// upload. One species: q = e, q/m = e / m_p (cell.h:502-503, 624-625); with
+// injection on, the injection species comes first, as an upload orders it.
+int init_normal_impl(ipic3d_ctx* ctx, uint64_t n, const double low[3], const double hig[3], const double mean[3],
+                     const double stddev[3]) {
+    const int64_t nc = ctx->ncells();
+    if (n > 0x7fffffffull) return fail(IPIC3D_E_INVALID, "%llu particles: at most 2^31 - 1", (unsigned long long)n);
+    for (int a = 0; a < 3; ++a)
+        if (!(low[a] < hig[a])) return fail(IPIC3D_E_INVALID, "position box: low must be below hig on every axis");
+    if (n > 0) {  // phase 1 must find positions inside the universe
+        const ipic3d_props& pr = ctx->props;
+        for (int a = 0; a < 3; ++a) {
+            const double top = pr.origin[a] + pr.size[a] * pr.cell_width[a];
+            if (!(hig[a] > pr.origin[a] && low[a] < top))
+                return fail(IPIC3D_E_INVALID, "position box does not meet the universe on axis %d", a);
+        }
+    }
+    std::vector<uint64_t> counts, zeros(nc, 0);
+    init_normal_counts(ctx->props, n, low, hig, counts);
+    std::vector<int64_t> off(nc + 1, 0);
+    for (int64_t c = 0; c < nc; ++c) off[c + 1] = off[c] + (int64_t)counts[c];
+    const double e = 1.602176565e-19, m = 1.672621777e-27;
+    const std::pair<double, double> proton{e, e / m};
+    std::vector<std::pair<double, double>> sp;
+    if (ctx->cfg.flags & IPIC3D_F_INJECT_LOW_X) sp.push_back({ctx->cfg.inject_q, ctx->cfg.inject_qom});
+    if (sp.empty() || sp[0] != proton) sp.push_back(proton);
+    drop_graph(ctx);
+    release_pops(ctx);
+    ctx->species = sp;
+    int rc;
+    for (auto& x : sp) {
+        const std::vector<uint64_t>& cnt = x == proton ? counts : zeros;
+        if (ctx->fp32) {
+            ctx->p32.emplace_back();
+            ctx->p32.back().q = x.first;
+            ctx->p32.back().qom = x.second;
+            if ((rc = alloc_pop(ctx, ctx->p32.back(), cnt, 0))) return rc;
+        } else {
+            ctx->p64.emplace_back();
+            ctx->p64.back().q = x.first;
+            ctx->p64.back().qom = x.second;
+            if ((rc = alloc_pop(ctx, ctx->p64.back(), cnt, 0))) return rc;
+        }
+    }
+    const uint64_t total = (uint64_t)off[nc];
+    if (total == 0) {
+        ctx->j_valid = false;
+        ctx->particles_hint = 0;
+        return IPIC3D_OK;
+    }
+    if ((rc = grow(reinterpret_cast<char*&>(ctx->st_parts), ctx->st_parts_cap, (size_t)total * sizeof(ipic3d_particle))))
+        return rc;
+    // per-cell counts (a temporary buffer) and offsets (the upload path's
+    // staging array) for the generator
+    uint64_t* d_count = nullptr;
+    CU(cudaMalloc(&d_count, (size_t)nc * sizeof(uint64_t)));
+    size_t cap_off = 0;
+    dfree(ctx->st_off);
+    if ((rc = grow(ctx->st_off, cap_off, (size_t)nc + 1))) {
+        cudaFree(d_count);
+        return rc;
+    }
+    cudaStream_t st = ctx->stream;
+    cudaError_t e1 = cudaMemcpyAsync(d_count, counts.data(), (size_t)nc * sizeof(uint64_t), cudaMemcpyHostToDevice, st);
+    if (e1 == cudaSuccess)
+        e1 = cudaMemcpyAsync(ctx->st_off, off.data(), (size_t)(nc + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st);
+    int nl = 0;
+    if (e1 == cudaSuccess)
+        nl = launch_init_normal(ctx->props, mean, stddev, proton.first, proton.second, d_count, ctx->st_off,
+                                ctx->st_parts, st);
+    if (e1 == cudaSuccess) e1 = cudaStreamSynchronize(st);
+    cudaFree(d_count);
+    if (e1 != cudaSuccess) return fail(IPIC3D_E_CUDA, "device initialisation: %s", cudaGetErrorString(e1));
+    if ((rc = check_launch(ctx, nl))) return rc;
+    rc = ctx->fp32 ? upload_fast(ctx, ctx->p32, nullptr, off, nullptr, true)
+                   : upload_fast(ctx, ctx->p64, nullptr, off, nullptr, true);
+    if (rc < 0) return rc;
+    if (rc > 0) return fail(IPIC3D_E_CUDA, "device initialisation: the scatter found an unexpected layout");
+    return IPIC3D_OK;
+}
+
 // Downloads every population, adding the pending particles to their cells.
 // The reference's record of a particle of population P in cell c from its
 // GPU state (cell-relative FP32 positions made absolute in FP64 with the
@@ -1497,6 +1580,16 @@ int ipic3d_gpu_init_uniform(ipic3d_ctx* ctx, uint64_t num_particles) {
     int rc = check_ctx(ctx);
     if (rc) return rc;
     if ((rc = init_uniform_impl(ctx, num_particles))) return rc;
+    CU(cudaStreamSynchronize(ctx->stream));
+    return IPIC3D_OK;
+}
+
+int ipic3d_gpu_init_uniform_pos_normal_speed(ipic3d_ctx* ctx, uint64_t num_particles, const double low[3],
+                                             const double hig[3], const double mean[3], const double stddev[3]) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!low || !hig || !mean || !stddev) return fail(IPIC3D_E_INVALID, "NULL argument");
+    if ((rc = init_normal_impl(ctx, num_particles, low, hig, mean, stddev))) return rc;
     CU(cudaStreamSynchronize(ctx->stream));
     return IPIC3D_OK;
 }

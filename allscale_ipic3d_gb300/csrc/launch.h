@@ -4,6 +4,9 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
+#include "../../include/ipic3d_types.h"
 #include "device.cuh"
 
 namespace ipg {
@@ -80,6 +83,13 @@ int launch_reduce_final(const double* partial, int blocks, int kq, double* out, 
 // grouped by cell), its random streams replayed on the device (init.cu)
 int launch_init_uniform(int sx, int sy, int sz, const double origin[3], const double w[3], uint64_t num_particles,
                         void* out, cudaStream_t st);
+// initCells<uniform_pos_normal_speed> (cell.h:492-636): phase 1 (per-cell
+// counts) on the host, phase 2 (every particle) on the device into `out`
+// (grouped by cell, cell c from record d_off[c]) (init.cu)
+void init_normal_counts(const ipic3d_props& pr, uint64_t num_particles, const double low[3], const double hig[3],
+                        std::vector<uint64_t>& counts);
+int launch_init_normal(const ipic3d_props& pr, const double mean[3], const double stddev[3], double q, double qom,
+                       const uint64_t* d_count, const int64_t* d_off, void* out, cudaStream_t st);
 
 // misc (ipic3d_gpu.cu)
 // records a status and message for ipic3d_gpu_last_error (this thread)

@@ -146,6 +146,19 @@ int ipic3d_gpu_reserve(ipic3d_ctx* ctx, uint64_t n);
  * values), electrons (q = -1, q/m = -25). Replaces the context's particles
  * as an upload does (ids = index in cell order). */
 int ipic3d_gpu_init_uniform(ipic3d_ctx* ctx, uint64_t num_particles);
+/* initCells(properties, num_particles, uniform_pos_normal_speed<>(low, hig,
+ * mean, stddev)) (cell.h:492-636), the .inp driver's universe
+ * (src/ipic3d.cxx:69-82, createUniverseFromDistribution universe.h:84-103):
+ * the per-cell counts from 100 pseudo-particles per cell of the position
+ * stream (phase 1, cell.h:505-590, on the host), then every cell's particles
+ * from its reseeded streams (phase 2, cell.h:596-632, on the device):
+ * positions uniform in the cell, velocities mean + stddev * a ziggurat
+ * normal variate per component, q = e, q/m = e / m_p. Bit-identical to the
+ * reference's particles. Replaces the context's particles as an upload does
+ * (ids = index in cell order). low / hig: the distribution's position box,
+ * which must meet the universe; mean / stddev: the velocity distribution. */
+int ipic3d_gpu_init_uniform_pos_normal_speed(ipic3d_ctx* ctx, uint64_t num_particles, const double low[3],
+                                             const double hig[3], const double mean[3], const double stddev[3]);
 /* Number of particles currently stored. */
 int ipic3d_gpu_particle_count(ipic3d_ctx* ctx, uint64_t* n);
 /* Downloads particles grouped by cell (row-major) with per-cell counts; the

@@ -81,3 +81,51 @@ def test_init_uniform_replaces_particles_and_zero():
     assert sim.particle_count() == 55
     assert sim.cell_counts().sum() == 55
     sim.close()
+
+
+@pytest.mark.parametrize("name", ["test", "tiny"])
+def test_init_inp_distribution_bit_identical(name):
+    """initCells with the .inp driver's uniform_pos_normal_speed distribution
+    (cell.h:492-636) on the device: every particle equals the compiled
+    reference's (the fixture's SHA-256 of its initial particles, grouped by
+    cell) and the oracle's restatement; FP32 storage holds the same values
+    within FP32 rounding."""
+    from common import golden_json, init_inp, props_from_dict, sha
+    run = golden_json("inp_runs.json")[name]
+    props = props_from_dict(run["props"])
+    ref_parts, ref_counts = init_inp(run)[1:]
+    args = [run["num_particles"], run["low"], run["hig"], run["mean"], run["stddev"]]
+    sim = gpu_sim(props, abi.Config.make(precision=abi.FP64, flags=abi.F_TRACK_IDS))
+    sim.init_uniform_pos_normal_speed(*args)
+    pg, cg, ig = sim.download_particles()
+    np.testing.assert_array_equal(cg, ref_counts)
+    assert sha(cg.astype(np.uint64)) == run["initial_counts_sha256"]
+    pg = pg[np.argsort(ig, kind="stable")]
+    assert sha(pg) == run["initial_particles_sha256"]
+    for f in ("position", "velocity", "q", "qom"):
+        np.testing.assert_array_equal(pg[f], ref_parts[f], err_msg=f)
+    sim.close()
+    sim = gpu_sim(props, abi.Config.make(precision=abi.FP32, flags=abi.F_TRACK_IDS))
+    sim.init_uniform_pos_normal_speed(*args)
+    p32, c32, i32 = sim.download_particles()
+    np.testing.assert_array_equal(c32, ref_counts)
+    p32 = p32[np.argsort(i32, kind="stable")]
+    w = np.array(props.cell_width)
+    assert (np.abs(p32["position"] - ref_parts["position"]) <= 1e-6 * w).all()
+    np.testing.assert_allclose(p32["velocity"], ref_parts["velocity"], rtol=1e-7, atol=0)
+    sim.close()
+
+
+def test_init_inp_distribution_arguments():
+    props = abi.Props.make(size=(4, 4, 4), cell_width=(1.0, 1.0, 1.0), dt=0.1)
+    sim = gpu_sim(props, abi.Config.make(precision=abi.FP64))
+    import allscale_ipic3d_gb300 as g
+    with pytest.raises(g.GpuPathError) as e:  # an empty position box
+        sim.init_uniform_pos_normal_speed(100, (1, 1, 1), (1, 2, 2), (0, 0, 0), (1, 1, 1))
+    assert e.value.status == abi.E_INVALID
+    with pytest.raises(g.GpuPathError) as e:  # a box outside the universe
+        sim.init_uniform_pos_normal_speed(100, (5, 5, 5), (6, 6, 6), (0, 0, 0), (1, 1, 1))
+    assert e.value.status == abi.E_INVALID
+    sim.init_uniform_pos_normal_speed(0, (0, 0, 0), (4, 4, 4), (0, 0, 0), (1, 1, 1))
+    assert sim.particle_count() == 0
+    sim.close()
