@@ -49,6 +49,7 @@ _SIGNATURES = [
     ("ipic3d_gpu_init_uniform_pos_normal_speed", C.c_int, [_vp, C.c_uint64, _vp, _vp, _vp, _vp]),
     ("ipic3d_gpu_particle_count", C.c_int, [_vp, C.POINTER(C.c_uint64)]),
     ("ipic3d_gpu_download_particles", C.c_int, [_vp, _vp, C.c_uint64, _vp, _vp]),
+    ("ipic3d_gpu_download_positions", C.c_int, [_vp, _vp, C.c_uint64, _vp]),
     ("ipic3d_gpu_cell_counts", C.c_int, [_vp, _vp]),
     ("ipic3d_gpu_upload_fields", C.c_int, [_vp, _vp, _vp, _vp]),
     ("ipic3d_gpu_download_fields", C.c_int, [_vp, _vp, _vp, _vp, _vp]),
@@ -270,6 +271,50 @@ class Simulation:
         i = np.zeros(n, np.uint32) if ids else None
         _check(library().ipic3d_gpu_download_particles(self._ctx, abi.vptr(p), n, abi.vptr(c), abi.vptr(i)))
         return p, c, i
+
+    def download_positions(self):
+        """(positions (n, 3), cell_counts): every particle's position in the
+        download order, packed on the device (24 bytes per particle cross
+        the host link)."""
+        c = self.cell_counts()
+        n = int(c.sum())
+        xyz = np.zeros((n, 3))
+        _check(library().ipic3d_gpu_download_positions(self._ctx, abi.vptr(xyz), n, abi.vptr(c)))
+        return xyz, c
+
+    def write_particle_positions(self, path):
+        """outputParticlePositions (cell.h:1400-1429): "x y z" per particle,
+        grouped by cell in row-major order, each number as the reference's
+        output stream prints a double (6 significant digits)."""
+        xyz, _ = self.download_positions()
+        with open(path, "w") as f:
+            f.write("".join("%g %g %g\n" % (x, y, z) for x, y, z in xyz.tolist()))
+
+    def write_field_grids(self, path):
+        """outputFieldGrids (field.h:464-530): the field grid ("i,j,k:[E]|[B]|
+        [Bext]" per node), then the BcField grid ("i,j,k:[Bc]" per cell),
+        each after its "[nx,ny,nz]" size line and followed by an empty line.
+        The reference writes both to the same file entry, one after the
+        other, so the second replaces the first; this writer does the same."""
+        f, b, _, _ = self.download_fields()
+
+        def vec(v):
+            return "[%g,%g,%g]" % tuple(v)
+
+        def grid(a, per_node):
+            nx, ny, nz = a.shape[:3]
+            lines = ["[%d,%d,%d]\n" % (nx, ny, nz)]
+            for i in range(nx):
+                for j in range(ny):
+                    for k in range(nz):
+                        lines.append("%d,%d,%d:%s\n" % (i, j, k, per_node(a[i, j, k].tolist())))
+            lines.append("\n")
+            return "".join(lines)
+
+        with open(path, "w") as out:
+            out.write(grid(f, lambda v: "%s|%s|%s" % (vec(v[0:3]), vec(v[3:6]), vec(v[6:9]))))
+        with open(path, "w") as out:
+            out.write(grid(b, vec))
 
     def cell_counts(self):
         c = np.zeros(self.ncells, np.uint64)

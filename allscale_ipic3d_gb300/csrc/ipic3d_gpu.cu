@@ -843,7 +843,7 @@ ipic3d_particle host_record(const ipic3d_ctx* ctx, const PopStore<T>& P, int64_t
 // 1's, and so on. `particles` / `ids` may be NULL (counts only).
 template <typename T>
 int download_device(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, ipic3d_particle* particles, uint64_t capacity,
-                    uint64_t* cell_counts, uint32_t* ids) {
+                    uint64_t* cell_counts, uint32_t* ids, double* xyz = nullptr) {
     const int64_t nc = ctx->ncells();
     const int npop = (int)pops.size();
     if (npop > kUploadMaxPops) return fail(IPIC3D_E_CAPACITY, "%d populations: at most %d", npop, kUploadMaxPops);
@@ -882,7 +882,7 @@ int download_device(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, ipic3d_part
         }
         if (cell_counts) cell_counts[c] = (uint64_t)(n - first);
     }
-    if ((!particles && !ids) || n == 0) return IPIC3D_OK;
+    if ((!particles && !ids && !xyz) || n == 0) return IPIC3D_OK;
     if ((uint64_t)n > capacity)
         return fail(IPIC3D_E_CAPACITY, "output capacity %llu too small", (unsigned long long)capacity);
     int rc;
@@ -906,6 +906,7 @@ int download_device(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, ipic3d_part
         P.qom[k] = S.qom;
     }
     P.dst = ctx->st_dst;
+    P.positions_only = xyz ? 1 : 0;
     UploadGeom g;
     g.ncells = (int)nc;
     g.sx = (int)ctx->props.size[0];
@@ -919,6 +920,7 @@ int download_device(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, ipic3d_part
     const int64_t chunk = std::max<int64_t>(1, (int64_t)(16u << 20) / (int64_t)sizeof(ipic3d_particle));
     cudaStream_t cs = ctx->copy_stream;
     auto* stage = static_cast<ipic3d_particle*>(ctx->st_parts);
+    auto* stage_xyz = static_cast<double*>(ctx->st_parts);  // positions only: 3 doubles per particle
     int nl = 0;
     for (int64_t c0 = 0; c0 < nc;) {
         const int64_t o0 = dst[(size_t)c0];
@@ -929,7 +931,10 @@ int download_device(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, ipic3d_part
         if (o1 > o0) {
             CU(cudaEventRecord(ctx->copy_ev, st));
             CU(cudaStreamWaitEvent(cs, ctx->copy_ev, 0));
-            if (particles)
+            if (xyz)
+                CU(cudaMemcpyAsync(xyz + 3 * o0, stage_xyz + 3 * o0, (size_t)(o1 - o0) * 3 * sizeof(double),
+                                   cudaMemcpyDeviceToHost, cs));
+            else if (particles)
                 CU(cudaMemcpyAsync(particles + o0, stage + o0, (size_t)(o1 - o0) * sizeof(ipic3d_particle),
                                    cudaMemcpyDeviceToHost, cs));
             if (ids)
@@ -948,6 +953,11 @@ int download_device(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, ipic3d_part
         for (const auto& m : pend[k]) {
             const size_t i = (size_t)k * nc + m.cell;
             const int64_t o = dst[i] + cnt[i] + rank[m.cell]++;
+            if (xyz) {
+                const ipic3d_particle r = host_record(ctx, pops[k], m.cell, m);
+                for (int a = 0; a < 3; ++a) xyz[3 * o + a] = r.position[a];
+                continue;
+            }
             if (particles) particles[o] = host_record(ctx, pops[k], m.cell, m);
             if (ids) ids[o] = m.id;
         }
@@ -1646,6 +1656,13 @@ int ipic3d_gpu_download_particles(ipic3d_ctx* ctx, ipic3d_particle* particles, u
     if (rc) return rc;
     if (ctx->fp32) return download_device(ctx, ctx->p32, particles, capacity, cell_counts, ids);
     return download_device(ctx, ctx->p64, particles, capacity, cell_counts, ids);
+}
+
+int ipic3d_gpu_download_positions(ipic3d_ctx* ctx, double* xyz, uint64_t capacity, uint64_t* cell_counts) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (ctx->fp32) return download_device(ctx, ctx->p32, nullptr, capacity, cell_counts, nullptr, xyz);
+    return download_device(ctx, ctx->p64, nullptr, capacity, cell_counts, nullptr, xyz);
 }
 
 int ipic3d_gpu_upload_fields(ipic3d_ctx* ctx, const double* field, const double* bcfield, const double* density) {

@@ -99,21 +99,8 @@ __device__ __forceinline__ float poly32(const float4& lo, const float4& hi, floa
     return fmaf(x, b, r);
 }
 
-// E and B of kN particles of one cell from the cell's polynomial
-// coefficients (kSmem: staged in shared memory; else read from global
-// memory): each 16-byte coefficient load serves all kN particles.
-template <bool kSmem, int kN>
-__device__ __forceinline__ void fields_n(const float* __restrict__ coef, const PState<float> (&p)[kN],
-                                         float (&E)[kN][6]) {
-    const float4* c4 = reinterpret_cast<const float4*>(coef);
-#pragma unroll
-    for (int q = 0; q < 6; ++q) {
-        const float4 lo = kSmem ? c4[2 * q] : __ldg(c4 + 2 * q);
-        const float4 hi = kSmem ? c4[2 * q + 1] : __ldg(c4 + 2 * q + 1);
-#pragma unroll
-        for (int i = 0; i < kN; ++i) E[i][q] = poly32(lo, hi, p[i].x, p[i].y, p[i].z);
-    }
-}
+// E and B of a particle from its cell's polynomial coefficients (kSmem:
+// staged in shared memory; else read from global memory).
 template <bool kSmem>
 __device__ __forceinline__ void fields_one(const float* __restrict__ coef, const PState<float>& a, float (&E)[6]) {
     const float4* c4 = reinterpret_cast<const float4*>(coef);

@@ -123,13 +123,6 @@ constexpr int kSlotWarps = kTileSlots / 128;        // slot mode: 128-slot slice
 // item mode (tiles of at most PushShape::item_cells cells, work items of
 // PushShape::item particles): the cells' field coefficients are staged
 constexpr int kItemMaxCells = 32;
-// particles per lane and warp step of the item mode's move pass
-constexpr int kItemPer = 1;
-// slot mode: moments added during the move pass (one pass) or in a second
-// pass over the stage (two passes, fewer live registers)
-constexpr bool kSlotOnePass = false;
-// item mode: items assigned to warps by a fixed rotation (no counter)
-constexpr bool kStaticItems = false;
 
 // Every member is a bulk-copy destination: 16-byte aligned offsets.
 struct __align__(16) PipeStage {
@@ -394,11 +387,10 @@ __device__ __forceinline__ void leave_and_hole(const Geom& g, const Pop<float>& 
 }
 
 // Item mode: the warp pushes particles [a, b) (tile-local slots, b - a <=
-// PushShape::item) of cell `cell`, kItemPer at a time per lane: lane l takes
-// a + l, a + l + 32, ... (with two per lane one coefficient load serves both
-// and their arithmetic interleaves). When no particle of the warp step needs
-// more than one Boris sub-cycle (the common case) the step is straight-line
-// code with the species' one-step constants. Stayers go back to the stage (the producer writes the whole
+// PushShape::item) of cell `cell`, lane l taking a + l, a + l + 32, ... When
+// no particle of a warp step needs more than one Boris sub-cycle (the common
+// case) the step is straight-line code with the species' one-step
+// constants. Stayers go back to the stage (the producer writes the whole
 // tile back with bulk stores); the slots of leavers and drops are cleared
 // (holes now). A second pass sums the stayers' cloud-in-cell moments and
 // flushes the cell once, with the stayer count from the first pass's
@@ -415,59 +407,33 @@ __device__ __forceinline__ void push_item(const Geom& g, const Pop<float>& P, co
     if (kStep) {
         const float k1 = sp.k1, ksub = sp.k_sub;
 #pragma unroll 1
-        for (int s0 = a; s0 < b; s0 += 32 * kItemPer) {
-            PState<float> p[kItemPer];
-            int sl[kItemPer], o[kItemPer], d[kItemPer];
-            float E[kItemPer][6];
-            float r[kItemPer];
-#pragma unroll
-            for (int i = 0; i < kItemPer; ++i) {
-                sl[i] = s0 + 32 * i + lane;
-                // a lane past the item works on a copy of slot a and keeps nothing
-                p[i] = load_slot(st, sl[i] < b ? sl[i] : a);
-            }
+        for (int s0 = a; s0 < b; s0 += 32) {
+            const int sl = s0 + lane;
+            // a lane past the item works on a copy of slot a and keeps nothing
+            PState<float> p = load_slot(st, sl < b ? sl : a);
+            float E[6];
             if (kGather) {
-                fields_n<true, kItemPer>(coef, p, E);
+                fields_one<true>(coef, p, E);
             } else {
 #pragma unroll
-                for (int i = 0; i < kItemPer; ++i)
-#pragma unroll
-                    for (int q = 0; q < 6; ++q) E[i][q] = 0.f;
+                for (int q = 0; q < 6; ++q) E[q] = 0.f;
             }
-#pragma unroll
-            for (int i = 0; i < kItemPer; ++i) {
-                if (kDipole) add_dipole(pc, ci, p[i], E[i]);
-                r[i] = sub_ratio(ksub, E[i]);
-            }
-            bool fast = true;
-#pragma unroll
-            for (int i = 0; i < kItemPer; ++i) fast = fast && r[i] < 1.f;
-            if (__all_sync(0xffffffffu, fast)) {
-#pragma unroll
-                for (int i = 0; i < kItemPer; ++i) boris32<1>(k1, pc.a1[0], pc.a1[1], pc.a1[2], E[i], p[i]);
-            } else {
-#pragma unroll
-                for (int i = 0; i < kItemPer; ++i) {
-                    if (r[i] < 1.f) boris32<1>(k1, pc.a1[0], pc.a1[1], pc.a1[2], E[i], p[i]);
-                    else boris_sub(pc, sp, r[i], E[i], p[i]);
-                }
-            }
-            bool any = false;
-#pragma unroll
-            for (int i = 0; i < kItemPer; ++i) {
-                d[i] = 0;
-                o[i] = export32(g, pc, ci, p[i], d[i]);
-                o[i] = sl[i] < b ? o[i] : -1;
-                if (o[i] == kStay) store_slot(st, sl[i], p[i]);
-                else if (kDep && o[i] > 0) clear_slot(st, sl[i]);
-                any = any || o[i] > 0;
-            }
-            if (__any_sync(0xffffffffu, any)) {
-#pragma unroll
-                for (int i = 0; i < kItemPer; ++i) {
-                    gone += __popc(__ballot_sync(0xffffffffu, o[i] > 0));
-                    leave_and_hole<true>(g, P, pc, o[i], d[i], p[i], base + sl[i], cell, cstart, kDep, nmig, nrem);
-                }
+            if (kDipole) add_dipole(pc, ci, p, E);
+            const float r = sub_ratio(ksub, E);
+            if (__all_sync(0xffffffffu, r < 1.f))
+                boris32<1>(k1, pc.a1[0], pc.a1[1], pc.a1[2], E, p);
+            else if (r < 1.f)
+                boris32<1>(k1, pc.a1[0], pc.a1[1], pc.a1[2], E, p);
+            else
+                boris_sub(pc, sp, r, E, p);
+            int dir = 0;
+            int o = export32(g, pc, ci, p, dir);
+            o = sl < b ? o : -1;
+            if (o == kStay) store_slot(st, sl, p);
+            else if (kDep && o > 0) clear_slot(st, sl);
+            if (__any_sync(0xffffffffu, o > 0)) {
+                gone += __popc(__ballot_sync(0xffffffffu, o > 0));
+                leave_and_hole<true>(g, P, pc, o, dir, p, base + sl, cell, cstart, kDep, nmig, nrem);
             }
         }
         __syncwarp();
@@ -557,32 +523,7 @@ __device__ __forceinline__ void push_slots(const Geom& g, const Pop<float>& P, c
     const CellInfo ci = cell_info(g, pc, cell);
     const int sl0 = tid * kPer;
     int nst = nv;  // this thread's stayers
-    float acc[32];
-#pragma unroll
-    for (int l = 0; l < 32; ++l) acc[l] = 0.f;
-    if (kSlotOnePass && kStep) {
-        // one pass: a stayer's moments are added as soon as it is moved
-        const float* coef = g.cellcoef + (size_t)cell * 48;
-        const int rot = lane >> 3;
-#pragma unroll 1
-        for (int jj = 0; jj < kPer; ++jj) {
-            const int j = (jj + rot) & (kPer - 1);
-            const int sl = sl0 + j;
-            PState<float> p;
-            int outcome = -1, dir = 0;
-            if (j < nv) {
-                p = load_slot(st, sl);
-                outcome = step32f<false, (kF & kPipeGather) != 0, (kF & kPipeDipole) != 0>(g, pc, sp, coef, ci, p,
-                                                                                           dir);
-                if (outcome == kStay) {
-                    store_slot(st, sl, p);
-                    if (kDep) add_moments<false>(acc, p);
-                }
-            }
-            if (outcome > 0) --nst;
-            leave_and_hole<false>(g, P, pc, outcome, dir, p, base + sl, cell, cstart, kDep, nmig, nrem);
-        }
-    } else if (kStep) {
+    if (kStep) {
         const float* coef = g.cellcoef + (size_t)cell * 48;
         // lane groups start at different slots of their run of 4: the words a
         // warp reads in one step fall in 32 different banks
@@ -606,10 +547,11 @@ __device__ __forceinline__ void push_slots(const Geom& g, const Pop<float>& P, c
         __syncwarp();
     }
     if (!kDep) return;
-    if (!(kSlotOnePass && kStep)) {
+    float acc[32];
+#pragma unroll
+    for (int l = 0; l < 32; ++l) acc[l] = 0.f;
 #pragma unroll 1
-        for (int j = 0; j < nv; ++j) add_moments<false>(acc, load_slot(st, sl0 + j));
-    }
+    for (int j = 0; j < nv; ++j) add_moments<false>(acc, load_slot(st, sl0 + j));
     const unsigned todo = __ballot_sync(0xffffffffu, nst > 0);
     const int prev_cell = __shfl_up_sync(0xffffffffu, cell, 1);
     unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev_cell != cell);
@@ -664,17 +606,10 @@ __device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& 
     }
     const int excl = incl - items;
     const int total = __shfl_sync(0xffffffffu, incl, 31);
-    // kStaticItems: warp w takes items w + r, w + r + 11, ... (mod 11) with
-    // r turning from tile to tile; else items come from the stage's counter
-    const int wrot = (int)(((threadIdx.x >> 5) + 5u * (unsigned)tile) % (unsigned)kComputeWarps);
-    for (int jj = 0;; ++jj) {
+    for (;;) {
         int j = 0;
-        if (kStaticItems) {
-            j = wrot + jj * kComputeWarps;
-        } else {
-            if (lane == 0) j = atomicAdd(next_item, 1);
-            j = __shfl_sync(0xffffffffu, j, 0);
-        }
+        if (lane == 0) j = atomicAdd(next_item, 1);
+        j = __shfl_sync(0xffffffffu, j, 0);
         if (j >= total) break;
         const unsigned owners = __ballot_sync(0xffffffffu, items > 0 && excl <= j);
         const int src = 31 - __clz(owners);

@@ -260,6 +260,13 @@ __global__ void k_pack_cells(PackPops<T> P, UploadGeom g, int c0, int c1, ipic3d
                 r.position[1] = (double)P.y[k][s];
                 r.position[2] = (double)P.z[k][s];
             }
+            if (P.positions_only) {
+                double* o = reinterpret_cast<double*>(out) + 3 * (d0 + i);
+                o[0] = r.position[0];
+                o[1] = r.position[1];
+                o[2] = r.position[2];
+                continue;
+            }
             r.velocity[0] = (double)P.u[k][s];
             r.velocity[1] = (double)P.v[k][s];
             r.velocity[2] = (double)P.w[k][s];

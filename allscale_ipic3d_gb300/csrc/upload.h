@@ -74,6 +74,7 @@ struct PackPops {
     const int32_t* count[kUploadMaxPops];
     const int64_t* dst;  // [npop][ncells]
     double q[kUploadMaxPops], qom[kUploadMaxPops];
+    int positions_only;  // write the three position doubles of each particle (24 bytes), not its record
 };
 // Cells [c0, c1): one warp per cell; `out` (records) and `out_ids` (may be
 // null) are device buffers indexed by the output index.

@@ -166,6 +166,13 @@ int ipic3d_gpu_particle_count(ipic3d_ctx* ctx, uint64_t* n);
  * cell_counts and ids may be NULL. */
 int ipic3d_gpu_download_particles(ipic3d_ctx* ctx, ipic3d_particle* particles, uint64_t capacity,
                                   uint64_t* cell_counts, uint32_t* ids);
+/* The positions of every particle (3 doubles each, x y z), in the order of
+ * ipic3d_gpu_download_particles (grouped by cell): what
+ * outputParticlePositions (cell.h:1400-1429) writes. Packed on the device,
+ * so only these 24 bytes per particle cross the host link. capacity is in
+ * particles; cell_counts (may be NULL) receives the per-cell counts.
+ * xyz == NULL returns the counts only. */
+int ipic3d_gpu_download_positions(ipic3d_ctx* ctx, double* xyz, uint64_t capacity, uint64_t* cell_counts);
 /* Per-cell particle counts (outputNumberOfParticlesPerCell, cell.h:1360). */
 int ipic3d_gpu_cell_counts(ipic3d_ctx* ctx, uint64_t* cell_counts);
 

@@ -124,5 +124,7 @@ def load_reference():
         lib.ref_trilinear.restype = C.c_double
         lib.ref_conserved.argtypes = [vp, vp, vp, vp, vp]
         lib.ref_init_from_inp.argtypes = [C.c_char_p, vp, vp, vp, C.c_uint64, vp, vp, vp]
+        lib.ref_write_particle_positions.argtypes = [vp, vp, vp, C.c_char_p]
+        lib.ref_write_field_grids.argtypes = [vp, vp, vp, C.c_char_p]
         _ref = lib
     return _ref

@@ -268,6 +268,26 @@ int ref_conserved(const ipic3d_props* props, const ipic3d_particle* in, const ui
     return 0;
 }
 
+// outputParticlePositions (cell.h:1400-1429) of the given particles (grouped
+// by cell) into the file `path`.
+int ref_write_particle_positions(const ipic3d_props* props, const ipic3d_particle* in, const uint64_t* counts,
+                                 const char* path) {
+    Universe u(to_props(props));
+    fill_cells(u.cells, in, counts);
+    outputParticlePositions(u.cells, std::string(path));
+    return 0;
+}
+
+// outputFieldGrids (field.h:464-530) of the given Field ((size+3)^3 x 9) and
+// BcField ((size+2)^3 x 3) into the file `path`.
+int ref_write_field_grids(const ipic3d_props* props, const double* field, const double* bcfield, const char* path) {
+    Universe u(to_props(props));
+    grid_in(u.field, const_cast<double*>(field), 9);
+    grid_in(u.bcfield, const_cast<double*>(bcfield), 3);
+    outputFieldGrids(u.field, u.bcfield, std::string(path));
+    return 0;
+}
+
 // The .inp driver's set-up (src/ipic3d.cxx:30-83): parse, apply the driver's
 // overrides, build the universe with createUniverseFromDistribution. Returns
 // props, the field grid, the particles grouped by cell and ncycles. Call with

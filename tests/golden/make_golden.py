@@ -18,6 +18,8 @@ Fixtures (all small):
   moves_small.npz    seeded scenarios through simulateSteps with the default
                      policies (mover + export + import): inputs and outputs.
   project_small.npz  projectToDensityField over all nodes.
+  dumps_small.npz    outputParticlePositions and outputFieldGrids text of a
+                     small universe (the reference's writers).
   fields_small.npz   updateFieldsOnBoundaries, two-phase leapfrog, forward
                      solver at single nodes.
   aggregate_small.npz  aggregateDensityContributions over all nodes of two
@@ -273,6 +275,27 @@ def aggregate_small():
     np.savez_compressed(os.path.join(HERE, "aggregate_small.npz"), **out)
 
 
+def dumps_small():
+    """The reference's text dumps -- outputParticlePositions (cell.h:1400-1429)
+    and outputFieldGrids (field.h:464-530) -- of a small universe with
+    particles over several orders of magnitude and random fields."""
+    import tempfile
+    ref = oracle.load_reference()
+    props, parts, counts = make_scenario(71, (4, 3, 5), (0.5, 2.0, 1e-3), (-1.0, 3.0, 1e4), 0.1, 6, 0.3,
+                                         ragged=True)
+    rng = np.random.default_rng(72)
+    f = rng.normal(0.0, 1.0, abi.field_shape(props)) * 10.0 ** rng.integers(-8, 8, abi.field_shape(props))
+    bc = rng.normal(0.0, 1.0, abi.bcfield_shape(props))
+    with tempfile.TemporaryDirectory() as d:
+        pp, pf = os.path.join(d, "positions.txt"), os.path.join(d, "fields.txt")
+        ref.ref_write_particle_positions(C.byref(props), abi.vptr(parts), abi.vptr(counts), pp.encode())
+        ref.ref_write_field_grids(C.byref(props), abi.vptr(f), abi.vptr(bc), pf.encode())
+        pos_text, field_text = open(pp, "rb").read(), open(pf, "rb").read()
+    np.savez_compressed(os.path.join(HERE, "dumps_small.npz"), props=props_vec(props), parts=parts, counts=counts,
+                        field=f, bcfield=bc, positions_txt=np.frombuffer(pos_text, np.uint8),
+                        field_grids_txt=np.frombuffer(field_text, np.uint8))
+
+
 def fields_small():
     rng = np.random.default_rng(21)
     out = {}
@@ -306,3 +329,4 @@ if __name__ == "__main__":
     inp_runs()
     tracer_runs()
     aggregate_small()
+    dumps_small()

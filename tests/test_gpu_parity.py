@@ -346,3 +346,38 @@ def test_heavy_migration_placement(precision, graph):
             assert np.abs(d).max() < 1e-5, np.abs(d).max()
             np.testing.assert_allclose(pa["velocity"], pb["velocity"], rtol=0, atol=1e-6)
     sim.close()
+
+
+@pytest.mark.parametrize("precision", [abi.FP64, abi.FP32])
+def test_dumps_byte_identical_to_reference_writers(tmp_path, precision):
+    """outputParticlePositions (cell.h:1400-1429) and outputFieldGrids
+    (field.h:464-530) from the device: the positions packed on the device (24
+    bytes per particle over the link) and the grids, written in the
+    reference's text format, equal the reference's own writers' files
+    (fixture from the compiled reference) byte for byte. FP32 storage keeps
+    positions cell-relative; printed at 6 significant digits they agree with
+    the FP64 ones except where FP32 rounding crosses a printed digit."""
+    g = golden_npz("dumps_small.npz")
+    props = props_from_vec(g["props"])
+    sim = gpu_sim(props, abi.Config.make(precision=precision))
+    sim.upload_fields(g["field"], g["bcfield"], None)
+    sim.upload_particles(g["parts"], g["counts"])
+    xyz, c = sim.download_positions()
+    np.testing.assert_array_equal(c, g["counts"])
+    if precision == abi.FP64:
+        np.testing.assert_array_equal(xyz, g["parts"]["position"])
+    pos = tmp_path / "positions.txt"
+    grids = tmp_path / "fields.txt"
+    sim.write_particle_positions(str(pos))
+    sim.write_field_grids(str(grids))
+    want_pos = bytes(g["positions_txt"])
+    got_pos = pos.read_bytes()
+    if precision == abi.FP64:
+        assert got_pos == want_pos
+    else:
+        a, b = got_pos.decode().split("\n"), want_pos.decode().split("\n")
+        assert len(a) == len(b)
+        np.testing.assert_allclose(np.array([list(map(float, l.split())) for l in a if l]),
+                                   np.array([list(map(float, l.split())) for l in b if l]), rtol=1e-5)
+    assert grids.read_bytes() == bytes(g["field_grids_txt"])
+    sim.close()
