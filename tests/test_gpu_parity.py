@@ -356,7 +356,11 @@ def test_dumps_byte_identical_to_reference_writers(tmp_path, precision):
     reference's text format, equal the reference's own writers' files
     (fixture from the compiled reference) byte for byte. FP32 storage keeps
     positions cell-relative; printed at 6 significant digits they agree with
-    the FP64 ones except where FP32 rounding crosses a printed digit."""
+    the FP64 ones except where FP32 rounding crosses a printed digit. The
+    universe has one species: the device keeps a cell's particles of one
+    species in upload order (particles of different species are grouped by
+    species within a cell, so the reference's writer on a mixed-species cell
+    prints the same lines in another order)."""
     g = golden_npz("dumps_small.npz")
     props = props_from_vec(g["props"])
     sim = gpu_sim(props, abi.Config.make(precision=precision))
