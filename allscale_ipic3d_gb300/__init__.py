@@ -50,6 +50,8 @@ _SIGNATURES = [
     ("ipic3d_gpu_particle_count", C.c_int, [_vp, C.POINTER(C.c_uint64)]),
     ("ipic3d_gpu_download_particles", C.c_int, [_vp, _vp, C.c_uint64, _vp, _vp]),
     ("ipic3d_gpu_download_positions", C.c_int, [_vp, _vp, C.c_uint64, _vp]),
+    ("ipic3d_gpu_download_particles_async", C.c_int, [_vp, _vp, C.c_uint64, _vp, _vp]),
+    ("ipic3d_gpu_download_wait", C.c_int, [_vp]),
     ("ipic3d_gpu_cell_counts", C.c_int, [_vp, _vp]),
     ("ipic3d_gpu_upload_fields", C.c_int, [_vp, _vp, _vp, _vp]),
     ("ipic3d_gpu_download_fields", C.c_int, [_vp, _vp, _vp, _vp, _vp]),
@@ -271,6 +273,20 @@ class Simulation:
         i = np.zeros(n, np.uint32) if ids else None
         _check(library().ipic3d_gpu_download_particles(self._ctx, abi.vptr(p), n, abi.vptr(c), abi.vptr(i)))
         return p, c, i
+
+    def download_particles_async(self, out, ids=None):
+        """Starts a download into caller-owned host arrays `out` =
+        (particles, cell_counts) (pinned memory for full speed): the counts
+        are filled at once, the particles (and `ids`, an array or None) once
+        download_wait() returns. Meanwhile other calls may run, an upload
+        among them (its copies use the link's other direction)."""
+        p, c = out
+        _check(library().ipic3d_gpu_download_particles_async(self._ctx, abi.vptr(p), len(p), abi.vptr(c),
+                                                             abi.vptr(ids)))
+        return int(c.sum())
+
+    def download_wait(self):
+        _check(library().ipic3d_gpu_download_wait(self._ctx))
 
     def download_positions(self):
         """(positions (n, 3), cell_counts): every particle's position in the

@@ -192,6 +192,24 @@ struct ipic3d_ctx {
     int* st_flags = nullptr;            // fused upload: unknown species, cell overflow
     int64_t* st_dst = nullptr;          // download: output index of each (population, cell)
     size_t st_dst_cap = 0;
+    // the download's own staging buffers, copy stream and completion state
+    // (an asynchronous download's copies may run while the next upload's do)
+    void* st_dl = nullptr;
+    size_t st_dl_cap = 0;
+    uint32_t* st_dl_ids = nullptr;
+    size_t st_dl_ids_cap = 0;
+    cudaStream_t dl_stream = nullptr;
+    cudaEvent_t dl_ev = nullptr;
+    struct DlFill {                     // a waiting particle, written after the copies
+        int64_t at;
+        ipic3d_particle rec;
+        uint32_t id;
+    };
+    std::vector<DlFill> dl_fill;
+    ipic3d_particle* dl_parts = nullptr;
+    uint32_t* dl_ids = nullptr;
+    double* dl_xyz = nullptr;
+    bool dl_busy = false;
     cudaStream_t copy_stream = nullptr; // copies of the chunked upload and download
     cudaEvent_t copy_ev = nullptr;
     // second stream of a step: kernels that run beside the push / placement
@@ -841,9 +859,28 @@ ipic3d_particle host_record(const ipic3d_ctx* ctx, const PopStore<T>& P, int64_t
 // are filled in on the host. Order per cell: population 0's particles in
 // slot order, then its waiting particles in list order, then population
 // 1's, and so on. `particles` / `ids` may be NULL (counts only).
+// Completes a download: waits for its copies, then writes the waiting
+// particles into their places.
+int download_finish(ipic3d_ctx* ctx) {
+    if (!ctx->dl_busy) return IPIC3D_OK;
+    ctx->dl_busy = false;
+    CU(cudaStreamSynchronize(ctx->dl_stream));
+    for (const auto& f : ctx->dl_fill) {
+        if (ctx->dl_xyz)
+            for (int a = 0; a < 3; ++a) ctx->dl_xyz[3 * f.at + a] = f.rec.position[a];
+        else if (ctx->dl_parts)
+            ctx->dl_parts[f.at] = f.rec;
+        if (ctx->dl_ids) ctx->dl_ids[f.at] = f.id;
+    }
+    ctx->dl_fill.clear();
+    return IPIC3D_OK;
+}
+
 template <typename T>
 int download_device(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, ipic3d_particle* particles, uint64_t capacity,
-                    uint64_t* cell_counts, uint32_t* ids, double* xyz = nullptr) {
+                    uint64_t* cell_counts, uint32_t* ids, double* xyz = nullptr, bool async = false) {
+    int rc = download_finish(ctx);  // one download at a time
+    if (rc) return rc;
     const int64_t nc = ctx->ncells();
     const int npop = (int)pops.size();
     if (npop > kUploadMaxPops) return fail(IPIC3D_E_CAPACITY, "%d populations: at most %d", npop, kUploadMaxPops);
@@ -885,13 +922,12 @@ int download_device(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, ipic3d_part
     if ((!particles && !ids && !xyz) || n == 0) return IPIC3D_OK;
     if ((uint64_t)n > capacity)
         return fail(IPIC3D_E_CAPACITY, "output capacity %llu too small", (unsigned long long)capacity);
-    int rc;
-    if ((rc = grow(reinterpret_cast<char*&>(ctx->st_parts), ctx->st_parts_cap, (size_t)n * sizeof(ipic3d_particle))))
+    if ((rc = grow(reinterpret_cast<char*&>(ctx->st_dl), ctx->st_dl_cap, (size_t)n * sizeof(ipic3d_particle))))
         return rc;
-    if (ids && (rc = grow(ctx->st_ids, ctx->st_ids_cap, (size_t)n))) return rc;
+    if (ids && (rc = grow(ctx->st_dl_ids, ctx->st_dl_ids_cap, (size_t)n))) return rc;
     if ((rc = grow(ctx->st_dst, ctx->st_dst_cap, dst.size()))) return rc;
-    if (!ctx->copy_stream) CU(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
-    if (!ctx->copy_ev) CU(cudaEventCreateWithFlags(&ctx->copy_ev, cudaEventDisableTiming));
+    if (!ctx->dl_stream) CU(cudaStreamCreateWithFlags(&ctx->dl_stream, cudaStreamNonBlocking));
+    if (!ctx->dl_ev) CU(cudaEventCreateWithFlags(&ctx->dl_ev, cudaEventDisableTiming));
     CU(cudaMemcpyAsync(ctx->st_dst, dst.data(), dst.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
     PackPops<T> P{};
     P.npop = npop;
@@ -918,19 +954,19 @@ int download_device(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, ipic3d_part
     }
     // chunks of about 16 MB of records, cut at cell boundaries
     const int64_t chunk = std::max<int64_t>(1, (int64_t)(16u << 20) / (int64_t)sizeof(ipic3d_particle));
-    cudaStream_t cs = ctx->copy_stream;
-    auto* stage = static_cast<ipic3d_particle*>(ctx->st_parts);
-    auto* stage_xyz = static_cast<double*>(ctx->st_parts);  // positions only: 3 doubles per particle
+    cudaStream_t cs = ctx->dl_stream;
+    auto* stage = static_cast<ipic3d_particle*>(ctx->st_dl);
+    auto* stage_xyz = static_cast<double*>(ctx->st_dl);  // positions only: 3 doubles per particle
     int nl = 0;
     for (int64_t c0 = 0; c0 < nc;) {
         const int64_t o0 = dst[(size_t)c0];
         int64_t c1 = c0 + 1;
         while (c1 < nc && dst[(size_t)c1] - o0 < chunk) ++c1;
         const int64_t o1 = c1 < nc ? dst[(size_t)c1] : n;
-        nl += launch_pack_cells<T>(P, g, (int)c0, (int)c1, stage, ids ? ctx->st_ids : nullptr, st);
+        nl += launch_pack_cells<T>(P, g, (int)c0, (int)c1, stage, ids ? ctx->st_dl_ids : nullptr, st);
         if (o1 > o0) {
-            CU(cudaEventRecord(ctx->copy_ev, st));
-            CU(cudaStreamWaitEvent(cs, ctx->copy_ev, 0));
+            CU(cudaEventRecord(ctx->dl_ev, st));
+            CU(cudaStreamWaitEvent(cs, ctx->dl_ev, 0));
             if (xyz)
                 CU(cudaMemcpyAsync(xyz + 3 * o0, stage_xyz + 3 * o0, (size_t)(o1 - o0) * 3 * sizeof(double),
                                    cudaMemcpyDeviceToHost, cs));
@@ -938,31 +974,29 @@ int download_device(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, ipic3d_part
                 CU(cudaMemcpyAsync(particles + o0, stage + o0, (size_t)(o1 - o0) * sizeof(ipic3d_particle),
                                    cudaMemcpyDeviceToHost, cs));
             if (ids)
-                CU(cudaMemcpyAsync(ids + o0, ctx->st_ids + o0, (size_t)(o1 - o0) * sizeof(uint32_t),
+                CU(cudaMemcpyAsync(ids + o0, ctx->st_dl_ids + o0, (size_t)(o1 - o0) * sizeof(uint32_t),
                                    cudaMemcpyDeviceToHost, cs));
         }
         c0 = c1;
     }
     if ((rc = check_launch(ctx, nl))) return rc;
-    CU(cudaStreamSynchronize(cs));
-    CU(cudaStreamSynchronize(st));
-    // the waiting particles, into the gaps after each cell's slots
+    // the waiting particles go into the gaps after each cell's slots once
+    // the copies have landed
+    ctx->dl_fill.clear();
     for (int k = 0; k < npop; ++k) {
         if (pend[k].empty()) continue;
         std::vector<int32_t> rank(nc, 0);
         for (const auto& m : pend[k]) {
             const size_t i = (size_t)k * nc + m.cell;
-            const int64_t o = dst[i] + cnt[i] + rank[m.cell]++;
-            if (xyz) {
-                const ipic3d_particle r = host_record(ctx, pops[k], m.cell, m);
-                for (int a = 0; a < 3; ++a) xyz[3 * o + a] = r.position[a];
-                continue;
-            }
-            if (particles) particles[o] = host_record(ctx, pops[k], m.cell, m);
-            if (ids) ids[o] = m.id;
+            ctx->dl_fill.push_back({dst[i] + cnt[i] + rank[m.cell]++, host_record(ctx, pops[k], m.cell, m), m.id});
         }
     }
-    return IPIC3D_OK;
+    ctx->dl_parts = particles;
+    ctx->dl_ids = ids;
+    ctx->dl_xyz = xyz;
+    ctx->dl_busy = true;
+    if (async) return IPIC3D_OK;
+    return download_finish(ctx);
 }
 
 // Device re-layout of one population: new per-cell capacities from the
@@ -1410,6 +1444,7 @@ int destroy_impl(ipic3d_ctx* ctx) {
     if (!ctx) return IPIC3D_OK;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->dl_stream) cudaStreamSynchronize(ctx->dl_stream);
     drop_graph(ctx);
     release_pops(ctx);
     dfree(ctx->field);
@@ -1434,6 +1469,10 @@ int destroy_impl(ipic3d_ctx* ctx) {
     dfree(ctx->st_dst);
     if (ctx->copy_ev) cudaEventDestroy(ctx->copy_ev);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    dfree(ctx->st_dl);
+    dfree(ctx->st_dl_ids);
+    if (ctx->dl_ev) cudaEventDestroy(ctx->dl_ev);
+    if (ctx->dl_stream) cudaStreamDestroy(ctx->dl_stream);
     for (auto& e : ctx->aux_ev)
         if (e) cudaEventDestroy(e);
     if (ctx->aux_stream) cudaStreamDestroy(ctx->aux_stream);
@@ -1656,6 +1695,20 @@ int ipic3d_gpu_download_particles(ipic3d_ctx* ctx, ipic3d_particle* particles, u
     if (rc) return rc;
     if (ctx->fp32) return download_device(ctx, ctx->p32, particles, capacity, cell_counts, ids);
     return download_device(ctx, ctx->p64, particles, capacity, cell_counts, ids);
+}
+
+int ipic3d_gpu_download_particles_async(ipic3d_ctx* ctx, ipic3d_particle* particles, uint64_t capacity,
+                                        uint64_t* cell_counts, uint32_t* ids) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (ctx->fp32) return download_device(ctx, ctx->p32, particles, capacity, cell_counts, ids, nullptr, true);
+    return download_device(ctx, ctx->p64, particles, capacity, cell_counts, ids, nullptr, true);
+}
+
+int ipic3d_gpu_download_wait(ipic3d_ctx* ctx) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    return download_finish(ctx);
 }
 
 int ipic3d_gpu_download_positions(ipic3d_ctx* ctx, double* xyz, uint64_t capacity, uint64_t* cell_counts) {

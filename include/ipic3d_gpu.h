@@ -166,6 +166,20 @@ int ipic3d_gpu_particle_count(ipic3d_ctx* ctx, uint64_t* n);
  * cell_counts and ids may be NULL. */
 int ipic3d_gpu_download_particles(ipic3d_ctx* ctx, ipic3d_particle* particles, uint64_t capacity,
                                   uint64_t* cell_counts, uint32_t* ids);
+/* No counterpart in the reference. ipic3d_gpu_download_particles in two
+ * halves, so that a caller that moves the whole state every step can
+ * overlap this step's device-to-host copies with the next upload's
+ * host-to-device copies (the host link is full duplex): this call fills
+ * cell_counts, packs the records on the device and enqueues their copies,
+ * then returns; the particles / ids buffers are complete only after
+ * ipic3d_gpu_download_wait. Until then they must stay allocated and unread.
+ * Other calls may run meanwhile (an upload, a step); the next download (of
+ * either kind) and ipic3d_gpu_destroy wait for this one first. */
+int ipic3d_gpu_download_particles_async(ipic3d_ctx* ctx, ipic3d_particle* particles, uint64_t capacity,
+                                        uint64_t* cell_counts, uint32_t* ids);
+/* Waits for the copies of an asynchronous download and completes its
+ * buffers (returns at once when none is in flight). */
+int ipic3d_gpu_download_wait(ipic3d_ctx* ctx);
 /* The positions of every particle (3 doubles each, x y z), in the order of
  * ipic3d_gpu_download_particles (grouped by cell): what
  * outputParticlePositions (cell.h:1400-1429) writes. Packed on the device,

@@ -385,3 +385,31 @@ def test_dumps_byte_identical_to_reference_writers(tmp_path, precision):
                                    np.array([list(map(float, l.split())) for l in b if l]), rtol=1e-5)
     assert grids.read_bytes() == bytes(g["field_grids_txt"])
     sim.close()
+
+
+def test_async_download_overlaps_an_upload():
+    """ipic3d_gpu_download_particles_async: the counts at once, the particles
+    after ipic3d_gpu_download_wait, equal to the synchronous download of the
+    same state even when an upload of other particles runs in between (the
+    copies use separate staging buffers and streams)."""
+    props, parts, counts = scenario(91, (6, 5, 4), dt=0.1, ppc=20, vscale=0.3, species=((1.0, 1.0), (-1.0, -2.0)),
+                                    ragged=True)
+    _, parts2, counts2 = scenario(92, (6, 5, 4), dt=0.1, ppc=12, vscale=0.3, species=((1.0, 1.0), (-1.0, -2.0)))
+    cfg = abi.Config.make(precision=abi.FP32, mover=abi.MOVER_FIELD, projector=abi.PROJECT_CIC, bc=abi.BC_PERIODIC)
+    sim = gpu_sim(props, cfg)
+    sim.upload_particles(parts, counts)
+    sim.step(3)
+    want, want_c, _ = sim.download_particles(ids=False)
+    out = np.zeros(len(want) + 10, abi.PARTICLE_DTYPE)
+    oc = np.zeros(props.ncells, np.uint64)
+    n = sim.download_particles_async((out, oc))
+    assert n == len(want)
+    np.testing.assert_array_equal(oc, want_c)
+    sim.upload_particles(parts2, counts2)  # runs while the copies are in flight
+    sim.download_wait()
+    assert out[:n].tobytes() == want.tobytes()
+    got, got_c, _ = sim.download_particles(ids=False)
+    np.testing.assert_array_equal(got_c, counts2)
+    sim.step(2)
+    sim.download_particles_async((out, oc))
+    sim.close()  # waits for the copies in flight
