@@ -187,7 +187,9 @@ struct ipic3d_ctx {
     uint8_t* st_sid = nullptr;
     size_t st_sid_cap = 0;
     int64_t* st_off = nullptr;
+    size_t st_off_cap = 0;
     int32_t* st_cnt = nullptr;
+    size_t st_cnt_cap = 0;
     int* st_unknown = nullptr;
     int* st_flags = nullptr;            // fused upload: unknown species, cell overflow
     int64_t* st_dst = nullptr;          // download: output index of each (population, cell)
@@ -536,12 +538,13 @@ int upload_fast(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, const ipic3d_pa
     for (auto& P : pops)
         if ((int64_t)P.h_start.size() != nc + 1) return 2;
     int rc;
-    size_t cap_off = 0, cap_f = 0;
+    size_t cap_f = 0;
+    // staging buffers keep their capacity: a cudaFree here would wait for
+    // every stream of the device, an asynchronous download's copies included
     if ((rc = grow(reinterpret_cast<char*&>(ctx->st_parts), ctx->st_parts_cap, (size_t)n * sizeof(ipic3d_particle))))
         return rc;
     if (ids && (rc = grow(ctx->st_ids, ctx->st_ids_cap, (size_t)n))) return rc;
-    dfree(ctx->st_off);
-    if ((rc = grow(ctx->st_off, cap_off, (size_t)nc + 1))) return rc;
+    if ((rc = grow(ctx->st_off, ctx->st_off_cap, (size_t)nc + 1))) return rc;
     if (!ctx->st_flags && (rc = grow(ctx->st_flags, cap_f, 2))) return rc;
     if (!ctx->copy_stream) CU(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
     if (!ctx->copy_ev) CU(cudaEventCreateWithFlags(&ctx->copy_ev, cudaEventDisableTiming));
@@ -639,15 +642,13 @@ int upload_device(ipic3d_ctx* ctx, const ipic3d_particle* parts, const uint64_t*
     if (n == 0) return 1;
     int rc = ctx->fp32 ? upload_fast(ctx, ctx->p32, parts, off, ids) : upload_fast(ctx, ctx->p64, parts, off, ids);
     if (rc <= 1) return rc;  // done, error, or the host path (unknown species)
-    size_t cap_off = 0, cap_cnt = 0, cap_u = 0;
+    size_t cap_u = 0;
     if ((rc = grow(reinterpret_cast<char*&>(ctx->st_parts), ctx->st_parts_cap, (size_t)n * sizeof(ipic3d_particle))))
         return rc;
     if (ids && (rc = grow(ctx->st_ids, ctx->st_ids_cap, (size_t)n))) return rc;
     if ((rc = grow(ctx->st_sid, ctx->st_sid_cap, (size_t)n))) return rc;
-    dfree(ctx->st_off);
-    dfree(ctx->st_cnt);
-    if ((rc = grow(ctx->st_off, cap_off, (size_t)nc + 1))) return rc;
-    if ((rc = grow(ctx->st_cnt, cap_cnt, (size_t)nc * npop))) return rc;
+    if ((rc = grow(ctx->st_off, ctx->st_off_cap, (size_t)nc + 1))) return rc;
+    if ((rc = grow(ctx->st_cnt, ctx->st_cnt_cap, (size_t)nc * npop))) return rc;
     if (!ctx->st_unknown && (rc = grow(ctx->st_unknown, cap_u, 1))) return rc;
     cudaStream_t st = ctx->stream;
     CU(cudaMemcpyAsync(ctx->st_parts, parts, (size_t)n * sizeof(ipic3d_particle), cudaMemcpyHostToDevice, st));
@@ -800,9 +801,7 @@ int init_normal_impl(ipic3d_ctx* ctx, uint64_t n, const double low[3], const dou
     // staging array) for the generator
     uint64_t* d_count = nullptr;
     CU(cudaMalloc(&d_count, (size_t)nc * sizeof(uint64_t)));
-    size_t cap_off = 0;
-    dfree(ctx->st_off);
-    if ((rc = grow(ctx->st_off, cap_off, (size_t)nc + 1))) {
+    if ((rc = grow(ctx->st_off, ctx->st_off_cap, (size_t)nc + 1))) {
         cudaFree(d_count);
         return rc;
     }
