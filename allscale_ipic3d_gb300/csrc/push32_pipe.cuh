@@ -137,11 +137,25 @@ static_assert(offsetof(PipeStage, coef) % 16 == 0 && offsetof(PipeStage, start) 
                   sizeof(PipeStage) % 16 == 0 && sizeof(PopJob<float>) % 16 == 0,
               "bulk copies need 16-byte aligned shared-memory destinations");
 
+// Item mode: what the compute warps need to know about a cell of the
+// stage's tile -- its occupied slots [lo, hi) within the tile, the exclusive
+// prefix of the tile's items before it, its first slot and its CellInfo --
+// written once per tile by the first warp to reach it.
+struct CellDesc {
+    int lo, hi, excl, cst;
+    CellInfo ci;
+};
+static_assert(sizeof(CellDesc) == 32, "two 16-byte loads per cell");
+
 template <int kStages>
 struct PipeSmem {
     PipeStage stage[kStages];
+    CellDesc cells[kStages][kItemMaxCells];
     uint64_t full[kStages];               // the stage's copies landed
     uint64_t empty[kStages];              // the compute warps are done with the stage
+    uint64_t ready[kStages];              // the tile's cell descriptors are written
+    int total[kStages];                   // items of the stage's tile
+    int claim[kStages];                   // warps that reached the stage's tile (the first writes the descriptors)
     int2 desc[kStages];                   // (first cell, number of cells) of the stage's tile
     int pop[kStages];                     // population (batched launch: job) of the stage's tile
     int ltile[kStages];                   // the tile's index within its population
@@ -570,22 +584,23 @@ __device__ __forceinline__ void push_slots(const Geom& g, const Pop<float>& P, c
     }
 }
 
-// One compute warp's share of the tile in `st`.
-template <int kF>
-__device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& P, const Push32Const& pc,
-                                               const Push32Const& sp, int tile,
-                                               int2 desc, const PushShape& shp, PipeStage& st, int* next_item,
-                                               uint32_t& nmig, uint32_t& nrem) {
+// Item mode: where the stage's tile descriptors live, and the phase of the
+// stage's `ready` barrier that this use of the stage completes.
+struct TileDescs {
+    CellDesc* cells;
+    int* total;
+    int* claim;
+    uint64_t* ready;
+    uint32_t parity;
+    const volatile int* abort;
+    uint32_t polls;
+};
+
+// The item-mode descriptors of the tile, by the warp with lane i describing
+// cell c0 + i; the tile's items into *total.
+__device__ __forceinline__ void write_cell_descs(const Geom& g, const Push32Const& pc, const PipeStage& st,
+                                                 int base, int c0, int nc, int sh, CellDesc* cells, int* total) {
     const int lane = threadIdx.x & 31;
-    const int base = tile * kTileSlots;
-    const int c0 = desc.x, nc = desc.y;
-    if (nc > shp.item_cells) {
-        for (int w = threadIdx.x >> 5; w < kSlotWarps; w += kComputeWarps)
-            push_slots<kF>(g, P, pc, sp, st, base, desc, w, nmig, nrem);
-        return;
-    }
-    // item mode: lane i describes cell c0 + i: its occupied slots [lo, hi)
-    // within the tile, its items and their exclusive prefix, its CellInfo
     const int64_t* S = st.start + (c0 & 1);
     const int32_t* N = st.count + (c0 & 3);
     int lo = 0, hi = 0, cst = 0;
@@ -595,8 +610,6 @@ __device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& 
         lo = l < 0 ? 0 : l;
         hi = h > kTileSlots ? kTileSlots : h;
     }
-    const CellInfo mine = cell_info(g, pc, c0 + (lane < nc ? lane : 0));
-    const int sh = 31 - __clz(shp.item);  // items of 2^sh particles
     const int items = hi > lo ? (hi - lo + (1 << sh) - 1) >> sh : 0;
     int incl = items;
 #pragma unroll
@@ -604,23 +617,63 @@ __device__ __forceinline__ void push_tile_warp(const Geom& g, const Pop<float>& 
         const int n = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += n;
     }
-    const int excl = incl - items;
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    CellDesc d;
+    d.lo = lo;
+    d.hi = items > 0 ? hi : lo;  // cells with no slots here own no item
+    d.excl = incl - items;
+    d.cst = cst;
+    d.ci = cell_info(g, pc, c0 + (lane < nc ? lane : 0));
+    cells[lane] = d;
+    if (lane == 31) *total = incl;
+}
+
+// One compute warp's share of the tile in `st`; false if a wait expired.
+template <int kF>
+__device__ __forceinline__ bool push_tile_warp(const Geom& g, const Pop<float>& P, const Push32Const& pc,
+                                               const Push32Const& sp, int tile,
+                                               int2 desc, const PushShape& shp, PipeStage& st, int* next_item,
+                                               const TileDescs& td, uint32_t& nmig, uint32_t& nrem) {
+    const int lane = threadIdx.x & 31;
+    const int base = tile * kTileSlots;
+    const int c0 = desc.x, nc = desc.y;
+    // the first warp to reach the tile completes the phase of `ready` that
+    // belongs to this use of the stage (in item mode after writing the cells'
+    // descriptors, lane i: cell c0 + i); the others wait for it there
+    int first = 0;
+    if (lane == 0) first = atomicAdd(td.claim, 1) == 0;
+    first = __shfl_sync(0xffffffffu, first, 0);
+    if (nc > shp.item_cells) {
+        if (first && lane == 0) mbar_arrive(td.ready);
+        for (int w = threadIdx.x >> 5; w < kSlotWarps; w += kComputeWarps)
+            push_slots<kF>(g, P, pc, sp, st, base, desc, w, nmig, nrem);
+        return true;
+    }
+    const int sh = 31 - __clz(shp.item);  // items of 2^sh particles
+    if (first) {
+        write_cell_descs(g, pc, st, base, c0, nc, sh, td.cells, td.total);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(td.ready);
+    } else if (!__all_sync(0xffffffffu, mbar_wait(td.ready, td.parity, td.abort, td.polls))) {
+        return false;
+    }
+    const CellDesc d = td.cells[lane];
+    const int total = *td.total;
     for (;;) {
         int j = 0;
         if (lane == 0) j = atomicAdd(next_item, 1);
         j = __shfl_sync(0xffffffffu, j, 0);
         if (j >= total) break;
-        const unsigned owners = __ballot_sync(0xffffffffu, items > 0 && excl <= j);
+        const unsigned owners = __ballot_sync(0xffffffffu, d.hi > d.lo && d.excl <= j);
         const int src = 31 - __clz(owners);
-        const int clo = __shfl_sync(0xffffffffu, lo, src), chi = __shfl_sync(0xffffffffu, hi, src);
-        const int cex = __shfl_sync(0xffffffffu, excl, src);
-        const int cstart = __shfl_sync(0xffffffffu, cst, src);
+        const int clo = __shfl_sync(0xffffffffu, d.lo, src), chi = __shfl_sync(0xffffffffu, d.hi, src);
+        const int cex = __shfl_sync(0xffffffffu, d.excl, src);
+        const int cstart = __shfl_sync(0xffffffffu, d.cst, src);
         const int a = clo + ((j - cex) << sh);
         const int b = a + (1 << sh) < chi ? a + (1 << sh) : chi;
-        push_item<kF>(g, P, pc, sp, st, st.coef + src * 48, shfl_cell_info(mine, src), base, c0 + src, cstart, a, b,
+        push_item<kF>(g, P, pc, sp, st, st.coef + src * 48, shfl_cell_info(d.ci, src), base, c0 + src, cstart, a, b,
                       nmig, nrem);
     }
+    return true;
 }
 
 // Tile t of a launch over several populations: population i holds tiles
@@ -664,6 +717,7 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
         for (int s = 0; s < kStages; ++s) {
             mbar_init(&sm.full[s], 1);
             mbar_init(&sm.empty[s], kComputeWarps);
+            mbar_init(&sm.ready[s], 1);
         }
         sm.abort = 0;
         fence_mbar_init();
@@ -684,6 +738,7 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
             sm.desc[s] = d;
             sm.pop[s] = pi;
             sm.next_item[s] = 0;
+            sm.claim[s] = 0;
             issue_tile(S.p[pi], coef, t - tm.first[pi], d, shp.item_cells, sm.stage[s], &sm.full[s]);
         };
         int issued = 0;  // tiles of this CTA whose copies were issued
@@ -752,8 +807,13 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
         }
         // constants other than the species' are the same for every
         // population of the launch: population 0's, at fixed offsets
-        push_tile_warp<kF>(g, S.p[pi], pcs.c[0], pcs.c[pi], t - tm.first[pi], sm.desc[s], shp, sm.stage[s],
-                           &sm.next_item[s], nmig, nrem);
+        const TileDescs td{sm.cells[s], &sm.total[s], &sm.claim[s], &sm.ready[s], (uint32_t)(k / kStages) & 1u,
+                           abort, polls};
+        if (!push_tile_warp<kF>(g, S.p[pi], pcs.c[0], pcs.c[pi], t - tm.first[pi], sm.desc[s], shp, sm.stage[s],
+                                &sm.next_item[s], td, nmig, nrem)) {
+            if (lane == 0 && atomicExch(&sm.abort, 1) == 0) atomicAdd(&S.p[0].ctr->timeouts, 1u);
+            break;
+        }
         fence_proxy_async_smem();  // this warp's writes to the stage, before the bulk stores read it
         __syncwarp();
         if (lane == 0) mbar_arrive(&sm.empty[s]);
@@ -779,6 +839,7 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
         for (int s = 0; s < kStages; ++s) {
             mbar_init(&sm.full[s], 1);
             mbar_init(&sm.empty[s], kComputeWarps);
+            mbar_init(&sm.ready[s], 1);
         }
         sm.abort = 0;
         fence_mbar_init();
@@ -799,6 +860,7 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
             sm.pop[s] = cj.x;
             sm.ltile[s] = cj.y;
             sm.next_item[s] = 0;
+            sm.claim[s] = 0;
             issue_tile(P, coef, cj.y, d, shp.item_cells, sm.stage[s], &sm.full[s], (uint32_t)sizeof(PopJob<float>));
             bulk_load(&sm.stage[s].job, J, (uint32_t)sizeof(PopJob<float>), &sm.full[s]);
         };
@@ -858,8 +920,13 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
             if (cur) flush_counts(cur, nmig, nrem);
             cur = J.P.ctr;
         }
-        push_tile_warp<kF>(J.g, J.P, J.pc, J.pc, sm.ltile[s], sm.desc[s], shp, sm.stage[s], &sm.next_item[s],
-                           nmig, nrem);
+        const TileDescs td{sm.cells[s], &sm.total[s], &sm.claim[s], &sm.ready[s], (uint32_t)(k / kStages) & 1u,
+                           abort, polls};
+        if (!push_tile_warp<kF>(J.g, J.P, J.pc, J.pc, sm.ltile[s], sm.desc[s], shp, sm.stage[s], &sm.next_item[s],
+                                td, nmig, nrem)) {
+            if (lane == 0 && atomicExch(&sm.abort, 1) == 0) atomicAdd(&jobs[0].P.ctr->timeouts, 1u);
+            break;
+        }
         fence_proxy_async_smem();
         __syncwarp();
         if (lane == 0) mbar_arrive(&sm.empty[s]);
