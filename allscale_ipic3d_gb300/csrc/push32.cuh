@@ -6,8 +6,8 @@
 //   * fields: per-cell trilinear polynomial f = c0 + c1 x + c2 y + c3 z +
 //     c4 xy + c5 xz + c6 yz + c7 xyz of every E and B component (the
 //     expansion of trilinearInterpolationF2P, cell.h:867-885, with node
-//     values from the cell's 8 corners as in cell.h:905-937): 7 FMAs per
-//     component;
+//     values from the cell's 8 corners as in cell.h:905-937): 7 packed
+//     FP32-pair FMAs per two components;
 //   * dipole: |r|^-5 from one rsqrt;
 //   * sub-cycles (cell.h:947-952): dt/dt_sub = K |B|^2 with K per species.
 #pragma once
@@ -87,28 +87,52 @@ __device__ __forceinline__ CellInfo shfl_cell_info(const CellInfo& c, int src) {
     return r;
 }
 
-// One component of the cell's trilinear field polynomial at (x, y, z):
-// lo = (c0, cx, cy, cz), hi = (cxy, cxz, cyz, cxyz), seven FMAs.
-__device__ __forceinline__ float poly32(const float4& lo, const float4& hi, float x, float y, float z) {
-    const float a = fmaf(y, hi.w, hi.y);  // x z terms
-    float b = fmaf(y, hi.x, lo.y);        // x terms
-    b = fmaf(z, a, b);
-    const float gz = fmaf(z, hi.z, lo.z);  // y terms
-    float r = fmaf(y, gz, lo.x);
-    r = fmaf(z, lo.w, r);
-    return fmaf(x, b, r);
+// Packed FP32 pairs (sm_100+: one instruction for two lanes' worth of
+// work; each component rounds exactly as the scalar operation does).
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
+
+// Two components (a, b) of the cell's trilinear field polynomial at
+// (x, y, z), seven packed FMAs; c4 holds the pair's coefficients
+// interleaved: (c0a, c0b, cxa, cxb), (cya, cyb, cza, czb),
+// (cxya, cxyb, cxza, cxzb), (cyza, cyzb, cxyza, cxyzb).
+__device__ __forceinline__ float2 poly32x2(const float4& c01, const float4& c23, const float4& c45, const float4& c67,
+                                           float2 x, float2 y, float2 z) {
+    const float2 c0 = make_float2(c01.x, c01.y), cx = make_float2(c01.z, c01.w);
+    const float2 cy = make_float2(c23.x, c23.y), cz = make_float2(c23.z, c23.w);
+    const float2 cxy = make_float2(c45.x, c45.y), cxz = make_float2(c45.z, c45.w);
+    const float2 cyz = make_float2(c67.x, c67.y), cxyz = make_float2(c67.z, c67.w);
+    const float2 a = fma2(y, cxyz, cxz);  // x z terms
+    float2 b = fma2(y, cxy, cx);          // x terms
+    b = fma2(z, a, b);
+    const float2 gz = fma2(z, cyz, cy);   // y terms
+    float2 r = fma2(y, gz, c0);
+    r = fma2(z, cz, r);
+    return fma2(x, b, r);
 }
+
+// Coefficient m (monomials 1, x, y, z, xy, xz, yz, xyz) of component q (Ex,
+// Ey, Ez, Bx, By, Bz) within a cell's 48: components in pairs (Ex, Ey),
+// (Ez, Bx), (By, Bz), each pair's coefficients interleaved.
+__host__ __device__ constexpr int coef_index(int q, int m) { return (q >> 1) * 16 + m * 2 + (q & 1); }
 
 // E and B of a particle from its cell's polynomial coefficients (kSmem:
 // staged in shared memory; else read from global memory).
 template <bool kSmem>
 __device__ __forceinline__ void fields_one(const float* __restrict__ coef, const PState<float>& a, float (&E)[6]) {
     const float4* c4 = reinterpret_cast<const float4*>(coef);
+    const float2 x = dup2(a.x), y = dup2(a.y), z = dup2(a.z);
 #pragma unroll
-    for (int q = 0; q < 6; ++q) {
-        const float4 lo = kSmem ? c4[2 * q] : __ldg(c4 + 2 * q);
-        const float4 hi = kSmem ? c4[2 * q + 1] : __ldg(c4 + 2 * q + 1);
-        E[q] = poly32(lo, hi, a.x, a.y, a.z);
+    for (int q = 0; q < 3; ++q) {
+        const float4 c01 = kSmem ? c4[4 * q] : __ldg(c4 + 4 * q);
+        const float4 c23 = kSmem ? c4[4 * q + 1] : __ldg(c4 + 4 * q + 1);
+        const float4 c45 = kSmem ? c4[4 * q + 2] : __ldg(c4 + 4 * q + 2);
+        const float4 c67 = kSmem ? c4[4 * q + 3] : __ldg(c4 + 4 * q + 3);
+        const float2 e = poly32x2(c01, c23, c45, c67, x, y, z);
+        E[2 * q] = e.x;
+        E[2 * q + 1] = e.y;
     }
 }
 
@@ -298,7 +322,7 @@ __global__ void k_push_pending32(Geom g, const __grid_constant__ PopSet<float> S
 
 // Cell coefficients of the trilinear field polynomial, stored FP32:
 // coefficient m of component q (Ex, Ey, Ez, Bx, By, Bz) of cell c at
-// coef[c * 48 + q * 8 + m]; monomials m = 1, x, y, z, xy, xz, yz, xyz. One
+// coef[c * 48 + coef_index(q, m)]; monomials m = 1, x, y, z, xy, xz, yz, xyz. One
 // thread per (cell, component): the seven corner differences from corner
 // (0,0,0) are taken in FP64 and rounded once, the mixed terms are then FP32
 // sums of those differences (a few FP64 operations per coefficient instead
@@ -334,9 +358,9 @@ __device__ __forceinline__ void cell_coef_body(const double* __restrict__ field,
 #pragma unroll
             for (int k = 1; k < 8; ++k) m[k] *= fs;
         }
-        float4* out = reinterpret_cast<float4*>(coef + c * 48 + q * 8);
-        out[0] = make_float4(m[0], m[1], m[2], m[3]);
-        out[1] = make_float4(m[4], m[5], m[6], m[7]);
+        float* out = coef + c * 48;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) out[coef_index(q, k)] = m[k];
     }
 }
 
@@ -365,7 +389,7 @@ __global__ void k_cell_coef32(const float4* __restrict__ n32, int sx, int sy, in
             f[k][0] = e.x; f[k][1] = e.y; f[k][2] = e.z;
             f[k][3] = b.x; f[k][4] = b.y; f[k][5] = b.z;
         }
-        float4* out = reinterpret_cast<float4*>(coef + c * 48);
+        float m[6][8];
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
             // corner k = i + 2 j + 4 l at (x + i, y + j, z + l)
@@ -374,9 +398,15 @@ __global__ void k_cell_coef32(const float4* __restrict__ n32, int sx, int sy, in
             const float m1 = d100, m2 = d010, m3 = d001;
             const float m4 = d110 - d100 - d010, m5 = d101 - d100 - d001, m6 = d011 - d010 - d001;
             const float m7 = ((d111 - d110) - (d101 + d011)) + (d100 + d010 + d001);
-            out[2 * q] = make_float4(f000 * scale, m1 * scale, m2 * scale, m3 * scale);
-            out[2 * q + 1] = make_float4(m4 * scale, m5 * scale, m6 * scale, m7 * scale);
+            m[q][0] = f000 * scale; m[q][1] = m1 * scale; m[q][2] = m2 * scale; m[q][3] = m3 * scale;
+            m[q][4] = m4 * scale; m[q][5] = m5 * scale; m[q][6] = m6 * scale; m[q][7] = m7 * scale;
         }
+        float4* out = reinterpret_cast<float4*>(coef + c * 48);
+#pragma unroll
+        for (int P = 0; P < 3; ++P)
+#pragma unroll
+            for (int k = 0; k < 8; k += 2)
+                out[P * 4 + k / 2] = make_float4(m[2 * P][k], m[2 * P + 1][k], m[2 * P][k + 1], m[2 * P + 1][k + 1]);
     }
 }
 

@@ -276,34 +276,34 @@ __device__ __forceinline__ void deposit_leavers32(const Geom& g, unsigned lb, in
 }
 
 // Adds the centred cloud-in-cell moments of a particle to acc (index 8 Q +
-// m, Q in {u, v, w, 1}, m in {1, x, y, xy, z, xz, yz, xyz} of r - 1/2):
-// kCount also counts it in acc[24] (the work-item path counts its stayers
-// apart). A cleared slot (clear_slot) adds zero.
-template <bool kCount>
+// m, Q in {u, v, w, 1}, m in {1, x, y, xy, z, xz, yz, xyz} of r - 1/2) in
+// packed FP32 pairs (m, m + 1): four packed FMAs per velocity component and
+// four packed adds for the rho moments. acc[24] counts every slot it is
+// given, cleared or not; the callers replace that sum by the stayer count.
+// A cleared slot (clear_slot) adds zero to every other moment.
 __device__ __forceinline__ void add_moments(float (&acc)[32], const PState<float>& p) {
     const float x = p.x - 0.5f, y = p.y - 0.5f, z = p.z - 0.5f;
     // separate roundings (no fusion with the sums below in some kernels only)
     const float xy = __fmul_rn(x, y), xz = __fmul_rn(x, z), yz = __fmul_rn(y, z), xyz = __fmul_rn(xy, z);
+    const float2 M[4] = {make_float2(1.f, x), make_float2(y, xy), make_float2(z, xz), make_float2(yz, xyz)};
     const float Q[3] = {p.u, p.v, p.w};
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
-        acc[q * 8 + 0] += Q[q];
-        acc[q * 8 + 1] = fmaf(Q[q], x, acc[q * 8 + 1]);
-        acc[q * 8 + 2] = fmaf(Q[q], y, acc[q * 8 + 2]);
-        acc[q * 8 + 3] = fmaf(Q[q], xy, acc[q * 8 + 3]);
-        acc[q * 8 + 4] = fmaf(Q[q], z, acc[q * 8 + 4]);
-        acc[q * 8 + 5] = fmaf(Q[q], xz, acc[q * 8 + 5]);
-        acc[q * 8 + 6] = fmaf(Q[q], yz, acc[q * 8 + 6]);
-        acc[q * 8 + 7] = fmaf(Q[q], xyz, acc[q * 8 + 7]);
+        const float2 Q2 = dup2(Q[q]);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            // Q * 1 + acc rounds as acc + Q
+            const float2 r = fma2(Q2, M[k], make_float2(acc[q * 8 + 2 * k], acc[q * 8 + 2 * k + 1]));
+            acc[q * 8 + 2 * k] = r.x;
+            acc[q * 8 + 2 * k + 1] = r.y;
+        }
     }
-    if (kCount) acc[24] += 1.f;
-    acc[25] += x;
-    acc[26] += y;
-    acc[27] += xy;
-    acc[28] += z;
-    acc[29] += xz;
-    acc[30] += yz;
-    acc[31] += xyz;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float2 r = add2(make_float2(acc[24 + 2 * k], acc[25 + 2 * k]), M[k]);
+        acc[24 + 2 * k] = r.x;
+        acc[25 + 2 * k] = r.y;
+    }
 }
 
 // Lane v holds the summed moment v = 8 Q + m of one cell: the three axis
@@ -459,8 +459,8 @@ __device__ __forceinline__ void push_item(const Geom& g, const Pop<float>& P, co
     int s0 = a;
 #pragma unroll 1
     for (; s0 + 64 <= b; s0 += 64) {
-        add_moments<false>(acc, load_slot(st, s0 + lane));
-        add_moments<false>(acc, load_slot(st, s0 + 32 + lane));
+        add_moments(acc, load_slot(st, s0 + lane));
+        add_moments(acc, load_slot(st, s0 + 32 + lane));
     }
 #pragma unroll 1
     for (; s0 < b; s0 += 32) {
@@ -470,7 +470,7 @@ __device__ __forceinline__ void push_item(const Geom& g, const Pop<float>& P, co
             p.x = p.y = p.z = 0.5f;
             p.u = p.v = p.w = 0.f;
         }
-        add_moments<false>(acc, p);
+        add_moments(acc, p);
     }
     float s = warp_transpose_sum<float>(acc);
     if (lane == 24) s = (float)(b - a - gone);  // the stayers: sum of the rho weights' 1 term
@@ -565,7 +565,7 @@ __device__ __forceinline__ void push_slots(const Geom& g, const Pop<float>& P, c
 #pragma unroll
     for (int l = 0; l < 32; ++l) acc[l] = 0.f;
 #pragma unroll 1
-    for (int j = 0; j < nv; ++j) add_moments<false>(acc, load_slot(st, sl0 + j));
+    for (int j = 0; j < nv; ++j) add_moments(acc, load_slot(st, sl0 + j));
     const unsigned todo = __ballot_sync(0xffffffffu, nst > 0);
     const int prev_cell = __shfl_up_sync(0xffffffffu, cell, 1);
     unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev_cell != cell);
