@@ -115,8 +115,12 @@ __device__ __forceinline__ float2 poly32x2(const float4& c01, const float4& c23,
 
 // Coefficient m (monomials 1, x, y, z, xy, xz, yz, xyz) of component q (Ex,
 // Ey, Ez, Bx, By, Bz) within a cell's 48: components in pairs (Ex, Ey),
-// (Ez, Bx), (By, Bz), each pair's coefficients interleaved.
-__host__ __device__ constexpr int coef_index(int q, int m) { return (q >> 1) * 16 + m * 2 + (q & 1); }
+// (Bx, By), (Ez, Bz) -- the pairs the mover works on -- each pair's
+// coefficients interleaved.
+__host__ __device__ constexpr int coef_pair(int q) { return q == 2 ? 2 : (q == 5 ? 2 : q / 3); }
+__host__ __device__ constexpr int coef_index(int q, int m) {
+    return coef_pair(q) * 16 + m * 2 + (q == 5 ? 1 : (q == 2 ? 0 : q % 3));
+}
 
 // E and B of a particle from its cell's polynomial coefficients (kSmem:
 // staged in shared memory; else read from global memory).
@@ -131,8 +135,8 @@ __device__ __forceinline__ void fields_one(const float* __restrict__ coef, const
         const float4 c45 = kSmem ? c4[4 * q + 2] : __ldg(c4 + 4 * q + 2);
         const float4 c67 = kSmem ? c4[4 * q + 3] : __ldg(c4 + 4 * q + 3);
         const float2 e = poly32x2(c01, c23, c45, c67, x, y, z);
-        E[2 * q] = e.x;
-        E[2 * q + 1] = e.y;
+        E[q == 2 ? 2 : 3 * q] = e.x;
+        E[q == 2 ? 5 : 3 * q + 1] = e.y;
     }
 }
 
@@ -140,12 +144,15 @@ __device__ __forceinline__ void fields_one(const float* __restrict__ coef, const
 // 2z^2 - x^2 - y^2) mft / |r|^5, |r|^-5 from one reciprocal square root.
 __device__ __forceinline__ void add_dipole(const Push32Const& pc, const CellInfo& ci, const PState<float>& p,
                                            float (&E)[6]) {
-    const float X = fmaf(p.x, pc.w[0], ci.ox), Y = fmaf(p.y, pc.w[1], ci.oy), Z = fmaf(p.z, pc.w[2], ci.oz);
+    const float2 XY = fma2(make_float2(p.x, p.y), make_float2(pc.w[0], pc.w[1]), make_float2(ci.ox, ci.oy));
+    const float X = XY.x, Y = XY.y, Z = fmaf(p.z, pc.w[2], ci.oz);
     const float r2 = fmaf(X, X, fmaf(Y, Y, Z * Z));
     const float ir = rsqrtf(r2), ir2 = ir * ir;
     const float fac1 = pc.mft * (ir2 * ir2 * ir);
-    E[3] = fmaf(3.f * X * Z, fac1, E[3]);
-    E[4] = fmaf(3.f * Y * Z, fac1, E[4]);
+    // (3 X Z, 3 Y Z) fac1 added to (Bx, By)
+    const float2 b = fma2(mul2(mul2(dup2(3.f), XY), dup2(Z)), dup2(fac1), make_float2(E[3], E[4]));
+    E[3] = b.x;
+    E[4] = b.y;
     E[5] = fmaf(fmaf(2.f * Z, Z, -fmaf(X, X, Y * Y)), fac1, E[5]);
 }
 
@@ -164,25 +171,33 @@ __device__ __forceinline__ float sub_ratio(float k_sub, const float (&E)[6]) {
 template <int kFixedNs>
 __device__ __forceinline__ void boris32(float k, float ax, float ay, float az, const float (&E)[6], PState<float>& p,
                                         int ns = kFixedNs) {
-    const float tx = k * E[3], ty = k * E[4], tz = k * E[5];
-    const float den = fmaf(tx, tx, fmaf(ty, ty, fmaf(tz, tz, 1.f)));
-    const float f = __fdividef(2.f, den);
-    const float sx = tx * f, sy = ty * f, sz = tz * f;
+    const float2 k2 = dup2(k);
+    const float2 txy = mul2(k2, make_float2(E[3], E[4]));
     // k E as separate roundings: the adds below must not fuse with them in
     // one kernel and not in another (the batched and single-universe
     // kernels give the same particles bit for bit)
-    const float kex = __fmul_rn(k, E[0]), key = __fmul_rn(k, E[1]), kez = __fmul_rn(k, E[2]);
+    const float2 kexy = mul2(k2, make_float2(E[0], E[1]));
+    const float2 kez_tz = mul2(k2, make_float2(E[2], E[5]));
+    const float tx = txy.x, ty = txy.y, tz = kez_tz.y, kez = kez_tz.x;
+    const float den = fmaf(tx, tx, fmaf(ty, ty, fmaf(tz, tz, 1.f)));
+    const float f = __fdividef(2.f, den);
+    const float2 sxy = mul2(txy, dup2(f));
+    const float sx = sxy.x, sy = sxy.y, sz = tz * f;
+    const float2 axy = make_float2(ax, ay);
     int s = 0;
     do {
-        const float mx = p.u + kex, my = p.v + key, mz = p.w + kez;
+        const float2 mxy = add2(make_float2(p.u, p.v), kexy);
+        const float mx = mxy.x, my = mxy.y, mz = p.w + kez;
         const float qx = fmaf(my, tz, fmaf(-mz, ty, mx));
         const float qy = fmaf(mz, tx, fmaf(-mx, tz, my));
         const float qz = fmaf(mx, ty, fmaf(-my, tx, mz));
-        p.u = fmaf(qy, sz, fmaf(-qz, sy, mx)) + kex;
-        p.v = fmaf(qz, sx, fmaf(-qx, sz, my)) + key;
+        const float2 uv = add2(make_float2(fmaf(qy, sz, fmaf(-qz, sy, mx)), fmaf(qz, sx, fmaf(-qx, sz, my))), kexy);
+        p.u = uv.x;
+        p.v = uv.y;
         p.w = fmaf(qx, sy, fmaf(-qy, sx, mz)) + kez;
-        p.x = fmaf(p.u, ax, p.x);
-        p.y = fmaf(p.v, ay, p.y);
+        const float2 xy = fma2(uv, axy, make_float2(p.x, p.y));
+        p.x = xy.x;
+        p.y = xy.y;
         p.z = fmaf(p.w, az, p.z);
     } while (kFixedNs == 0 && ++s < ns);
 }
@@ -402,11 +417,14 @@ __global__ void k_cell_coef32(const float4* __restrict__ n32, int sx, int sy, in
             m[q][4] = m4 * scale; m[q][5] = m5 * scale; m[q][6] = m6 * scale; m[q][7] = m7 * scale;
         }
         float4* out = reinterpret_cast<float4*>(coef + c * 48);
+        constexpr int kPair[3][2] = {{0, 1}, {3, 4}, {2, 5}};  // coef_pair's order
 #pragma unroll
         for (int P = 0; P < 3; ++P)
 #pragma unroll
-            for (int k = 0; k < 8; k += 2)
-                out[P * 4 + k / 2] = make_float4(m[2 * P][k], m[2 * P + 1][k], m[2 * P][k + 1], m[2 * P + 1][k + 1]);
+            for (int k = 0; k < 8; k += 2) {
+                const int a = kPair[P][0], b = kPair[P][1];
+                out[P * 4 + k / 2] = make_float4(m[a][k], m[b][k], m[a][k + 1], m[b][k + 1]);
+            }
     }
 }
 
