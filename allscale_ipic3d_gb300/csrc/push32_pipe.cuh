@@ -154,6 +154,7 @@ struct PipeSmem {
     uint64_t full[kStages];               // the stage's copies landed
     uint64_t empty[kStages];              // the compute warps are done with the stage
     uint64_t ready[kStages];              // the tile's cell descriptors are written
+    uint8_t item_cell[kStages][kTileSlots / 32 + kItemMaxCells];  // item j of the tile: its cell - c0
     int total[kStages];                   // items of the stage's tile
     int claim[kStages];                   // warps that reached the stage's tile (the first writes the descriptors)
     int2 desc[kStages];                   // (first cell, number of cells) of the stage's tile
@@ -588,6 +589,7 @@ __device__ __forceinline__ void push_slots(const Geom& g, const Pop<float>& P, c
 // stage's `ready` barrier that this use of the stage completes.
 struct TileDescs {
     CellDesc* cells;
+    uint8_t* item_cell;
     int* total;
     int* claim;
     uint64_t* ready;
@@ -599,7 +601,8 @@ struct TileDescs {
 // The item-mode descriptors of the tile, by the warp with lane i describing
 // cell c0 + i; the tile's items into *total.
 __device__ __forceinline__ void write_cell_descs(const Geom& g, const Push32Const& pc, const PipeStage& st,
-                                                 int base, int c0, int nc, int sh, CellDesc* cells, int* total) {
+                                                 int base, int c0, int nc, int sh, CellDesc* cells,
+                                                 uint8_t* item_cell, int* total) {
     const int lane = threadIdx.x & 31;
     const int64_t* S = st.start + (c0 & 1);
     const int32_t* N = st.count + (c0 & 3);
@@ -624,6 +627,7 @@ __device__ __forceinline__ void write_cell_descs(const Geom& g, const Push32Cons
     d.cst = cst;
     d.ci = cell_info(g, pc, c0 + (lane < nc ? lane : 0));
     cells[lane] = d;
+    for (int k = 0; k < items; ++k) item_cell[d.excl + k] = (uint8_t)lane;
     if (lane == 31) *total = incl;
 }
 
@@ -650,28 +654,23 @@ __device__ __forceinline__ bool push_tile_warp(const Geom& g, const Pop<float>& 
     }
     const int sh = 31 - __clz(shp.item);  // items of 2^sh particles
     if (first) {
-        write_cell_descs(g, pc, st, base, c0, nc, sh, td.cells, td.total);
+        write_cell_descs(g, pc, st, base, c0, nc, sh, td.cells, td.item_cell, td.total);
         __syncwarp();
         if (lane == 0) mbar_arrive(td.ready);
     } else if (!__all_sync(0xffffffffu, mbar_wait(td.ready, td.parity, td.abort, td.polls))) {
         return false;
     }
-    const CellDesc d = td.cells[lane];
     const int total = *td.total;
     for (;;) {
         int j = 0;
         if (lane == 0) j = atomicAdd(next_item, 1);
         j = __shfl_sync(0xffffffffu, j, 0);
         if (j >= total) break;
-        const unsigned owners = __ballot_sync(0xffffffffu, d.hi > d.lo && d.excl <= j);
-        const int src = 31 - __clz(owners);
-        const int clo = __shfl_sync(0xffffffffu, d.lo, src), chi = __shfl_sync(0xffffffffu, d.hi, src);
-        const int cex = __shfl_sync(0xffffffffu, d.excl, src);
-        const int cstart = __shfl_sync(0xffffffffu, d.cst, src);
-        const int a = clo + ((j - cex) << sh);
-        const int b = a + (1 << sh) < chi ? a + (1 << sh) : chi;
-        push_item<kF>(g, P, pc, sp, st, st.coef + src * 48, shfl_cell_info(d.ci, src), base, c0 + src, cstart, a, b,
-                      nmig, nrem);
+        const int src = td.item_cell[j];
+        const CellDesc d = td.cells[src];
+        const int a = d.lo + ((j - d.excl) << sh);
+        const int b = a + (1 << sh) < d.hi ? a + (1 << sh) : d.hi;
+        push_item<kF>(g, P, pc, sp, st, st.coef + src * 48, d.ci, base, c0 + src, d.cst, a, b, nmig, nrem);
     }
     return true;
 }
@@ -807,8 +806,8 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
         }
         // constants other than the species' are the same for every
         // population of the launch: population 0's, at fixed offsets
-        const TileDescs td{sm.cells[s], &sm.total[s], &sm.claim[s], &sm.ready[s], (uint32_t)(k / kStages) & 1u,
-                           abort, polls};
+        const TileDescs td{sm.cells[s], sm.item_cell[s], &sm.total[s], &sm.claim[s], &sm.ready[s],
+                           (uint32_t)(k / kStages) & 1u, abort, polls};
         if (!push_tile_warp<kF>(g, S.p[pi], pcs.c[0], pcs.c[pi], t - tm.first[pi], sm.desc[s], shp, sm.stage[s],
                                 &sm.next_item[s], td, nmig, nrem)) {
             if (lane == 0 && atomicExch(&sm.abort, 1) == 0) atomicAdd(&S.p[0].ctr->timeouts, 1u);
@@ -920,8 +919,8 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
             if (cur) flush_counts(cur, nmig, nrem);
             cur = J.P.ctr;
         }
-        const TileDescs td{sm.cells[s], &sm.total[s], &sm.claim[s], &sm.ready[s], (uint32_t)(k / kStages) & 1u,
-                           abort, polls};
+        const TileDescs td{sm.cells[s], sm.item_cell[s], &sm.total[s], &sm.claim[s], &sm.ready[s],
+                           (uint32_t)(k / kStages) & 1u, abort, polls};
         if (!push_tile_warp<kF>(J.g, J.P, J.pc, J.pc, sm.ltile[s], sm.desc[s], shp, sm.stage[s], &sm.next_item[s],
                                 td, nmig, nrem)) {
             if (lane == 0 && atomicExch(&sm.abort, 1) == 0) atomicAdd(&jobs[0].P.ctr->timeouts, 1u);

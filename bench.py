@@ -994,6 +994,9 @@ def main():
     ap.add_argument("--error-cpu-steps", type=int, default=10, help="steps of the FP64 GPU vs CPU oracle statement")
     ap.add_argument("--no-configs", action="store_true", help="skip the C5 and :U:N rows in the full run")
     ap.add_argument("--c5-steps", type=int, default=20, help="timed steps of the C5 row in the full run")
+    ap.add_argument("--push-shape", default=None,
+                    help="ITEM,ITEM_CELLS,BLOCKS_PER_SM: fix the FP32 push shape of the headline run instead of "
+                         "autotuning it (profiling runs, where a profiler's timing would steer the autotuner)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -1074,6 +1077,9 @@ def main():
     # ---- FP32 headline ----
     sim32 = g.Simulation(props, make_config(abi.FP32))
     sim32.upload_particles(parts, counts)
+    if args.push_shape:
+        item, item_cells, bps = (int(v) for v in args.push_shape.split(","))
+        sim32.set_push_shape(item=item, item_cells=item_cells, blocks_per_sm=bps)
     if dist:
         dist.barrier()
     sampler = ClockSampler(local)
