@@ -421,6 +421,7 @@ __device__ __forceinline__ void push_item(const Geom& g, const Pop<float>& P, co
     int gone = 0;  // leavers and drops of the item (warp-uniform)
     if (kStep) {
         const float k1 = sp.k1, ksub = sp.k_sub;
+        const bool plain = (ci.flags & (kCellEdge | kCellNear)) == 0;
 #pragma unroll 1
         for (int s0 = a; s0 < b; s0 += 32) {
             const int sl = s0 + lane;
@@ -441,6 +442,14 @@ __device__ __forceinline__ void push_item(const Geom& g, const Pop<float>& P, co
                 boris32<1>(k1, pc.a1[0], pc.a1[1], pc.a1[2], E, p);
             else
                 boris_sub(pc, sp, r, E, p);
+            // a cell away from the domain faces and the planet, whose
+            // particles all stayed in it: export32 would return kStay for
+            // each, so they go straight back to the stage
+            const bool in = p.x >= 0.f && p.x <= 1.f && p.y >= 0.f && p.y <= 1.f && p.z >= 0.f && p.z <= 1.f;
+            if (plain && __all_sync(0xffffffffu, in || sl >= b)) {
+                if (sl < b) store_slot(st, sl, p);
+                continue;
+            }
             int dir = 0;
             int o = export32(g, pc, ci, p, dir);
             o = sl < b ? o : -1;
