@@ -200,19 +200,26 @@ __device__ __forceinline__ TileCopy tile_copy(const Pop<float>& P, int tile, int
 // Issued by the producer: the tile's copies into `st`, counted on `bar`
 // (`extra` more bytes are expected from copies the caller issues);
 // with `coef` (item mode, field gather) also the cells' field coefficients
-// (48 floats = 192 bytes per cell, contiguous from cell c0).
-__device__ __forceinline__ void issue_tile(const Pop<float>& P, const float* coef, int tile, int2 desc,
-                                           int item_cells, PipeStage& st, uint64_t* bar, uint32_t extra = 0) {
+// (48 floats = 192 bytes per cell, contiguous from cell c0). In two parts:
+// the byte count and the cell tables first, the slot arrays second, so that
+// a refill can start before the previous tile's bulk stores have read the
+// slot arrays.
+__device__ __forceinline__ void issue_tile_tables(const Pop<float>& P, const float* coef, int tile, int2 desc,
+                                                  int item_cells, PipeStage& st, uint64_t* bar, uint32_t extra = 0) {
     const TileCopy t = tile_copy(P, tile, desc);
     const bool with_coef = coef != nullptr && desc.y <= item_cells;
     const uint32_t coef_bytes = with_coef ? (uint32_t)desc.y * 192u : 0u;
     mbar_arrive_expect_tx(bar, 6u * t.slot_bytes + t.s_bytes + t.c_bytes + coef_bytes + extra);
-    float* const arr[6] = {P.x, P.y, P.z, P.u, P.v, P.w};
-#pragma unroll
-    for (int a = 0; a < 6; ++a) bulk_load(st.s[a], arr[a] + t.base, t.slot_bytes, bar);
     bulk_load(st.start, P.start + t.s_first, t.s_bytes, bar);
     bulk_load(st.count, P.count + t.c_first, t.c_bytes, bar);
     if (coef_bytes) bulk_load(st.coef, coef + (size_t)desc.x * 48, coef_bytes, bar);
+}
+__device__ __forceinline__ void issue_tile_slots(const Pop<float>& P, int tile, int2 desc, PipeStage& st,
+                                                 uint64_t* bar) {
+    const TileCopy t = tile_copy(P, tile, desc);
+    float* const arr[6] = {P.x, P.y, P.z, P.u, P.v, P.w};
+#pragma unroll
+    for (int a = 0; a < 6; ++a) bulk_load(st.s[a], arr[a] + t.base, t.slot_bytes, bar);
 }
 
 // ---- per-particle physics --------------------------------------------------------
@@ -741,19 +748,23 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
             const int pi = tile_pop(tm, t);
             return __ldg(S.p[pi].cta_cells + (t - tm.first[pi]));
         };
-        auto issue = [&](int t, int s, int2 d) {
+        // wait_store: bulk stores of the stage's previous tile are in flight;
+        // the slot arrays are loaded once they have read them
+        auto issue = [&](int t, int s, int2 d, bool wait_store) {
             const int pi = tile_pop(tm, t);
             sm.desc[s] = d;
             sm.pop[s] = pi;
             sm.next_item[s] = 0;
             sm.claim[s] = 0;
-            issue_tile(S.p[pi], coef, t - tm.first[pi], d, shp.item_cells, sm.stage[s], &sm.full[s]);
+            issue_tile_tables(S.p[pi], coef, t - tm.first[pi], d, shp.item_cells, sm.stage[s], &sm.full[s]);
+            if (wait_store) bulk_wait_read_all();
+            issue_tile_slots(S.p[pi], t - tm.first[pi], d, sm.stage[s], &sm.full[s]);
         };
         int issued = 0;  // tiles of this CTA whose copies were issued
         for (int s = 0; s < kStages; ++s) {
             const int t = blockIdx.x + s * G;
             if (t >= ntiles) break;
-            issue(t, s, load_desc(t));
+            issue(t, s, load_desc(t), false);
             ++issued;
         }
         int2 next_desc = make_int2(0, 0);
@@ -779,10 +790,9 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
             }
             const int tn = t + kStages * G;
             if (tn < ntiles) {
-                if (store) bulk_wait_read_all();  // the stores have read the stage
                 const int2 d = next_desc;
                 if (tn + G < ntiles) next_desc = load_desc(tn + G);
-                issue(tn, s, d);
+                issue(tn, s, d, store);
                 ++issued;
             }
         }
@@ -858,7 +868,7 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
     if (warp == kComputeWarps) {
         // ---- producer ----
         if (lane != 0) return;
-        auto issue = [&](int t, int s) {
+        auto issue = [&](int t, int s, bool wait_store) {
             const int2 cj = __ldg(cta_job + t);
             const PopJob<float>* J = jobs + cj.x;
             const Pop<float> P = J->P;
@@ -869,14 +879,17 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
             sm.ltile[s] = cj.y;
             sm.next_item[s] = 0;
             sm.claim[s] = 0;
-            issue_tile(P, coef, cj.y, d, shp.item_cells, sm.stage[s], &sm.full[s], (uint32_t)sizeof(PopJob<float>));
+            issue_tile_tables(P, coef, cj.y, d, shp.item_cells, sm.stage[s], &sm.full[s],
+                              (uint32_t)sizeof(PopJob<float>));
             bulk_load(&sm.stage[s].job, J, (uint32_t)sizeof(PopJob<float>), &sm.full[s]);
+            if (wait_store) bulk_wait_read_all();
+            issue_tile_slots(P, cj.y, d, sm.stage[s], &sm.full[s]);
         };
         int issued = 0;
         for (int s = 0; s < kStages; ++s) {
             const int t = blockIdx.x + s * G;
             if (t >= ntiles) break;
-            issue(t, s);
+            issue(t, s, false);
             ++issued;
         }
         bool failed = false;
@@ -898,8 +911,7 @@ __global__ void __launch_bounds__(kPipeThreads, kMinBlocks)
             }
             const int tn = t + kStages * G;
             if (tn < ntiles) {
-                if (store) bulk_wait_read_all();  // the stores have read the stage
-                issue(tn, s);
+                issue(tn, s, store);
                 ++issued;
             }
         }
