@@ -110,3 +110,36 @@ def test_raw_j_read_matches_j_finalisation(prec, width, flags):
     np.testing.assert_array_equal(a["velocity"], b["velocity"])
     run.close()
     eager.close()
+
+
+@pytest.mark.parametrize("n", [5, 16])
+def test_fp32_node_b_refresh_matches_interp_c2n(n):
+    """The FP32 leapfrog solve with the node B refresh: every node B equals
+    interpC2N's (field.h:234-247) 1/8 sum of the 8 surrounding Bc, summed in
+    the same order, bit for bit, on every node of [1, s+1]^3 (the + faces
+    included); the ghost nodes keep the uploaded B."""
+    props, parts, counts = scenario(7300 + n, (n, n, n), width=(0.5, 0.5, 0.5), dt=0.05, ppc=2, vscale=0.1,
+                                    species=((-1.0, -1.0),))
+    rng = np.random.default_rng(73 + n)
+    f = rng.normal(0.0, 0.02, abi.field_shape(props))
+    bc = rng.normal(0.0, 0.02, abi.bcfield_shape(props))
+    dens = rng.normal(0.0, 0.01, abi.density_shape(props))
+    cfg = abi.Config.make(precision=abi.FP32, mover=abi.MOVER_FIELD, solver=abi.SOLVER_LEAPFROG,
+                          projector=abi.PROJECT_NONE, bc=abi.BC_PERIODIC, flags=abi.F_REFRESH_NODE_B)
+    sim = gpu_sim(props, cfg)
+    sim.upload_fields(f, bc, dens)
+    sim.upload_particles(parts, counts)
+    sim.solve_fields()
+    field, bcf, _, _ = sim.download_fields()
+    sim.close()
+    s = n
+    a = np.zeros((s + 1, s + 1, s + 1, 3))
+    for i in range(2):
+        for j in range(2):
+            for k in range(2):
+                a = a + bcf[1 - i:s + 2 - i, 1 - j:s + 2 - j, 1 - k:s + 2 - k, 0:3]
+    np.testing.assert_array_equal(field[1:s + 2, 1:s + 2, 1:s + 2, 3:6], 0.125 * a)
+    # nodes outside [1, s+1]^3 keep the uploaded B
+    mask = np.ones(field.shape[:3], dtype=bool)
+    mask[1:s + 2, 1:s + 2, 1:s + 2] = False
+    np.testing.assert_array_equal(field[mask][:, 3:6], f[mask][:, 3:6])
