@@ -144,8 +144,10 @@ static_assert(offsetof(PipeStage, coef) % 16 == 0 && offsetof(PipeStage, start) 
 struct CellDesc {
     int lo, hi, excl, cst;
     CellInfo ci;
+    int64_t node0;  // the node of the cell's corner (0,0,0)
+    int64_t unused;
 };
-static_assert(sizeof(CellDesc) == 32, "two 16-byte loads per cell");
+static_assert(sizeof(CellDesc) == 48, "three 16-byte loads per cell");
 
 template <int kStages>
 struct PipeSmem {
@@ -255,10 +257,9 @@ __device__ __forceinline__ void clear_slot(PipeStage& st, int sl) {
 // of the cell at (cx, cy, cz).
 __device__ __forceinline__ void corner_atomic_add(const Geom& g, int cx, int cy, int cz, int m, int q, double val) {
     const int64_t n = node_index(g, cx + (m & 1), cy + ((m >> 1) & 1), cz + (m >> 2));
-    if (q < 3)
-        atomicAdd(g.J + 3 * n + q, val);
-    else
-        atomicAdd(g.rho + n, val);
+    // one atomic instruction for the warp: the address is selected, not the branch
+    double* p = q < 3 ? g.J + 3 * n + q : g.rho + n;
+    atomicAdd(p, val);
 }
 
 // Cloud-in-cell deposit of the warp's leavers (ballot `lb`) into their
@@ -325,6 +326,20 @@ __device__ __forceinline__ void emit_corner_sums(const Geom& g, float s, int cx,
         s = (m & bit) ? fmaf(0.5f, o, s) : fmaf(0.5f, s, -o);
     }
     if (s != 0.f) corner_atomic_add(g, cx, cy, cz, m, lane >> 3, (double)s * q);
+}
+
+// emit_corner_sums for a cell given by the node of its corner (0,0,0).
+__device__ __forceinline__ void emit_node_sums(const Geom& g, float s, int64_t node0, double q) {
+    const int lane = threadIdx.x & 31, m = lane & 7, Q = lane >> 3;
+#pragma unroll
+    for (int bit = 1; bit < 8; bit <<= 1) {
+        const float o = __shfl_xor_sync(0xffffffffu, s, bit);
+        s = (m & bit) ? fmaf(0.5f, o, s) : fmaf(0.5f, s, -o);
+    }
+    const int64_t nz = g.sz + 1, nyz = (int64_t)(g.sy + 1) * nz;
+    const int64_t n = node0 + ((m & 1) ? nyz : 0) + ((m & 2) ? nz : 0) + (m >> 2);
+    double* p = Q < 3 ? g.J + 3 * n + Q : g.rho + n;
+    if (s != 0.f) atomicAdd(p, (double)s * q);
 }
 
 // Leaver bookkeeping of one warp step: outbox (one warp-aggregated append),
@@ -420,8 +435,8 @@ __device__ __forceinline__ void leave_and_hole(const Geom& g, const Pop<float>& 
 template <int kF>
 __device__ __forceinline__ void push_item(const Geom& g, const Pop<float>& P, const Push32Const& pc,
                                           const Push32Const& sp, PipeStage& st, const float* coef,
-                                          const CellInfo& ci, int base, int cell, int cstart, int a, int b,
-                                          uint32_t& nmig, uint32_t& nrem) {
+                                          const CellInfo& ci, int base, int cell, int64_t node0, int cstart, int a,
+                                          int b, uint32_t& nmig, uint32_t& nrem) {
     constexpr bool kStep = (kF & kPipeStep) != 0, kDep = (kF & kPipeDeposit) != 0;
     constexpr bool kGather = (kF & kPipeGather) != 0, kDipole = (kF & kPipeDipole) != 0;
     const int lane = threadIdx.x & 31;
@@ -491,8 +506,7 @@ __device__ __forceinline__ void push_item(const Geom& g, const Pop<float>& P, co
     }
     float s = warp_transpose_sum<float>(acc);
     if (lane == 24) s = (float)(b - a - gone);  // the stayers: sum of the rho weights' 1 term
-    const int3 c = cell_xyz(g, pc, cell);
-    emit_corner_sums(g, s, c.x, c.y, c.z, P.q);
+    emit_node_sums(g, s, node0, P.q);
 }
 
 // warp_transpose_sum of acc over the lanes with `mine` set (the others add
@@ -641,7 +655,11 @@ __device__ __forceinline__ void write_cell_descs(const Geom& g, const Push32Cons
     d.hi = items > 0 ? hi : lo;  // cells with no slots here own no item
     d.excl = incl - items;
     d.cst = cst;
-    d.ci = cell_info(g, pc, c0 + (lane < nc ? lane : 0));
+    const int cell = c0 + (lane < nc ? lane : 0);
+    d.ci = cell_info(g, pc, cell);
+    const int3 cx = cell_xyz(g, pc, cell);
+    d.node0 = node_index(g, cx.x, cx.y, cx.z);
+    d.unused = 0;
     cells[lane] = d;
     for (int k = 0; k < items; ++k) item_cell[d.excl + k] = (uint8_t)lane;
     if (lane == 31) *total = incl;
@@ -686,7 +704,7 @@ __device__ __forceinline__ bool push_tile_warp(const Geom& g, const Pop<float>& 
         const CellDesc d = td.cells[src];
         const int a = d.lo + ((j - d.excl) << sh);
         const int b = a + (1 << sh) < d.hi ? a + (1 << sh) : d.hi;
-        push_item<kF>(g, P, pc, sp, st, st.coef + src * 48, d.ci, base, c0 + src, d.cst, a, b, nmig, nrem);
+        push_item<kF>(g, P, pc, sp, st, st.coef + src * 48, d.ci, base, c0 + src, d.node0, d.cst, a, b, nmig, nrem);
     }
     return true;
 }
