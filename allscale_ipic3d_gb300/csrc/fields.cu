@@ -496,17 +496,19 @@ __global__ void k_reduce_fields(const double* field, int s, double vol, double f
     block_merge<2>(acc, partial + 4 * blockIdx.x);
 }
 
-// Final merge of `blocks` partial records of kq (s, c) pairs.
+// Final merge of `blocks` partial records of kq (s, c) pairs: warp q merges
+// quantity q, lane l the records l, l + 32, ... in order, then the lanes'
+// sums in a fixed shuffle tree (the same order every call).
 __global__ void k_reduce_final(const double* partial, int blocks, int kq, double* out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    for (int q = 0; q < kq; ++q) {
-        Neu t = {0.0, 0.0};
-        for (int b = 0; b < blocks; ++b) {
-            t.add(partial[2 * kq * b + 2 * q]);
-            t.c += partial[2 * kq * b + 2 * q + 1];
-        }
-        out[q] = t.s + t.c;
+    const int lane = threadIdx.x & 31, q = threadIdx.x >> 5;
+    if (blockIdx.x != 0 || q >= kq) return;
+    Neu t = {0.0, 0.0};
+    for (int b = lane; b < blocks; b += 32) {
+        t.add(partial[2 * kq * b + 2 * q]);
+        t.c += partial[2 * kq * b + 2 * q + 1];
     }
+    for (int off = 16; off > 0; off >>= 1) t.merge(shfl_neu(t, off));
+    if (lane == 0) out[q] = t.s + t.c;
 }
 
 inline int grid_for(int64_t n, int threads, int64_t max_blocks = 152 * 32) {
@@ -645,7 +647,7 @@ int launch_reduce_fields(const Geom& g, double* partial, cudaStream_t st) {
 }
 
 int launch_reduce_final(const double* partial, int blocks, int kq, double* out, cudaStream_t st) {
-    k_reduce_final<<<1, 32, 0, st>>>(partial, blocks, kq, out);
+    k_reduce_final<<<1, 32 * kq, 0, st>>>(partial, blocks, kq, out);
     return 1;
 }
 
