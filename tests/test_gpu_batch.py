@@ -230,3 +230,53 @@ def test_batch_empty_universes_and_lent_contexts():
         assert lib.ipic3d_gpu_batch_universe(batch._b, 2, C.byref(ctx)) == abi.E_INVALID
         n = C.c_uint32()
         assert lib.ipic3d_gpu_batch_size(batch._b, C.byref(n)) == 0 and n.value == 2
+
+
+def test_batch_forward_fp64_matches_oracle():
+    """The forward solver (forward E, forward B, node B refresh) per universe
+    in the batched form against the oracle."""
+    us = ensemble([(4, 4, 4), (6, 6, 6)], seed0=720, species=((-1.0 / 12, -1.0), (1.0 / 12, 0.01)))
+    cfg = abi.Config.make(precision=abi.FP64, mover=abi.MOVER_FIELD, solver=abi.SOLVER_FORWARD,
+                          projector=abi.PROJECT_CIC, bc=abi.BC_PERIODIC, flags=abi.F_TRACK_IDS)
+    with Batch([u[0] for u in us], cfg) as batch:
+        for i, u in enumerate(us):
+            load(batch.universe(i), u)
+        batch.step(5)
+        for i, u in enumerate(us):
+            orc = OracleSim(u[0], cfg)
+            load(orc, u)
+            orc.step(5)
+            a, b = align_by_id(batch.universe(i).download_particles(), orc.download_particles())
+            assert_states_close(a, b, rtol=1e-9, atol=1e-11, what="universe %d" % i)
+            (f1, b1, _, _), (f2, b2, _, _) = batch.universe(i).download_fields(), orc.download_fields()
+            np.testing.assert_allclose(f1, f2, rtol=1e-9, atol=1e-12)
+            np.testing.assert_allclose(b1, b2, rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("solver", [abi.SOLVER_LEAPFROG, abi.SOLVER_FORWARD])
+def test_batch_fp32_self_consistent_fields_against_oracle(solver):
+    """FP32 batched form with self-consistent fields (the cell polynomials
+    rebuilt from the solved fields every step) against the FP64 oracle:
+    every particle within 1e-4 cell widths, kinetic energy within 1e-5."""
+    us = ensemble([(4, 4, 4), (6, 6, 6)], seed0=740, ppc=16, vscale=0.01,
+                  species=((-1.0 / 16, -1.0), (1.0 / 16, 0.01)))
+    flags = abi.F_TRACK_IDS | (abi.F_REFRESH_NODE_B if solver == abi.SOLVER_LEAPFROG else 0)
+    kw = dict(mover=abi.MOVER_FIELD, solver=solver, projector=abi.PROJECT_CIC, bc=abi.BC_PERIODIC, flags=flags)
+    with Batch([u[0] for u in us], abi.Config.make(precision=abi.FP32, **kw)) as batch:
+        for i, u in enumerate(us):
+            load(batch.universe(i), u)
+        batch.step(10)
+        for i, u in enumerate(us):
+            orc = OracleSim(u[0], abi.Config.make(precision=abi.FP64, **kw))
+            load(orc, u)
+            orc.step(10)
+            c1, c2 = batch.universe(i).conserved(), orc.conserved()
+            assert c1["particles"] == c2["particles"]
+            assert abs(c1["kinetic_energy"] - c2["kinetic_energy"]) <= 1e-5 * abs(c2["kinetic_energy"])
+            # matched by id (an FP32 rounding may carry a particle across a face)
+            pa, _, ia = batch.universe(i).download_particles()
+            pb, _, ib = orc.download_particles()
+            ka, kb = np.argsort(ia), np.argsort(ib)
+            np.testing.assert_array_equal(ia[ka], ib[kb])
+            d = np.abs(pa["position"][ka] - pb["position"][kb]).max()
+            assert d < 1e-4, (i, d)
