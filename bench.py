@@ -154,11 +154,11 @@ def measured_peak():
 
 
 # DRAM bytes (read + write) per push launch on the headline workload, from
-# one ncu capture of each kernel (the committed summaries under profiles/
-# give the command); a citation of that capture, not a measurement of this
+# one ncu capture of each kernel (k_push32_pipe with the push shape 256, 32,
+# 2; k_push<double>); a citation of that capture, not a measurement of this
 # run. FP32: one launch for both species; FP64: one launch per species.
-PUSH_TRAFFIC = {"fp32": (436869120, "ncu capture, profiles/k_push32_pipe_dipole32.md"),
-                "fp64": (369767168, "ncu capture, profiles/k_push64_dipole32.md")}
+PUSH_TRAFFIC = {"fp32": (436869120, "ncu capture of k_push32_pipe<3, 2, 15> on this workload (cited, not of this run)"),
+                "fp64": (369767168, "ncu capture of k_push<double> on this workload (cited, not of this run)")}
 
 
 def combine_ranks(ms, psteps, dist, device):
@@ -235,8 +235,8 @@ def push_roofline(sim, precision, nsteps, props, pops, headline=True):
     and written once (12 x 4 B FP32, 12 x 8 B FP64), the per-cell field
     coefficients read once (FP32: 48 floats per cell) or the node E, B read
     once (FP64: 48 B per node), and the 4 FP64 node moments written once
-    (32 B per node). The ncu DRAM traffic in `profiles/` is the headline
-    workload's: other workloads report traffic null."""
+    (32 B per node). The cited ncu DRAM traffic is the headline workload's:
+    other workloads report traffic null."""
     sim.profile(True)
     sim.step(nsteps)
     prof = sim.profile_read(reset=True)
