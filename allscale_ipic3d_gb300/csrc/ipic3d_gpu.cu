@@ -951,8 +951,10 @@ int download_device(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, ipic3d_part
         g.origin[a] = ctx->props.origin[a];
         g.w[a] = ctx->props.cell_width[a];
     }
-    // chunks of about 16 MB of records, cut at cell boundaries
-    const int64_t chunk = std::max<int64_t>(1, (int64_t)(16u << 20) / (int64_t)sizeof(ipic3d_particle));
+    // chunks of about 64 MB of records, cut at cell boundaries: few enough
+    // that enqueueing them (a pack kernel, an event and a copy each) costs
+    // little host time, which otherwise delays the caller's next upload
+    const int64_t chunk = std::max<int64_t>(1, (int64_t)(64u << 20) / (int64_t)sizeof(ipic3d_particle));
     cudaStream_t cs = ctx->dl_stream;
     auto* stage = static_cast<ipic3d_particle*>(ctx->st_dl);
     auto* stage_xyz = static_cast<double*>(ctx->st_dl);  // positions only: 3 doubles per particle
