@@ -117,10 +117,20 @@ __device__ __forceinline__ float2 poly32x2(const float4& c01, const float4& c23,
 // Ey, Ez, Bx, By, Bz) within a cell's 48: components in pairs (Ex, Ey),
 // (Bx, By), (Ez, Bz) -- the pairs the mover works on -- each pair's
 // coefficients interleaved.
-__host__ __device__ constexpr int coef_pair(int q) { return q == 2 ? 2 : (q == 5 ? 2 : q / 3); }
-__host__ __device__ constexpr int coef_index(int q, int m) {
-    return coef_pair(q) * 16 + m * 2 + (q == 5 ? 1 : (q == 2 ? 0 : q % 3));
+__host__ __device__ constexpr int coef_pair(int q) { return q == 2 || q == 5 ? 2 : q / 3; }
+__host__ __device__ constexpr int coef_slot(int q) { return q == 5 ? 1 : (q == 2 ? 0 : q % 3); }
+__host__ __device__ constexpr int coef_index(int q, int m) { return coef_pair(q) * 16 + m * 2 + coef_slot(q); }
+// The inverse: component and monomial stored at position p of a cell's 48.
+__host__ __device__ constexpr int coef_comp(int p) {
+    return p / 16 == 0 ? (p % 2) : (p / 16 == 1 ? 3 + p % 2 : (p % 2 ? 5 : 2));
 }
+__host__ __device__ constexpr int coef_mono(int p) { return (p % 16) / 2; }
+constexpr bool coef_layout_is_a_bijection() {
+    for (int p = 0; p < 48; ++p)
+        if (coef_index(coef_comp(p), coef_mono(p)) != p) return false;
+    return true;
+}
+static_assert(coef_layout_is_a_bijection(), "coef_index and its inverse disagree");
 
 // E and B of a particle from its cell's polynomial coefficients (kSmem:
 // staged in shared memory; else read from global memory).
@@ -135,8 +145,8 @@ __device__ __forceinline__ void fields_one(const float* __restrict__ coef, const
         const float4 c45 = kSmem ? c4[4 * q + 2] : __ldg(c4 + 4 * q + 2);
         const float4 c67 = kSmem ? c4[4 * q + 3] : __ldg(c4 + 4 * q + 3);
         const float2 e = poly32x2(c01, c23, c45, c67, x, y, z);
-        E[q == 2 ? 2 : 3 * q] = e.x;
-        E[q == 2 ? 5 : 3 * q + 1] = e.y;
+        E[coef_comp(16 * q)] = e.x;
+        E[coef_comp(16 * q + 1)] = e.y;
     }
 }
 
@@ -417,14 +427,11 @@ __global__ void k_cell_coef32(const float4* __restrict__ n32, int sx, int sy, in
             m[q][4] = m4 * scale; m[q][5] = m5 * scale; m[q][6] = m6 * scale; m[q][7] = m7 * scale;
         }
         float4* out = reinterpret_cast<float4*>(coef + c * 48);
-        constexpr int kPair[3][2] = {{0, 1}, {3, 4}, {2, 5}};  // coef_pair's order
 #pragma unroll
-        for (int P = 0; P < 3; ++P)
-#pragma unroll
-            for (int k = 0; k < 8; k += 2) {
-                const int a = kPair[P][0], b = kPair[P][1];
-                out[P * 4 + k / 2] = make_float4(m[a][k], m[b][k], m[a][k + 1], m[b][k + 1]);
-            }
+        for (int v = 0; v < 12; ++v)
+            out[v] = make_float4(m[coef_comp(4 * v)][coef_mono(4 * v)], m[coef_comp(4 * v + 1)][coef_mono(4 * v + 1)],
+                                 m[coef_comp(4 * v + 2)][coef_mono(4 * v + 2)],
+                                 m[coef_comp(4 * v + 3)][coef_mono(4 * v + 3)]);
     }
 }
 
