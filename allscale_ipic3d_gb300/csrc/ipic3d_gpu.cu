@@ -894,13 +894,15 @@ int download_device(ipic3d_ctx* ctx, std::vector<PopStore<T>>& pops, ipic3d_part
     CU(cudaStreamSynchronize(st));
     std::vector<std::vector<Mover<T>>> pend(npop);
     std::vector<int32_t> pcell;  // waiting particles per (population, cell), if any
+    bool waiting = false;
     for (int k = 0; k < npop; ++k) {
         if (!npend[k]) continue;
         pend[k].resize(npend[k]);
         CU(cudaMemcpyAsync(pend[k].data(), pops[k].pending_in, npend[k] * sizeof(Mover<T>), cudaMemcpyDeviceToHost,
                            st));
+        waiting = true;
     }
-    CU(cudaStreamSynchronize(st));
+    if (waiting) CU(cudaStreamSynchronize(st));
     for (int k = 0; k < npop; ++k)
         for (const auto& m : pend[k]) {
             if (m.cell < 0 || m.cell >= nc) return fail(IPIC3D_E_STATE, "waiting particle in cell %d", m.cell);
